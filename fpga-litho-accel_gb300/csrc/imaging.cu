@@ -1,0 +1,775 @@
+// FP32 imaging pipeline: mask -> spectrum window -> SOCS intensity band -> image.
+//
+// The reference computes (litho.cpp:1318-1451)
+//   mskf  = fftshift(FFT2(ifftshift(pad(mask)))) / (Fx*Fy)          FT_r2c_padded
+//   tmpImg = sum_k s_k |IFFT_N(embed(K_k * mskf_window))|^2          calcSOCS kernel loop
+//   image = crop(roll(C2R_F(zero-pad(R2C_N(tmpImg)/N^2))))           FI + crop
+// Only the (2Ny+1)x(2Nx+1) window of mskf around DC reaches the kernels, and the
+// intensity is band-limited to |f| <= 2N, so this file computes exactly those
+// pieces and nothing else:
+//
+//   win_dft_kernel : W[v][u] = 1/(FxFy) sum_{y,x} m[y][x] e^{-2 pi i (u x'/Fx + v y'/Fy)}
+//                    (x' = x + (Fx-Lx)/2 - Fx/2).  A separable partial DFT: the
+//                    column stage is a 128 x Lx x (2Nx+1) FP32 contraction per CTA
+//                    with the mask tile staged in shared memory, the row stage a
+//                    small complex contraction in the epilogue.  HBM: one read of
+//                    the mask.
+//   socs_kernel    : per kernel k, embed K_k*W in an N x N grid, 2-D inverse FFT
+//                    (warp-shuffle radix-2, fft_warp.cuh), accumulate s_k|E|^2 in
+//                    registers; then a forward FFT of the intensity and the
+//                    |f| <= 2N band S[fy][fx] / N^2 is written out.
+//   fi_prep_kernel : T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx}   (fy >= 0)
+//   fi_out_kernel  : image[Y][X] = T0 + 2 sum_{fy>0} Re(e^{2 pi i fy y'/Fy} T[fy][X]),
+//                    a rank-(4Ny+1) FP32 contraction written once with 16-byte
+//                    streaming stores.  HBM: one write of the image.
+// With C2R's Hermitian completion and the two rolls of litho.cpp:934 and
+// litho.cpp:700, that is exactly FI's zero-padded interpolation followed by
+// crop2DCentered (litho.cpp:164-177, 997-1001).
+#include "litho_internal.cuh"
+#include "fft_warp.cuh"
+
+#include <algorithm>
+
+namespace litho {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int pmod(long long a, int m) {
+  long long r = a % m;
+  return (int)(r < 0 ? r + m : r);
+}
+
+// exp(sign * 2 pi i * m / F) for an exact integer phase m (the argument of
+// sincospif is exact because F is a power of two).
+__device__ __forceinline__ float2 cis_exact(long long m, int F, float sign) {
+  const int r = pmod(m, F);
+  float s, c;
+  sincospif(2.0f * (float)r / (float)F, &s, &c);
+  return make_float2(c, sign * s);
+}
+
+// ---------------------------------------------------------------------------
+// window DFT column twiddles: twx[x][j], j in [0, NJT):
+//   j <= Nx          : cos(2 pi j x'/Fx)
+//   Nx < j <= 2Nx    : -sin(2 pi (j-Nx) x'/Fx)
+//   otherwise 0 (padding to a multiple of 4)
+// ---------------------------------------------------------------------------
+__global__ void twx_init_kernel(float* __restrict__ twx, int Lx, int Fx, int Nx, int NJT) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= Lx) return;
+  const long long xp = (long long)x + (Fx - Lx) / 2 - Fx / 2;
+  for (int j = 0; j < NJT; ++j) {
+    float v = 0.f;
+    if (j <= 2 * Nx) {
+      const int u = j <= Nx ? j : j - Nx;
+      long long m = ((long long)u * xp) % Fx;
+      if (m < 0) m += Fx;
+      double s, c;
+      sincospi(2.0 * (double)m / (double)Fx, &s, &c);
+      v = j <= Nx ? (float)c : (float)(-s);
+    }
+    twx[(size_t)x * NJT + j] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// window DFT
+// ---------------------------------------------------------------------------
+constexpr int WD_BM = 128;     // mask rows per CTA
+constexpr int WD_BK = 64;      // mask columns per shared-memory chunk
+constexpr int WD_SA = WD_BM + 1;
+constexpr int WD_THREADS = 256;
+
+template <int NJT>
+constexpr size_t win_dft_smem(int Ny) {
+  return 0;  // computed on the host (see run_win_dft)
+}
+
+template <int NJT, bool VEC>
+__global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __restrict__ masks, int Lx, int Ly,
+                                                             int Fx, int Fy, int Nx, int Ny,
+                                                             const float* __restrict__ twx,
+                                                             float2* __restrict__ win_part) {
+  extern __shared__ __align__(16) float sm[];
+  float* sA = sm;                    // [WD_BK][WD_SA]   mask chunk, transposed
+  float* sB = sA + WD_BK * WD_SA;    // [WD_BK][NJT]     column twiddles of the chunk
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rb = blockIdx.x, cs = blockIdx.y, img = blockIdx.z;
+  const int colSplits = gridDim.y;
+  const int nparts = gridDim.x * gridDim.y;
+  const int part = rb * colSplits + cs;
+  const int y0 = rb * WD_BM;
+  const int nch = (Lx + WD_BK - 1) / WD_BK;
+  const int ch0 = (int)((long long)nch * cs / colSplits);
+  const int ch1 = (int)((long long)nch * (cs + 1) / colSplits);
+  const float* M = masks + (size_t)img * Lx * Ly;
+
+  float acc[4][NJT];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < NJT; ++j) acc[i][j] = 0.f;
+
+  float4 ra[8];
+  const int lc4 = (tid & 15) * 4;
+  const int lr = tid >> 4;
+  auto loadA = [&](int ch) {
+    const int x0 = ch * WD_BK + lc4;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = y0 + lr + 16 * i;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row < Ly) {
+        const float* p = M + (size_t)row * Lx + x0;
+        if (VEC && x0 + 3 < Lx) {
+          v = __ldcs(reinterpret_cast<const float4*>(p));
+        } else {
+          if (x0 + 0 < Lx) v.x = p[0];
+          if (x0 + 1 < Lx) v.y = p[1];
+          if (x0 + 2 < Lx) v.z = p[2];
+          if (x0 + 3 < Lx) v.w = p[3];
+        }
+      }
+      ra[i] = v;
+    }
+  };
+
+  if (ch0 < ch1) loadA(ch0);
+  for (int ch = ch0; ch < ch1; ++ch) {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = lr + 16 * i;
+      sA[(lc4 + 0) * WD_SA + r] = ra[i].x;
+      sA[(lc4 + 1) * WD_SA + r] = ra[i].y;
+      sA[(lc4 + 2) * WD_SA + r] = ra[i].z;
+      sA[(lc4 + 3) * WD_SA + r] = ra[i].w;
+    }
+    {
+      const float4* T4 = reinterpret_cast<const float4*>(twx);
+      float4* sB4 = reinterpret_cast<float4*>(sB);
+      const int q = NJT / 4;
+      for (int idx = tid; idx < WD_BK * q; idx += WD_THREADS) {
+        const int kr = idx / q, c = idx - kr * q;
+        const int x = ch * WD_BK + kr;
+        sB4[idx] = x < Lx ? T4[(size_t)x * q + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    if (ch + 1 < ch1) loadA(ch + 1);
+#pragma unroll 2
+    for (int kk = 0; kk < WD_BK / 8; ++kk) {
+      const int k = warp * (WD_BK / 8) + kk;
+      const float* a = sA + k * WD_SA + lane;
+      const float a0 = a[0], a1 = a[32], a2 = a[64], a3 = a[96];
+      const float4* b4 = reinterpret_cast<const float4*>(sB + k * NJT);
+#pragma unroll
+      for (int c = 0; c < NJT / 4; ++c) {
+        const float4 b = b4[c];
+        const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          acc[0][4 * c + e] = fmaf(a0, bb[e], acc[0][4 * c + e]);
+          acc[1][4 * c + e] = fmaf(a1, bb[e], acc[1][4 * c + e]);
+          acc[2][4 * c + e] = fmaf(a2, bb[e], acc[2][4 * c + e]);
+          acc[3][4 * c + e] = fmaf(a3, bb[e], acc[3][4 * c + e]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // tree reduction of the 8 k-split warps: red[w][j][r], r fastest (conflict free)
+  float* red = sm;
+  for (int s = 4; s >= 1; s >>= 1) {
+    if (warp >= s && warp < 2 * s) {
+      float* dst = red + (size_t)(warp - s) * NJT * WD_BM;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < NJT; ++j) dst[j * WD_BM + lane + 32 * i] = acc[i][j];
+    }
+    __syncthreads();
+    if (warp < s) {
+      const float* src = red + (size_t)warp * NJT * WD_BM;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < NJT; ++j) acc[i][j] += src[j * WD_BM + lane + 32 * i];
+    }
+    __syncthreads();
+  }
+  float* sR = red;  // [NJT][WD_BM] row transforms of this block
+  if (warp == 0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < NJT; ++j) sR[j * WD_BM + lane + 32 * i] = acc[i][j];
+  }
+  // row twiddles e^{-2 pi i v y'/Fy}, v = 0..Ny
+  float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NJT * WD_BM);
+  const int oyc = (Fy - Ly) / 2 - Fy / 2;
+  for (int idx = tid; idx < (Ny + 1) * WD_BM; idx += WD_THREADS) {
+    const int v = idx / WD_BM, r = idx - v * WD_BM;
+    sRT[idx] = cis_exact((long long)v * (y0 + r + oyc), Fy, -1.f);
+  }
+  __syncthreads();
+
+  const int KY = 2 * Ny + 1, NU = Nx + 1;
+  const float scale = 1.0f / ((float)Fx * (float)Fy);
+  float2* out = win_part + ((size_t)img * nparts + part) * KY * NU;
+  for (int o = tid; o < KY * NU; o += WD_THREADS) {
+    const int vi = o / NU, u = o - vi * NU;
+    const int v = vi - Ny;
+    const int av = v < 0 ? -v : v;
+    const float ts = v < 0 ? -1.f : 1.f;
+    const float* rc = sR + u * WD_BM;
+    const float* rs = sR + (Nx + u) * WD_BM;
+    const float2* rt = sRT + av * WD_BM;
+    float re = 0.f, im = 0.f;
+    if (u == 0) {
+#pragma unroll 4
+      for (int r = 0; r < WD_BM; ++r) {
+        const float2 t = rt[r];
+        re = fmaf(rc[r], t.x, re);
+        im = fmaf(rc[r], ts * t.y, im);
+      }
+    } else {
+#pragma unroll 4
+      for (int r = 0; r < WD_BM; ++r) {
+        const float2 t = rt[r];
+        const float ty = ts * t.y;
+        re = fmaf(rc[r], t.x, fmaf(-rs[r], ty, re));
+        im = fmaf(rc[r], ty, fmaf(rs[r], t.x, im));
+      }
+    }
+    out[o] = make_float2(re * scale, im * scale);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SOCS: K inverse FFTs on the N x N conv grid, intensity accumulation in
+// registers, forward FFT of the intensity, band output.
+// ---------------------------------------------------------------------------
+constexpr int SOCS_THREADS = 256;
+
+template <int N>
+__global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
+    const float2* __restrict__ win_part, int nparts, const float* __restrict__ mskf_r,
+    const float* __restrict__ mskf_i, int Fx, int Fy, int Nx, int Ny, const float2* __restrict__ krn,
+    const float* __restrict__ scales, int nk, int kpg, float2* __restrict__ band_part,
+    float* __restrict__ tmpImgp) {
+  constexpr int J = N / 32, SG = N + 1, CPW = N / 8;
+  extern __shared__ __align__(16) float2 sg[];
+  float2* grid = sg;             // [N][SG]
+  float2* tw = grid + N * SG;    // [N/2]
+  float2* win = tw + N / 2;      // [KY][KX]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = blockIdx.x, img = blockIdx.y, ngroups = gridDim.x;
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
+
+  for (int e = tid; e < N / 2; e += SOCS_THREADS) {
+    float s, c;
+    sincospif(2.0f * (float)e / (float)N, &s, &c);
+    tw[e] = make_float2(c, -s);
+  }
+  for (int idx = tid; idx < KD; idx += SOCS_THREADS) {
+    const int ky = idx / KX, kx = idx - ky * KX;
+    const int v = ky - Ny, u = kx - Nx;
+    float2 w;
+    if (mskf_r != nullptr) {
+      const size_t off = (size_t)img * Fx * Fy + (size_t)(Fy / 2 + v) * Fx + (Fx / 2 + u);
+      w = make_float2(mskf_r[off], mskf_i[off]);
+    } else {
+      const bool neg = u < 0;
+      const int vv = neg ? -v : v, uu = neg ? -u : u;
+      const float2* P = win_part + (size_t)img * nparts * KY * (Nx + 1) + (size_t)(vv + Ny) * (Nx + 1) + uu;
+      float re = 0.f, im = 0.f;
+      for (int p = 0; p < nparts; ++p) {
+        const float2 t = P[(size_t)p * KY * (Nx + 1)];
+        re += t.x;
+        im += t.y;
+      }
+      w = make_float2(re, neg ? -im : im);
+    }
+    win[idx] = w;
+  }
+  for (int i = tid; i < N * SG; i += SOCS_THREADS) grid[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+
+  const int ex = (N - KX) / 2, ey = (N - KY) / 2;
+  float acc[CPW][J];
+#pragma unroll
+  for (int m = 0; m < CPW; ++m)
+#pragma unroll
+    for (int j = 0; j < J; ++j) acc[m][j] = 0.f;
+
+  const int k0 = g * kpg, k1 = min(nk, k0 + kpg);
+  for (int k = k0; k < k1; ++k) {
+    const float2* K = krn + (size_t)k * KD;
+    const float lam = scales[k];
+    for (int ky = warp; ky < KY; ky += 8) {
+      float2 x[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const int kx = lane + 32 * j - ex;
+        x[j] = (kx >= 0 && kx < KX) ? cmul(K[ky * KX + kx], win[ky * KX + kx]) : make_float2(0.f, 0.f);
+      }
+      warp_fft_dif<N, true>(x, tw, lane);
+#pragma unroll
+      for (int j = 0; j < J; ++j) grid[(ey + ky) * SG + lane + 32 * j] = x[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < CPW; ++m) {
+      const int c = warp + 8 * m;
+      float2 x[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) x[j] = grid[(lane + 32 * j) * SG + c];
+      warp_fft_dif<N, true>(x, tw, lane);
+#pragma unroll
+      for (int j = 0; j < J; ++j) acc[m][j] = fmaf(lam, fmaf(x[j].x, x[j].x, x[j].y * x[j].y), acc[m][j]);
+    }
+    __syncthreads();
+  }
+
+  if (tmpImgp != nullptr) {
+    // litho.cpp:934 myShift(tmpImg -> tmpImgp, fftshift); positions are bit-reversed
+    float* T = tmpImgp + (size_t)img * N * N;
+#pragma unroll
+    for (int m = 0; m < CPW; ++m) {
+      const int xs = bitrev<N>(warp + 8 * m);
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const int ys = bitrev<N>(lane + 32 * j);
+        T[((ys + N / 2) & (N - 1)) * N + ((xs + N / 2) & (N - 1))] = acc[m][j];
+      }
+    }
+  }
+
+  // forward transform of the intensity: columns (DIT, bit-reversed in -> natural out)
+#pragma unroll
+  for (int m = 0; m < CPW; ++m) {
+    const int c = warp + 8 * m;
+    float2 x[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) x[j] = make_float2(acc[m][j], 0.f);
+    warp_fft_dit<N, false>(x, tw, lane);
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int fy = lane + 32 * j;
+      if (fy <= 2 * Ny) grid[fy * SG + c] = x[j];
+    }
+  }
+  __syncthreads();
+  const int BW = 4 * Nx + 1;
+  const float inv = 1.0f / ((float)N * (float)N);
+  float2* band = band_part + ((size_t)img * ngroups + g) * KY * BW;
+  for (int fy = warp; fy <= 2 * Ny; fy += 8) {
+    float2 x[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) x[j] = grid[fy * SG + lane + 32 * j];
+    warp_fft_dit<N, false>(x, tw, lane);
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int fx = lane + 32 * j;
+      int d = 1 << 30;
+      if (fx <= 2 * Nx) d = fx;
+      else if (fx >= N - 2 * Nx) d = fx - N;
+      if (d != (1 << 30)) band[fy * BW + d + 2 * Nx] = cscale(x[j], inv);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FI, step 1: T[fy][X] for fy = 0..2Ny (T[-fy] = conj(T[fy]) because the
+// intensity is real).  tm layout per image: row 0 = Re T0, rows 1..2Ny = Re T,
+// rows 2Ny+1..4Ny = Im T; Lx columns.
+// ---------------------------------------------------------------------------
+constexpr int FIP_THREADS = 256;
+
+__global__ void __launch_bounds__(FIP_THREADS) fi_prep_kernel(const float2* __restrict__ band_part, int ngroups,
+                                                              int Lx, int Fx, int Nx, int Ny,
+                                                              float* __restrict__ tm) {
+  extern __shared__ __align__(16) float2 fs[];
+  const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
+  float2* sS = fs;                 // [BH][BW]
+  float2* sT = fs + BH * BW;       // [ND][FIP_THREADS]
+  const int tid = threadIdx.x, img = blockIdx.y;
+  const float2* B = band_part + (size_t)img * ngroups * BH * BW;
+  for (int idx = tid; idx < BH * BW; idx += FIP_THREADS) {
+    float re = 0.f, im = 0.f;
+    for (int gi = 0; gi < ngroups; ++gi) {
+      const float2 t = B[(size_t)gi * BH * BW + idx];
+      re += t.x;
+      im += t.y;
+    }
+    sS[idx] = make_float2(re, im);
+  }
+  const int X = blockIdx.x * FIP_THREADS + tid;
+  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
+  for (int d = 0; d < ND; ++d) sT[d * FIP_THREADS + tid] = cis_exact((long long)d * xp, Fx, 1.f);
+  __syncthreads();
+  if (X >= Lx) return;
+  float* out = tm + (size_t)img * (4 * Ny + 1) * Lx;
+  for (int fy = 0; fy < BH; ++fy) {
+    const float2* S = sS + fy * BW + 2 * Nx;
+    float re = S[0].x, im = S[0].y;
+    for (int d = 1; d < ND; ++d) {
+      const float2 t = sT[d * FIP_THREADS + tid];
+      const float2 p = S[d], q = S[-d];
+      // p * t + q * conj(t)
+      re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
+      im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+    }
+    if (fy == 0) {
+      out[X] = re;
+    } else {
+      out[(size_t)fy * Lx + X] = re;
+      out[(size_t)(2 * Ny + fy) * Lx + X] = im;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FI, step 2: image = Cy (Ly x KB) * Tm (KB x Lx), KB = 4Ny+1.
+// ---------------------------------------------------------------------------
+constexpr int FO_BM = 64, FO_BN = 128, FO_THREADS = 256;
+
+template <bool VEC>
+__global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restrict__ tm, int Lx, int Ly, int Fy,
+                                                            int Ny, float* __restrict__ images) {
+  extern __shared__ __align__(16) float fo[];
+  const int KB = 4 * Ny + 1;
+  float* sC = fo;                // [KB][FO_BM]
+  float* sT = fo + KB * FO_BM;   // [KB][FO_BN]
+  const int tid = threadIdx.x;
+  const int X0 = blockIdx.x * FO_BN, Y0 = blockIdx.y * FO_BM, img = blockIdx.z;
+  const float* T = tm + (size_t)img * KB * Lx;
+  for (int idx = tid; idx < KB * FO_BN; idx += FO_THREADS) {
+    const int r = idx / FO_BN, c = idx - r * FO_BN;
+    const int X = X0 + c;
+    sT[idx] = X < Lx ? T[(size_t)r * Lx + X] : 0.f;
+  }
+  const long long yoff = (long long)(Fy - Ly) / 2 - Fy / 2;
+  for (int idx = tid; idx < KB * FO_BM; idx += FO_THREADS) {
+    const int r = idx / FO_BM, rr = idx - r * FO_BM;
+    const long long yp = (long long)(Y0 + rr) + yoff;
+    float v = 1.f;
+    if (r > 0) {
+      const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
+      const float2 e = cis_exact((long long)dy * yp, Fy, 1.f);
+      v = r <= 2 * Ny ? 2.f * e.x : -2.f * e.y;
+    }
+    sC[idx] = v;
+  }
+  __syncthreads();
+  const int ty = tid >> 4, tx = tid & 15;
+  float acc[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+  for (int r = 0; r < KB; ++r) {
+    const float4 c = *reinterpret_cast<const float4*>(sC + r * FO_BM + 4 * ty);
+    const float4 t0 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 4 * tx);
+    const float4 t1 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 64 + 4 * tx);
+    const float cc[4] = {c.x, c.y, c.z, c.w};
+    const float tt[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(cc[i], tt[j], acc[i][j]);
+  }
+  float* O = images + (size_t)img * Lx * Ly;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int Y = Y0 + 4 * ty + i;
+    if (Y >= Ly) continue;
+    float* row = O + (size_t)Y * Lx;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int X = X0 + 64 * h + 4 * tx;
+      if (VEC && X + 3 < Lx) {
+        __stcs(reinterpret_cast<float4*>(row + X),
+               make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]));
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (X + e < Lx) row[X + e] = acc[i][4 * h + e];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Full centred mask spectrum (litho_fft_mask): two passes of a block FFT over
+// shared-memory rows, each pass writing its result transposed.
+//   C[X] = sum_p a[p] e^{-2 pi i (X - F/2)(p - F/2)/F}
+//        = (-1)^(X + F/2) * DFT((-1)^p a[p])[X]
+// ---------------------------------------------------------------------------
+constexpr int FM_THREADS = 256;
+
+// rows: `nrows` input rows of length `len` (real if in_i == nullptr), padded
+// centred into F; output written transposed: out[X][row] (row stride ldo).
+__global__ void __launch_bounds__(FM_THREADS) fft_rows_centred_kernel(
+    const float* __restrict__ in_r, const float* __restrict__ in_i, const float2* __restrict__ in_c,
+    int nrows, int len, int F, int TR, float scale, float2* __restrict__ out_c, float* __restrict__ out_r,
+    float* __restrict__ out_i, int ldo) {
+  extern __shared__ __align__(16) float2 fr[];
+  const int SF = F + 1;
+  float2* s = fr;                 // [TR][SF]
+  float2* tw = fr + TR * SF;      // [F/2]
+  const int tid = threadIdx.x;
+  const int r0 = blockIdx.x * TR;
+  const int logF = 31 - __clz(F);
+  const int off = (F - len) / 2;
+  for (int e = tid; e < F / 2; e += FM_THREADS) {
+    float sn, cs;
+    sincospif(2.0f * (float)e / (float)F, &sn, &cs);
+    tw[e] = make_float2(cs, -sn);
+  }
+  // load with bit-reversed placement, pre-multiplied by (-1)^p
+  for (int idx = tid; idx < TR * F; idx += FM_THREADS) {
+    const int r = idx / F, p = idx - r * F;
+    const int row = r0 + r;
+    float2 v = make_float2(0.f, 0.f);
+    const int q = p - off;
+    if (row < nrows && q >= 0 && q < len) {
+      const size_t o = (size_t)row * len + q;
+      if (in_c) v = in_c[o];
+      else v = make_float2(in_r[o], in_i ? in_i[o] : 0.f);
+      if (p & 1) v = make_float2(-v.x, -v.y);
+    }
+    const int br = (int)(__brev((unsigned)p) >> (32 - logF));
+    s[r * SF + br] = v;
+  }
+  __syncthreads();
+  for (int h = 1; h < F; h <<= 1) {
+    for (int idx = tid; idx < TR * (F / 2); idx += FM_THREADS) {
+      const int r = idx / (F / 2), b = idx - r * (F / 2);
+      const int grp = b / h, pos = b - grp * h;
+      const int i0 = grp * 2 * h + pos, i1 = i0 + h;
+      const float2 w = tw[pos * (F / (2 * h))];
+      float2* rowp = s + r * SF;
+      const float2 t = cmul(w, rowp[i1]);
+      const float2 a = rowp[i0];
+      rowp[i0] = cadd(a, t);
+      rowp[i1] = csub(a, t);
+    }
+    __syncthreads();
+  }
+  // transposed write with (-1)^(X + F/2) and scale
+  const float sgnF = ((F / 2) & 1) ? -1.f : 1.f;
+  for (int idx = tid; idx < TR * F; idx += FM_THREADS) {
+    const int X = idx / TR, r = idx - X * TR;
+    const int row = r0 + r;
+    if (row >= nrows) continue;
+    float2 v = s[r * SF + X];
+    const float sg = ((X & 1) ? -sgnF : sgnF) * scale;
+    v = make_float2(v.x * sg, v.y * sg);
+    const size_t o = (size_t)X * ldo + row;
+    if (out_c) out_c[o] = v;
+    else {
+      out_r[o] = v.x;
+      out_i[o] = v.y;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int njt_for(int Nx) {
+  const int nj = 2 * Nx + 1;
+  if (nj <= 8) return 8;
+  if (nj <= 12) return 12;
+  if (nj <= 20) return 20;
+  if (nj <= 36) return 36;
+  return -1;
+}
+
+ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count) {
+  ImgPlan p;
+  p.g = g;
+  p.batch = batch;
+  p.rowBlocks = (g.Ly + WD_BM - 1) / WD_BM;
+  const int nch = (g.Lx + WD_BK - 1) / WD_BK;
+  const int want = 2 * sm_count;
+  int cs = (want + p.rowBlocks * batch - 1) / (p.rowBlocks * batch);
+  cs = std::max(1, std::min(cs, std::max(1, nch / 2)));
+  p.colSplits = cs;
+  int ng = (sm_count + batch - 1) / batch;
+  ng = std::max(1, std::min(ng, g.nk));
+  p.kpg = (g.nk + ng - 1) / ng;
+  p.ngroups = (g.nk + p.kpg - 1) / p.kpg;
+  return p;
+}
+
+static int twx_table(litho_ctx* ctx, int Lx, int Fx, int Nx, int NJT, const float** out) {
+  auto key = std::make_tuple(Lx, Fx, Nx, NJT);
+  auto it = ctx->twx_tables.find(key);
+  if (it == ctx->twx_tables.end()) {
+    DevBuf b;
+    LITHO_RET(b.ensure(ctx, (size_t)Lx * NJT * sizeof(float)));
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    twx_init_kernel<<<(Lx + 127) / 128, 128, 0, ctx->stream>>>(b.as<float>(), Lx, Fx, Nx, NJT);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    it = ctx->twx_tables.emplace(key, b).first;
+  }
+  *out = it->second.as<float>();
+  return LITHO_OK;
+}
+
+template <int NJT>
+static int launch_win_dft_t(litho_ctx* ctx, const ImgPlan& p, const float* masks, const float* twx,
+                            float2* win_part) {
+  const ImgGeom& g = p.g;
+  const size_t main_sm = (size_t)(WD_BK * WD_SA + WD_BK * NJT) * sizeof(float);
+  const size_t red_sm = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(g.Ny + 1) * WD_BM * sizeof(float2);
+  const size_t smem = std::max(main_sm, red_sm);
+  dim3 grid(p.rowBlocks, p.colSplits, p.batch);
+  StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
+  if ((g.Lx & 3) == 0) {
+    auto k = win_dft_kernel<NJT, true>;
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+  } else {
+    auto k = win_dft_kernel<NJT, false>;
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+  }
+  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  return LITHO_OK;
+}
+
+int run_win_dft(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
+  const int NJT = njt_for(p.g.Nx);
+  if (NJT < 0) {
+    set_error(ctx, LITHO_ERR_UNSUPPORTED, "window DFT supports Nx <= 16 (got %d)", p.g.Nx);
+    return LITHO_ERR_UNSUPPORTED;
+  }
+  const float* twx = nullptr;
+  LITHO_RET(twx_table(ctx, p.g.Lx, p.g.Fx, p.g.Nx, NJT, &twx));
+  switch (NJT) {
+    case 8: return launch_win_dft_t<8>(ctx, p, masks, twx, win_part);
+    case 12: return launch_win_dft_t<12>(ctx, p, masks, twx, win_part);
+    case 20: return launch_win_dft_t<20>(ctx, p, masks, twx, win_part);
+    default: return launch_win_dft_t<36>(ctx, p, masks, twx, win_part);
+  }
+}
+
+template <int N>
+static int launch_socs_t(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2* krn,
+                         const float* scales, float2* band_part, float* tmpImgp) {
+  const ImgGeom& g = p.g;
+  const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
+  const size_t smem = ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = socs_kernel<N>;
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(p.ngroups, p.batch);
+  StageScope sc(ctx, LITHO_STAGE_SOCS);
+  k<<<grid, SOCS_THREADS, smem, ctx->stream>>>(w.part, w.nparts, w.mskf_r, w.mskf_i, g.Fx, g.Fy, g.Nx, g.Ny, krn,
+                                                scales, g.nk, p.kpg, band_part, tmpImgp);
+  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  return LITHO_OK;
+}
+
+int run_socs(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2* krn, const float* scales,
+             float2* band_part, float* tmpImgp) {
+  if (tmpImgp != nullptr && p.ngroups != 1) {
+    set_error(ctx, LITHO_ERR_ARG, "tmpImgp output needs a single kernel group");
+    return LITHO_ERR_ARG;
+  }
+  switch (p.g.convN) {
+    case 32: return launch_socs_t<32>(ctx, p, w, krn, scales, band_part, tmpImgp);
+    case 64: return launch_socs_t<64>(ctx, p, w, krn, scales, band_part, tmpImgp);
+    case 128: return launch_socs_t<128>(ctx, p, w, krn, scales, band_part, tmpImgp);
+    default:
+      set_error(ctx, LITHO_ERR_UNSUPPORTED, "conv grid %d not in {32, 64, 128}", p.g.convN);
+      return LITHO_ERR_UNSUPPORTED;
+  }
+}
+
+int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images) {
+  const ImgGeom& g = p.g;
+  {
+    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
+    const size_t smem = ((size_t)BH * BW + (size_t)ND * FIP_THREADS) * sizeof(float2);
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((g.Lx + FIP_THREADS - 1) / FIP_THREADS, p.batch);
+    StageScope sc(ctx, LITHO_STAGE_FI_PREP);
+    fi_prep_kernel<<<grid, FIP_THREADS, smem, ctx->stream>>>(band_part, p.ngroups, g.Lx, g.Fx, g.Nx, g.Ny, tm);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  {
+    const int KB = 4 * g.Ny + 1;
+    const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);
+    dim3 grid((g.Lx + FO_BN - 1) / FO_BN, (g.Ly + FO_BM - 1) / FO_BM, p.batch);
+    StageScope sc(ctx, LITHO_STAGE_FI_OUT);
+    if ((g.Lx & 3) == 0) {
+      LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_out_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      fi_out_kernel<true><<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, images);
+    } else {
+      LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_out_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      fi_out_kernel<false><<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, images);
+    }
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  return LITHO_OK;
+}
+
+static int fm_rows_per_cta(int F) { return std::max(1, 16384 / F) > 16 ? 16 : std::max(1, 16384 / F); }
+
+int run_fft_mask(litho_ctx* ctx, const float* mask, int Lx, int Ly, float* mskf_r, float* mskf_i) {
+  const int Fx = next_pow2(Lx), Fy = next_pow2(Ly);
+  // pass 1: mask rows -> tmp[X][y] (Fx x Ly complex)
+  LITHO_RET(ctx->stage_x.ensure(ctx, (size_t)Fx * Ly * sizeof(float2)));
+  float2* tmp = ctx->stage_x.as<float2>();
+  StageScope sc(ctx, LITHO_STAGE_FFT_MASK, 2);
+  {
+    const int TR = fm_rows_per_cta(Fx);
+    const size_t smem = ((size_t)TR * (Fx + 1) + Fx / 2) * sizeof(float2);
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fft_rows_centred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fft_rows_centred_kernel<<<(Ly + TR - 1) / TR, FM_THREADS, smem, ctx->stream>>>(
+        mask, nullptr, nullptr, Ly, Lx, Fx, TR, 1.0f, tmp, nullptr, nullptr, Ly);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  // pass 2: tmp rows (one per X, length Ly) -> mskf[Y][X] / (Fx*Fy)
+  {
+    const int TR = fm_rows_per_cta(Fy);
+    const size_t smem = ((size_t)TR * (Fy + 1) + Fy / 2) * sizeof(float2);
+    const float scale = 1.0f / ((float)Fx * (float)Fy);
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fft_rows_centred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    fft_rows_centred_kernel<<<(Fx + TR - 1) / TR, FM_THREADS, smem, ctx->stream>>>(
+        nullptr, nullptr, tmp, Fx, Ly, Fy, TR, scale, nullptr, mskf_r, mskf_i, Fx);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  return LITHO_OK;
+}
+
+int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const float2* krn,
+                   const float* scales, float* images, int precision) {
+  ImgPlan p = make_plan(g, batch, ctx->sm_count);
+  const int KY = 2 * g.Ny + 1;
+  LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
+  LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));
+  LITHO_RET(ctx->tm.ensure(ctx, (size_t)batch * (4 * g.Ny + 1) * g.Lx * sizeof(float)));
+  const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
+  if (tc) {
+    p.colSplits = 1;
+    LITHO_RET(run_win_dft_tc(ctx, p, masks, ctx->win_part.as<float2>()));
+  } else {
+    LITHO_RET(run_win_dft(ctx, p, masks, ctx->win_part.as<float2>()));
+  }
+  WindowSrc w;
+  w.part = ctx->win_part.as<float2>();
+  w.nparts = p.nparts();
+  LITHO_RET(run_socs(ctx, p, w, krn, scales, ctx->band_part.as<float2>(), nullptr));
+  if (tc) return run_fi_tc(ctx, p, ctx->band_part.as<float2>(), ctx->tm.as<float>(), images);
+  return run_fi(ctx, p, ctx->band_part.as<float2>(), ctx->tm.as<float>(), images);
+}
+
+}  // namespace litho

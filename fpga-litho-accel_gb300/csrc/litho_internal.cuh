@@ -1,0 +1,163 @@
+// Internal declarations shared by the liblitho_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "../../include/litho_gb300.h"
+
+namespace litho {
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+struct Status {
+  int code = LITHO_OK;
+  std::string msg;
+};
+
+void set_error(litho_ctx* ctx, int code, const char* fmt, ...);
+
+#define LITHO_CUDA_TRY(ctx, call)                                                       \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::litho::set_error((ctx), LITHO_ERR_CUDA, "%s failed: %s (%s:%d)", #call,          \
+                         cudaGetErrorString(e_), __FILE__, __LINE__);                   \
+      return LITHO_ERR_CUDA;                                                            \
+    }                                                                                   \
+  } while (0)
+
+#define LITHO_ARG_CHECK(ctx, cond, ...)                                                 \
+  do {                                                                                  \
+    if (!(cond)) {                                                                      \
+      ::litho::set_error((ctx), LITHO_ERR_ARG, __VA_ARGS__);                            \
+      return LITHO_ERR_ARG;                                                             \
+    }                                                                                   \
+  } while (0)
+
+#define LITHO_RET(expr)             \
+  do {                              \
+    int r_ = (expr);                \
+    if (r_ != LITHO_OK) return r_;  \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// grow-only device buffer owned by a context
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(litho_ctx* ctx, size_t need);
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+inline int next_pow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+inline bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
+
+}  // namespace litho
+
+// The context.  One stream, a set of grow-only workspaces and cached tables.
+struct litho_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  // imaging workspaces
+  litho::DevBuf win_part, band_part, tm, stage_in, stage_out, stage_k, stage_s, stage_x;
+  // window-DFT column twiddle tables keyed by (Lx, Fx, Nx, NJT)
+  std::map<std::tuple<int, int, int, int>, litho::DevBuf> twx_tables;
+  // TCC / eigensolver workspaces
+  litho::DevBuf tcc_a, tcc_b, tcc_c, eig_w, eig_v, eig_work, eig_info;
+  // mixed-precision (tensor-core) workspaces
+  litho::DevBuf mx_b, mx_c, mx_d;
+  // per-stage timers
+  bool timing = false;
+  double stage_ms[LITHO_STAGE_COUNT] = {};
+  long long stage_launches[LITHO_STAGE_COUNT] = {};
+  struct Pending { int stage; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+struct litho_kernel_set {
+  litho_ctx* ctx = nullptr;
+  int nk = 0, Nx = 0, Ny = 0;
+  float2* krn = nullptr;    // [nk][(2Ny+1)(2Nx+1)]
+  float* scales = nullptr;  // [nk]
+};
+
+namespace litho {
+
+// Brackets one stage's launches with CUDA events when timing is on and counts
+// its kernel launches always.
+struct StageScope {
+  litho_ctx* ctx;
+  int stage;
+  cudaEvent_t b = nullptr;
+  StageScope(litho_ctx* c, int s, int launches = 1);
+  ~StageScope();
+};
+
+// ---------------------------------------------------------------------------
+// imaging pipeline (imaging.cu)
+// ---------------------------------------------------------------------------
+struct ImgGeom {
+  int Lx, Ly;   // physical size (image and mask)
+  int Fx, Fy;   // padded FFT size (power of two >= L)
+  int Nx, Ny;   // kernel half-support
+  int nk;
+  int convN;    // SOCS conv grid (power of two >= 4*max(N)+1)
+};
+
+// Launch plan for one batch of one size class.
+struct ImgPlan {
+  ImgGeom g;
+  int batch = 1;
+  int rowBlocks = 1, colSplits = 1;  // window-DFT partition -> nparts
+  int kpg = 1, ngroups = 1;          // SOCS kernels per CTA -> ngroups
+  int nparts() const { return rowBlocks * colSplits; }
+};
+
+ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count);
+
+// Window source for the SOCS stage.
+struct WindowSrc {
+  const float2* part = nullptr;  // [batch][nparts][2Ny+1][Nx+1] partial sums (fused path)
+  int nparts = 0;
+  const float* mskf_r = nullptr;  // or full spectrum planes [batch][Fy][Fx]
+  const float* mskf_i = nullptr;
+};
+
+int run_win_dft(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+int run_socs(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2* krn,
+             const float* scales, float2* band_part, float* tmpImgp);
+int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
+int run_fft_mask(litho_ctx* ctx, const float* mask, int Lx, int Ly, float* mskf_r, float* mskf_i);
+int upload_kernels(litho_ctx* ctx, const float* krn_r, const float* krn_i, const float* scales,
+                   int nk, int kdim, int mem, float2* krn_dev, float* scales_dev);
+
+// Full imaging pipeline on device pointers for one size class (window DFT ->
+// SOCS -> FI), FP32 or mixed precision.
+int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks,
+                   const float2* krn, const float* scales, float* images, int precision);
+
+// mixed precision window DFT / interpolation (imaging_tc.cu)
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
+bool tc_supported(const ImgGeom& g);
+
+}  // namespace litho

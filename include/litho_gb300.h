@@ -1,0 +1,175 @@
+/*
+ * litho_gb300.h -- C ABI of liblitho_gb300.so, a GB300 (sm_103a) implementation
+ * of the Hopkins/SOCS aerial-image path: TCC assembly, SOCS kernel extraction
+ * and calcSOCS imaging (with Fourier interpolation).
+ *
+ * Every entry point replaces one function of the reference program
+ * validation/golden/src/litho.cpp (or of its FPGA top functions) and keeps its
+ * data conventions:
+ *   - all arrays are row-major, float32 unless stated;
+ *   - complex data is passed as separate real/imaginary planes (the BIN layout
+ *     of mskf_r.bin / mskf_i.bin / kernels/krn_{k}_{r,i}.bin), or interleaved
+ *     (re, im) float64 for the TCC (std::complex<double> layout);
+ *   - SOCS kernels are concatenated k-major: kernel k occupies
+ *     [k*(2Ny+1)*(2Nx+1), (k+1)*(2Ny+1)*(2Nx+1)), element ky*(2Nx+1)+kx,
+ *     exactly as litho.cpp:1420-1425 writes them and the HLS top reads them
+ *     (socs_2048_stream_refactored_v18_hls_fft.cpp:78);
+ *   - the mask spectrum has DC at (fftLy/2, fftLx/2) and is divided by
+ *     fftLx*fftLy (litho.cpp:242-318);
+ *   - callers allocate every output; the library never exits the process and
+ *     reports failures as LITHO_ERR_* status codes.
+ *
+ * Pointer location: entry points taking `int mem` accept either host pointers
+ * (LITHO_MEM_HOST: the library stages them through its own device buffers and
+ * returns after the results are back on the host) or device pointers
+ * (LITHO_MEM_DEVICE: work is enqueued on the context's stream and the call
+ * returns without synchronising).
+ *
+ * Threading: a litho_ctx is not re-entrant; use one context per host thread.
+ */
+#ifndef LITHO_GB300_H
+#define LITHO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LITHO_OK               0
+#define LITHO_ERR_ARG          1  /* invalid argument (size, pointer, nk > tccSize ...) */
+#define LITHO_ERR_CUDA         2  /* a CUDA runtime call failed (see litho_last_error) */
+#define LITHO_ERR_NOCONVERGE   3  /* eigensolver iteration cap reached */
+#define LITHO_ERR_NAN          4  /* non-finite input or output detected */
+#define LITHO_ERR_NOMEM        5  /* device or pinned allocation failed */
+#define LITHO_ERR_IO           6  /* file read/write failed (BIN / JSON helpers) */
+#define LITHO_ERR_UNSUPPORTED  7  /* size or mode outside what this build implements */
+#define LITHO_ERR_TIMEOUT      8  /* a bounded device-side wait gave up */
+
+#define LITHO_MEM_HOST   0
+#define LITHO_MEM_DEVICE 1
+
+/* Arithmetic of the imaging pipeline.
+ * LITHO_PREC_FP32  : window DFT, FFTs, intensity sum and interpolation in FP32
+ *                    on the CUDA cores (the plain path).
+ * LITHO_PREC_MIXED : the two dense DFT contractions (mask -> spectrum window,
+ *                    intensity band -> image) on the tensor cores with
+ *                    split-operand TF32 products and FP32 accumulation; FFTs
+ *                    and intensity sum in FP32.                               */
+#define LITHO_PREC_FP32  0
+#define LITHO_PREC_MIXED 1
+
+/* Arithmetic of the TCC contraction (litho.cpp:428-516).
+ * LITHO_TCC_FP64      : pupil in FP32 exactly as the reference, FP64 accumulation.
+ * LITHO_TCC_SPLIT_BF16: pupil split into three BF16 terms (hi*hi + hi*lo + lo*hi),
+ *                       tensor-core (tcgen05) contraction with FP32 accumulation. */
+#define LITHO_TCC_FP64       0
+#define LITHO_TCC_SPLIT_BF16 1
+
+typedef struct litho_ctx litho_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+int litho_ctx_create(int device, litho_ctx** out);
+int litho_ctx_destroy(litho_ctx* ctx);
+/* Use a caller-owned stream (cudaStream_t passed as void*); NULL restores the
+ * context's own stream. */
+int litho_ctx_set_stream(litho_ctx* ctx, void* stream);
+void* litho_ctx_get_stream(litho_ctx* ctx);
+/* Block until all work queued on the context's stream has finished. */
+int litho_ctx_synchronize(litho_ctx* ctx);
+/* Text of the last failure on this context (empty string if none). */
+const char* litho_last_error(const litho_ctx* ctx);
+const char* litho_status_string(int status);
+/* Library version as major*10000 + minor*100 + patch. */
+int litho_version(void);
+
+/* ---- per-stage device timers ---------------------------------------------
+ * The GPU counterpart of litho.cpp's per-module [TIME] lines
+ * (litho.cpp:1259-1474).  When enabled, every stage launch is bracketed by CUDA
+ * events on the context's stream.  Launch counts are kept whether or not timing
+ * is enabled. */
+#define LITHO_STAGE_WIN_DFT   0  /* mask -> spectrum window (partial DFT)        */
+#define LITHO_STAGE_SOCS      1  /* K inverse FFTs + intensity + band            */
+#define LITHO_STAGE_FI_PREP   2  /* band -> per-column interpolation rows        */
+#define LITHO_STAGE_FI_OUT    3  /* interpolation contraction, image write       */
+#define LITHO_STAGE_FFT_MASK  4  /* full centred mask spectrum                   */
+#define LITHO_STAGE_TCC       5  /* pupil build + TCC contraction                */
+#define LITHO_STAGE_EIG       6  /* Hermitian eigensolve                         */
+#define LITHO_STAGE_UPLOAD    7  /* kernel packing and other small helpers       */
+#define LITHO_STAGE_COUNT     8
+int litho_ctx_enable_timing(litho_ctx* ctx, int enable);
+/* Synchronise the stream; fill ms[LITHO_STAGE_COUNT] (summed device time) and
+ * launches[LITHO_STAGE_COUNT] (kernel launches) since the last reset; either
+ * output may be NULL.  reset != 0 clears the counters afterwards. */
+int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int reset);
+
+/* ---- optics helpers (litho.cpp:414-426, 1297-1302) --------------------- */
+/* getOuterSigma: max lit-pixel radius / ((srcSize-1)/2), clamped to 1 as
+ * litho.cpp:1298 does.  Host pointer. */
+float litho_outer_sigma(const float* src, int srcSize);
+/* Nx = floor(NA * L * (1 + outerSigma) / lambda) evaluated in float32. */
+int litho_optics_n(float NA, int L, float outerSigma, float wavelength);
+
+/* ---- mask spectrum (litho.cpp:242-318 FT_r2c_padded) --------------------
+ * mask: Ly x Lx.  Outputs fftLy x fftLx planes with fftL = nextPow2(L); DC at
+ * (fftLy/2, fftLx/2), divided by fftLx*fftLy. */
+int litho_fft_mask(litho_ctx* ctx, const float* mask, int Lx, int Ly,
+                   float* mskf_r, float* mskf_i, int mem);
+
+/* ---- SOCS imaging from a mask spectrum (litho.cpp:795-1006 calcSOCS) ----
+ * mskf_r/mskf_i: fftLy x fftLx planes (litho_fft_mask output).
+ * krn_r/krn_i: nk kernels, k-major, (2Ny+1)*(2Nx+1) each.  scales: nk.
+ * image: physLy x physLx output (calcSOCS + FI + centred crop).
+ * tmpImgp (optional, NULL to skip): convN x convN fftshifted intensity before
+ * interpolation (litho.cpp:934, the tmpImgp_full_{N}.bin dump).
+ * convN: conv grid; 0 selects 128 as litho.cpp:815-816 forces.  Any power of
+ * two >= 4*max(Nx,Ny)+1 gives the same image (the embed position only adds a
+ * linear phase before |.|^2). */
+int litho_calc_socs(litho_ctx* ctx, const float* mskf_r, const float* mskf_i,
+                    int fftLx, int fftLy, const float* krn_r, const float* krn_i,
+                    const float* scales, int nk, int Nx, int Ny, int physLx, int physLy,
+                    float* image, float* tmpImgp, int convN, int mem);
+
+/* ---- fused mask -> aerial image (FT_r2c_padded + calcSOCS, litho.cpp:1318-1451)
+ * One mask (Ly x Lx) to one image (Ly x Lx).  Only the (2Ny+1)x(2Nx+1) window
+ * of the spectrum is formed (a partial DFT), so the full spectrum never
+ * touches HBM.  precision: LITHO_PREC_FP32 or LITHO_PREC_MIXED. */
+int litho_image(litho_ctx* ctx, const float* mask, int Lx, int Ly,
+                const float* krn_r, const float* krn_i, const float* scales, int nk,
+                int Nx, int Ny, float* image, int precision, int mem);
+
+/* ---- batched imaging ------------------------------------------------------
+ * A kernel set is uploaded once and reused by every batch (kernels fixed, as in
+ * the reference's FPGA flow).  Masks of one batch share (Lx, Ly); masks are
+ * packed back to back (image i at offset i*Lx*Ly), outputs likewise. */
+typedef struct litho_kernel_set litho_kernel_set;
+int litho_kernel_set_create(litho_ctx* ctx, const float* krn_r, const float* krn_i,
+                            const float* scales, int nk, int Nx, int Ny, int mem,
+                            litho_kernel_set** out);
+int litho_kernel_set_destroy(litho_kernel_set* ks);
+int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* masks,
+                      int batch, int Lx, int Ly, float* images, int precision, int mem);
+
+/* ---- TCC (litho.cpp:428-516 calcTCC) --------------------------------------
+ * src: srcSize x srcSize normalised source (host or device per mem).
+ * tcc: tccSize x tccSize interleaved (re, im) float64, tccSize=(2Nx+1)(2Ny+1);
+ * Hermitian, upper triangle accumulated then mirrored as the reference. */
+int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSigma,
+                   float wavelength, float NA, float defocus, int Lx, int Ly, int Nx, int Ny,
+                   double* tcc, int tccPrecision, int mem);
+
+/* ---- SOCS kernels (litho.cpp:579-645 calcKernels) --------------------------
+ * Top-nk eigenpairs of the Hermitian tcc (interleaved float64, upper triangle
+ * used as zheevr 'U').  scales descending (float32, and optionally float64);
+ * kernel i is eigenvector i stored reversed: krn[i][j] = v_i[n-1-j].
+ * krn64 (optional): nk*tccSize interleaved float64 kernels. */
+int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize, int nk,
+                       float* krn_r, float* krn_i, float* scales,
+                       double* krn64, double* scales64, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LITHO_GB300_H */
