@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Aerial-image throughput of the SOCS path on GB300 (one JSON line on stdout).
+
+Workload (one "step"): a batch of B seeded 1024x1024 float32 Manhattan masks
+(line/space gratings and contact arrays, ~50 % density) imaged with K=24 fixed
+SOCS kernels.  The kernels come from this library's own GPU TCC + FP64
+eigensolver for a quasar source (4 poles at 45/135/225/315 deg, sigma 0.7-0.9,
+~2000 lit points), NA 0.8, lambda 193 nm, defocus 0.  B=64 masks are 256 MB in
+and 256 MB out per step, larger than the 129 MB L2, so no flush is needed.
+
+  value : images/s with masks resident in HBM (litho_image_batch on device
+          pointers), timed with CUDA events over K steps on the library's stream.
+  e2e   : images/s through the same C-ABI call with pinned host buffers
+          (host->device copy of the masks and device->host copy of the images
+          inside every step).
+  roofline : the dominant kernel's algorithmic bytes per launch / its average
+          launch time (CUDA events recorded by the library around each launch on
+          the launching stream) vs the measured HBM copy bandwidth.
+  cpu_baseline : the reference CPU algorithm (FT_r2c_padded + calcSOCS + FI in
+          FP64, multi-threaded scipy port) on a bounded sample of the same masks,
+          which also yields the GPU result's rel-L2 vs FP64.
+
+--impl reference times that CPU port alone on all host cores (the reference's
+own CPU implementation of the path cannot travel to the GPU host: it is built
+from the reference checkout with a project-written FFTW shim).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "fpga-litho-accel_gb300"))
+
+METRIC = "aerial images/s at 1024^2 K=24: mixed/batched/surrogate vs plain GPU at stated rel-L2"
+L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
+WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
+            "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--cpu-budget-s", type=float, default=12.0)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_masks(n, seed0=100):
+    import numpy as np
+    from litho_gb300 import synth
+    base = [synth.manhattan_mask(L_SIZE, seed=seed0 + i) for i in range(min(n, 8))]
+    return np.stack([base[i % len(base)] for i in range(n)])
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def setup_kernels(ctx):
+    """GPU TCC (FP64) + GPU FP64 eigensolver for the quasar source."""
+    import litho_gb300 as L
+    from litho_gb300 import synth
+    src, S, npts = synth.quasar_source(2000)
+    sig = L.outer_sigma(src)
+    nx = L.optics_n(NA, L_SIZE, sig, WAVELENGTH)
+    tcc = ctx.calc_tcc(src, sig, WAVELENGTH, NA, DEFOCUS, L_SIZE, L_SIZE, nx, nx)
+    krn, s32, s64 = ctx.calc_kernels(tcc, K_KERNELS)
+    return krn, s32, nx, npts
+
+
+def cpu_sample(masks, krn, scales, nx, budget):
+    from oracle import cpu_socs
+    ips, n, el, imgs = cpu_socs.time_images(masks, krn, scales, nx, nx, budget_s=budget)
+    return ips, n, el, imgs
+
+
+def run_reference(args, ws, rank):
+    """The reference CPU algorithm on the host cores, one bounded sample per step."""
+    if rank != 0:
+        return
+    import numpy as np
+    from litho_gb300 import synth
+    from oracle import np_ref as R
+    from oracle import cpu_socs
+    src, S, npts = synth.quasar_source(2000)
+    sig = R.get_outer_sigma(src)
+    nx = R.optics_nx(NA, L_SIZE, sig, WAVELENGTH)
+    tcc = R.calc_tcc(src, sig, WAVELENGTH, NA, DEFOCUS, L_SIZE, L_SIZE, nx, nx)
+    krn, scales, _ = R.calc_kernels(tcc, K_KERNELS)
+    per_step = 2
+    masks = make_masks(per_step)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        for m in masks:
+            cpu_socs.socs_image(m, krn, scales, nx, nx, workers=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for m in masks:
+            cpu_socs.socs_image(m, krn, scales, nx, nx, workers=cores)
+    el = time.perf_counter() - t0
+    v = per_step * args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": "images/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "per_step_images": per_step},
+            "cpu_baseline": {"value": v, "unit": "images/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} masks per step x {args.steps} steps: FT_r2c_padded + calcSOCS "
+                                       f"(128^2 conv grid, embed 94) + FI in FP64, scipy.fft workers={cores}"},
+            "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    import numpy as np
+    import torch
+    import litho_gb300 as L
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ctx = L.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    krn, scales, nx, npts = setup_kernels(ctx)
+    ks = ctx.kernel_set(krn, scales, nx, nx)
+    B = args.batch
+    masks_h = make_masks(B)
+    masks = torch.from_numpy(masks_h).cuda()
+    images = torch.empty_like(masks)
+    prec = {"auto": L.PREC_FP32, "fp32": L.PREC_FP32, "mixed": L.PREC_MIXED}[args.precision]
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.image_batch(ks, masks, images, precision=prec)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ctx.stage_times(reset=True)
+    ctx.enable_timing(True)
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    clk = clocks.stop()
+    ctx.enable_timing(False)
+    st = ctx.stage_times(reset=True)
+    value = ws * B * args.steps / (ms / 1e3)
+    launches = sum(n for _, n in st.values())
+
+    # roofline of the dominant kernel (algorithmic bytes per launch)
+    img_bytes = 4 * L_SIZE * L_SIZE
+    alg = {"win_dft": B * img_bytes, "fi_out": B * img_bytes,
+           "socs": B * (K_KERNELS * (2 * nx + 1) ** 2 * 8 + 4 * K_KERNELS),
+           "fi_prep": B * (4 * nx + 1) * L_SIZE * 4}
+    dom = max(("win_dft", "socs", "fi_prep", "fi_out"), key=lambda s: st[s][0])
+    dom_ms = st[dom][0] / max(1, st[dom][1])
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg[dom] / (dom_ms / 1e3) / 1e9
+    shares = {s: round(st[s][0] / max(1e-9, sum(st[k][0] for k in ("win_dft", "socs", "fi_prep", "fi_out"))), 4)
+              for s in ("win_dft", "socs", "fi_prep", "fi_out")}
+
+    # e2e through the C ABI with pinned host buffers
+    pin_in = torch.from_numpy(masks_h).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    hin, hout = pin_in.numpy(), pin_out.numpy()
+    ctx.set_stream(None)
+    for _ in range(2):
+        ctx.image_batch(ks, hin, hout, precision=prec)
+    if dist:
+        dist.barrier()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.image_batch(ks, hin, hout, precision=prec)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = ws * B * e2e_steps / e2e_s
+
+    line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if prec == L.PREC_FP32 else "tf32x3/f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "source_points": npts,
+                       "batch_per_step": B, "precision": "fp32" if prec == L.PREC_FP32 else "mixed",
+                       "l2": "inputs larger than L2 (256 MB in + 256 MB out per step)"},
+            "gpu_launches": int(launches),
+            "stage_ms_per_step": {s: st[s][0] / args.steps for s in ("win_dft", "socs", "fi_prep", "fi_out")},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json)"
+                         if peaks else "fallback", "shares": shares,
+                         "bytes_per_image": 2 * img_bytes + K_KERNELS * (2 * nx + 1) ** 2 * 8 + 4 * K_KERNELS,
+                         "path_frac": value / ws * (2 * img_bytes + K_KERNELS * (2 * nx + 1) ** 2 * 8 +
+                                                    4 * K_KERNELS) / 1e9 / hbm},
+            "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": int(masks_h.nbytes),
+                    "d2h_bytes_per_step": int(masks_h.nbytes)},
+            "clocks": clk}
+
+    if rank == 0 and not args.no_cpu:
+        ips, n, el, ref_imgs = cpu_sample(masks_h[:16], krn, scales, nx, args.cpu_budget_s)
+        from oracle import np_ref as R
+        errs = [R.rel_l2(images[i].cpu().numpy(), ref_imgs[i]) for i in range(n)]
+        line["cpu_baseline"] = {"value": ips, "unit": "images/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n} of the step's masks in {el:.1f} s: FT_r2c_padded + calcSOCS "
+                                          "(128^2 conv grid) + FI in FP64, scipy.fft on all host cores"}
+        line["rel_l2_vs_fp64"] = max(errs)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ks.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

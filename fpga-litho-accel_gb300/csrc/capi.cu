@@ -124,7 +124,7 @@ int litho_ctx_destroy(litho_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   DevBuf* bufs[] = {&ctx->win_part, &ctx->band_part, &ctx->tm,     &ctx->stage_in, &ctx->stage_out,
                     &ctx->stage_k,  &ctx->stage_s,   &ctx->stage_x, &ctx->tcc_a,   &ctx->tcc_b,
-                    &ctx->tcc_c,    &ctx->eig_w,     &ctx->eig_v,   &ctx->eig_work, &ctx->eig_info,
+                    &ctx->tcc_c,    &ctx->tcc_pq,  &ctx->eig_w,     &ctx->eig_v,   &ctx->eig_work, &ctx->eig_info,
                     &ctx->mx_b,     &ctx->mx_c,      &ctx->mx_d};
   for (DevBuf* b : bufs) b->release();
   for (auto& kv : ctx->twx_tables) kv.second.release();

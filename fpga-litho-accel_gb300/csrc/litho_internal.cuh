@@ -81,7 +81,7 @@ struct litho_ctx {
   // window-DFT column twiddle tables keyed by (Lx, Fx, Nx, NJT)
   std::map<std::tuple<int, int, int, int>, litho::DevBuf> twx_tables;
   // TCC / eigensolver workspaces
-  litho::DevBuf tcc_a, tcc_b, tcc_c, eig_w, eig_v, eig_work, eig_info;
+  litho::DevBuf tcc_a, tcc_b, tcc_c, tcc_pq, eig_w, eig_v, eig_work, eig_info;
   // mixed-precision (tensor-core) workspaces
   litho::DevBuf mx_b, mx_c, mx_d;
   // per-stage timers
@@ -133,6 +133,9 @@ struct ImgPlan {
 };
 
 ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count);
+
+// Host input -> device staging buffer (device input passes through).
+int stage_in(litho_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem, const void** dev);
 
 // Window source for the SOCS stage.
 struct WindowSrc {
