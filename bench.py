@@ -47,7 +47,7 @@ WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--batch", type=int, default=64)
@@ -88,7 +88,7 @@ class Clocks:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -209,10 +209,17 @@ def main():
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-    ctx.stage_times(reset=True)
-    ctx.enable_timing(True)
+    # clocks are sampled from here through the timed region and the e2e region;
+    # a short untimed pre-roll keeps the GPU under load until the sampler is live
     clocks = Clocks(local)
     clocks.start()
+    t_pre = time.perf_counter()
+    while time.perf_counter() - t_pre < 0.6:
+        for _ in range(8):
+            step()
+        torch.cuda.synchronize()
+    ctx.stage_times(reset=True)
+    ctx.enable_timing(True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -227,7 +234,6 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    clk = clocks.stop()
     ctx.enable_timing(False)
     st = ctx.stage_times(reset=True)
     value = ws * B * args.steps / (ms / 1e3)
@@ -269,6 +275,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = ws * B * e2e_steps / e2e_s
+    clk = clocks.stop()
 
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",

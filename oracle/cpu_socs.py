@@ -60,18 +60,22 @@ def socs_image(mask: np.ndarray, krns: np.ndarray, scales: np.ndarray, Nx: int, 
 
 def time_images(masks, krns, scales, Nx, Ny, budget_s: float = 15.0, min_images: int = 2,
                 workers: int | None = None):
-    """Image masks in order until ``budget_s`` has elapsed (at least ``min_images``).
+    """Image masks cyclically until ``budget_s`` has elapsed (at least ``min_images``).
 
-    Returns (images_per_s, n_images, elapsed_s, images).
+    Returns (images_per_s, n_images, elapsed_s, images of the first pass over ``masks``).
     """
     workers = workers or os.cpu_count() or 1
     socs_image(masks[0], krns, scales, Nx, Ny, workers=workers)   # warm the FFT plan caches
     out = []
+    n = 0
     t0 = time.perf_counter()
-    for i in range(len(masks)):
-        out.append(socs_image(masks[i], krns, scales, Nx, Ny, workers=workers))
+    while True:
+        img = socs_image(masks[n % len(masks)], krns, scales, Nx, Ny, workers=workers)
+        if n < len(masks):
+            out.append(img)
+        n += 1
         el = time.perf_counter() - t0
-        if len(out) >= min_images and el >= budget_s:
+        if n >= min_images and el >= budget_s:
             break
     el = time.perf_counter() - t0
-    return len(out) / el, len(out), el, out
+    return n / el, n, el, out
