@@ -750,6 +750,119 @@ int run_fft_mask(litho_ctx* ctx, const float* mask, int Lx, int Ly, float* mskf_
   return LITHO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Context-free launch of the FP32 pipeline for one image into caller-provided
+// scratch (used by the allocation-free entry point in noalloc.cu).  Launches
+// only; it allocates nothing and records nothing on a context.
+// ---------------------------------------------------------------------------
+__global__ void pack_planes_kernel(const float* __restrict__ kr, const float* __restrict__ ki, int n,
+                                   float2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_float2(kr[i], ki[i]);
+}
+
+size_t noctx_scratch_layout(const ImgPlan& p, size_t off[6]) {
+  const ImgGeom& g = p.g;
+  const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1), KY = 2 * g.Ny + 1;
+  const size_t sz[6] = {(size_t)g.nk * KD * sizeof(float2),
+                        (size_t)g.nk * sizeof(float),
+                        (size_t)g.Lx * njt_for(g.Nx) * sizeof(float),
+                        (size_t)p.nparts() * KY * (g.Nx + 1) * sizeof(float2),
+                        (size_t)p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2),
+                        (size_t)(4 * g.Ny + 1) * g.Lx * sizeof(float)};
+  size_t o = 0;
+  for (int i = 0; i < 6; ++i) {
+    off[i] = o;
+    o += (sz[i] + 255) & ~size_t(255);
+  }
+  return o;
+}
+
+template <int NJT>
+static cudaError_t noctx_win_dft_t(cudaStream_t s, const ImgPlan& p, const float* masks, const float* twx,
+                                   float2* win_part) {
+  const ImgGeom& g = p.g;
+  const size_t main_sm = (size_t)(WD_BK * WD_SA + WD_BK * NJT) * sizeof(float);
+  const size_t red_sm = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(g.Ny + 1) * WD_BM * sizeof(float2);
+  const size_t smem = std::max(main_sm, red_sm);
+  dim3 grid(p.rowBlocks, p.colSplits, p.batch);
+  auto k = (g.Lx & 3) == 0 ? win_dft_kernel<NJT, true> : win_dft_kernel<NJT, false>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, WD_THREADS, smem, s>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t noctx_socs_t(cudaStream_t s, const ImgPlan& p, const float2* win_part, const float2* krn,
+                                const float* scales, float2* band_part) {
+  const ImgGeom& g = p.g;
+  const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
+  const size_t smem = ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = socs_kernel<N>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<dim3(p.ngroups, p.batch), SOCS_THREADS, smem, s>>>(win_part, p.nparts(), nullptr, nullptr, g.Fx, g.Fy, g.Nx,
+                                                          g.Ny, krn, scales, g.nk, p.kpg, band_part, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t image_pipeline_noctx(cudaStream_t s, const ImgPlan& p, const float* mask, const float* krn_r,
+                                 const float* krn_i, const float* scales, char* scratch, float* image) {
+  const ImgGeom& g = p.g;
+  size_t off[6];
+  noctx_scratch_layout(p, off);
+  float2* krn = reinterpret_cast<float2*>(scratch + off[0]);
+  float* sc = reinterpret_cast<float*>(scratch + off[1]);
+  float* twx = reinterpret_cast<float*>(scratch + off[2]);
+  float2* win_part = reinterpret_cast<float2*>(scratch + off[3]);
+  float2* band_part = reinterpret_cast<float2*>(scratch + off[4]);
+  float* tm = reinterpret_cast<float*>(scratch + off[5]);
+  const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
+  const int NJT = njt_for(g.Nx);
+  cudaError_t e;
+  pack_planes_kernel<<<(g.nk * KD + 255) / 256, 256, 0, s>>>(krn_r, krn_i, g.nk * KD, krn);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(sc, scales, g.nk * sizeof(float), cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return e;
+  twx_init_kernel<<<(g.Lx + 127) / 128, 128, 0, s>>>(twx, g.Lx, g.Fx, g.Nx, NJT);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  switch (NJT) {
+    case 8: e = noctx_win_dft_t<8>(s, p, mask, twx, win_part); break;
+    case 12: e = noctx_win_dft_t<12>(s, p, mask, twx, win_part); break;
+    case 20: e = noctx_win_dft_t<20>(s, p, mask, twx, win_part); break;
+    default: e = noctx_win_dft_t<36>(s, p, mask, twx, win_part); break;
+  }
+  if (e != cudaSuccess) return e;
+  switch (g.convN) {
+    case 32: e = noctx_socs_t<32>(s, p, win_part, krn, sc, band_part); break;
+    case 64: e = noctx_socs_t<64>(s, p, win_part, krn, sc, band_part); break;
+    default: e = noctx_socs_t<128>(s, p, win_part, krn, sc, band_part); break;
+  }
+  if (e != cudaSuccess) return e;
+  {
+    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
+    const size_t smem = ((size_t)BH * BW + (size_t)ND * FIP_THREADS) * sizeof(float2);
+    if ((e = cudaFuncSetAttribute(fi_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+      return e;
+    fi_prep_kernel<<<dim3((g.Lx + FIP_THREADS - 1) / FIP_THREADS, 1), FIP_THREADS, smem, s>>>(band_part, p.ngroups,
+                                                                                              g.Lx, g.Fx, g.Nx,
+                                                                                              g.Ny, tm);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  {
+    const int KB = 4 * g.Ny + 1;
+    const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);
+    dim3 grid((g.Lx + FO_BN - 1) / FO_BN, (g.Ly + FO_BM - 1) / FO_BM, 1);
+    auto k = (g.Lx & 3) == 0 ? fi_out_kernel<true> : fi_out_kernel<false>;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+      return e;
+    k<<<grid, FO_THREADS, smem, s>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, image);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const float2* krn,
                    const float* scales, float* images, int precision) {
   ImgPlan p = make_plan(g, batch, ctx->sm_count);

@@ -152,6 +152,24 @@ int litho_kernel_set_destroy(litho_kernel_set* ks);
 int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* masks,
                       int batch, int Lx, int Ly, float* images, int precision, int mem);
 
+/* ---- mask -> image with no device allocation ------------------------------
+ * No counterpart in the reference.  For callers that cannot let a library call
+ * cudaMalloc/cudaFree: those calls synchronise the whole device (a latency-
+ * critical loop on several streams cannot afford that), and a plugin whose host
+ * application owns the device memory budget through its own allocator must not
+ * allocate behind it.  The same FP32 pipeline as litho_image, but its
+ * intermediates live in one fixed 6 MiB __device__ array compiled into the
+ * library (held by every GPU that loads it until the process exits).
+ * All pointers are device pointers on the current device; work is queued on
+ * `stream` (cudaStream_t as void*, NULL = legacy default stream) and the call
+ * returns without synchronising.  Limits: 2 <= Lx, Ly <= 4096, Nx, Ny <= 16,
+ * 1 <= nk <= 64; anything beyond returns LITHO_ERR_ARG.  The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture).  Calls share the array: calls whose work overlaps on the GPU race
+ * and must be serialised by the caller. */
+int litho_image_noalloc(const float* mask, int Lx, int Ly, const float* krn_r, const float* krn_i,
+                        const float* scales, int nk, int Nx, int Ny, float* image, void* stream);
+
 /* ---- TCC (litho.cpp:428-516 calcTCC) --------------------------------------
  * src: srcSize x srcSize normalised source (host or device per mem).
  * tcc: tccSize x tccSize interleaved (re, im) float64, tccSize=(2Nx+1)(2Ny+1);
