@@ -149,7 +149,7 @@ void* litho_ctx_get_stream(litho_ctx* ctx) { return ctx ? (void*)ctx->stream : n
 int litho_ctx_synchronize(litho_ctx* ctx) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return LITHO_OK;
+  return tc_check_flag(ctx);
 }
 
 int litho_ctx_enable_timing(litho_ctx* ctx, int enable) {
@@ -399,6 +399,7 @@ int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* m
   if (mem == LITHO_MEM_HOST) {
     LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(images, dimg, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (precision == LITHO_PREC_MIXED) LITHO_RET(tc_check_flag(ctx));
   }
   return LITHO_OK;
 }

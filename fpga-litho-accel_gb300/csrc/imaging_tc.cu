@@ -1,18 +1,658 @@
-// Mixed-precision (tensor-core) window DFT and interpolation.
+// Mixed-precision imaging: the two dense DFT contractions of the pipeline on the
+// 5th-generation tensor cores (tcgen05, kind::tf32) with split operands and
+// FP32 accumulation in TMEM.  The FFTs and the intensity sum (socs_kernel) stay
+// FP32 on the CUDA cores.
+//
+// Split products.  Every operand X is written as X = Xh + Xl with
+// Xh = round_tf32(X) and Xl = X - Xh (exact in FP32); each contraction issues
+// Ah*Bh + Ah*Bl + Al*Bh, all accumulated into one TMEM accumulator.  The
+// dropped Al*Bl term and the TF32 rounding of Xl leave a relative error of about
+// 2^-22 per product.
+//
+// win_dft_tc_kernel   D[y][j] = sum_x mask[y][x] * T[x][j]  (M = 128 mask rows
+//                     per CTA, N = 2Nx+1 column twiddles padded to NB, K = Lx).
+//                     TMA streams 128 x 32 mask tiles (SWIZZLE_128B) through a
+//                     5-stage mbarrier ring; the CTA splits each landed tile into
+//                     Ah (in place) and Al; one thread issues 12 MMAs per tile.
+//                     The row-DFT epilogue is the FP32 kernel's.
+// fi_tc_kernel        image[Y][X] = sum_r Cy[Y][r] * Tm[r][X]  (M = 128 image
+//                     rows, N = 128 columns per tile, K = 4Ny+1 padded to 32*KBLK).
+//                     Persistent over the X tiles of one row band: A (the Cy
+//                     table) is loaded once, B (Tm^T) is double-buffered, and the
+//                     accumulator leaves TMEM through a swizzled staging tile and
+//                     TMA bulk stores (the image is written exactly once).
 #include "litho_internal.cuh"
+#include "tc_common.cuh"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
 
 namespace litho {
+using namespace tc;
 
-bool tc_supported(const ImgGeom& g) { return false; }
+// ---------------------------------------------------------------------------
+// operand tables (built once per geometry, cached on the context)
+// ---------------------------------------------------------------------------
+// twT[j][x] (NB rows): j <= Nx cos(2 pi j x'/Fx); Nx < j <= 2Nx -sin(2 pi (j-Nx) x'/Fx); else 0
+__global__ void twT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, int Lx, int Fx, int Nx, int NB) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (x >= Lx || j >= NB) return;
+  const long long xp = (long long)x + (Fx - Lx) / 2 - Fx / 2;
+  double v = 0.0;
+  if (j <= 2 * Nx) {
+    const int u = j <= Nx ? j : j - Nx;
+    long long m = ((long long)u * xp) % Fx;
+    if (m < 0) m += Fx;
+    double s, c;
+    sincospi(2.0 * (double)m / (double)Fx, &s, &c);
+    v = j <= Nx ? c : -s;
+  }
+  const float h = tf32_round((float)v);
+  hi[(size_t)j * Lx + x] = h;
+  lo[(size_t)j * Lx + x] = (float)(v - (double)h);
+}
+
+// CyT[Y][r] (KP columns): r = 0 -> 1; 1..2Ny -> 2cos(2 pi r y'/Fy); 2Ny+1..4Ny -> -2sin; else 0
+__global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, int Ly, int Fy, int Ny, int KP) {
+  const int Y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (Y >= Ly || r >= KP) return;
+  const long long yp = (long long)Y + (Fy - Ly) / 2 - Fy / 2;
+  double v = 0.0;
+  if (r == 0) {
+    v = 1.0;
+  } else if (r <= 4 * Ny) {
+    const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
+    long long m = ((long long)dy * yp) % Fy;
+    if (m < 0) m += Fy;
+    double s, c;
+    sincospi(2.0 * (double)m / (double)Fy, &s, &c);
+    v = r <= 2 * Ny ? 2.0 * c : -2.0 * s;
+  }
+  const float h = tf32_round((float)v);
+  hi[(size_t)Y * KP + r] = h;
+  lo[(size_t)Y * KP + r] = (float)(v - (double)h);
+}
+
+// ---------------------------------------------------------------------------
+// window DFT on the tensor cores
+// ---------------------------------------------------------------------------
+constexpr int WT_STAGES = 5;
+
+template <int NB>
+struct WinTC {
+  static constexpr uint32_t A_B = 128 * 128;   // 128 rows x 32 fp32
+  static constexpr uint32_t B_B = NB * 128;    // NB rows x 32 fp32
+  static constexpr uint32_t STAGE_B = 2 * A_B + 2 * B_B;
+  static constexpr uint32_t NCOL = NB <= 32 ? 32 : 64;
+  static constexpr size_t SMEM = 1024 + (size_t)WT_STAGES * STAGE_B + 256;
+};
+
+template <int NB>
+__global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
+                                                            const __grid_constant__ CUtensorMap tmBh,
+                                                            const __grid_constant__ CUtensorMap tmBl, int Lx,
+                                                            int Ly, int Fx, int Fy, int Nx, int Ny,
+                                                            float2* __restrict__ win_part, int* __restrict__ err) {
+  using P = WinTC<NB>;
+  extern __shared__ unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + WT_STAGES * P::STAGE_B);
+  uint64_t* empty = full + WT_STAGES;
+  uint64_t* done = empty + WT_STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
+  const int nch = (Lx + 31) / 32;
+
+  if (warp == 0) tmem_alloc(tslot, P::NCOL);
+  if (tid == 0) {
+    for (int s = 0; s < WT_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
+  auto sAl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
+  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B; };
+  auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B + P::B_B; };
+  auto issue = [&](int c) {
+    const int s = c % WT_STAGES;
+    mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
+    tma_load_3d(sA(s), &tmM, &full[s], 32 * c, y0, img);
+    tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
+    tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
+  };
+  int issued = 0;
+  if (tid == 0)
+    for (; issued < min(nch, WT_STAGES); ++issued) issue(issued);
+
+  constexpr uint32_t IDESC = idesc_tf32(128, NB);
+  int bad = 0, c = 0;
+  for (; c < nch; ++c) {
+    const int s = c % WT_STAGES;
+    const uint32_t ph = (uint32_t)(c / WT_STAGES) & 1u;
+    const bool okw = mbar_wait(&full[s], ph);
+    if (__syncthreads_or(!okw)) {
+      bad = 1;
+      break;
+    }
+    float4* a = reinterpret_cast<float4*>(sA(s));
+    float4* al = reinterpret_cast<float4*>(sAl(s));
+#pragma unroll 4
+    for (int i = tid; i < (int)(P::A_B / 16); i += 128) {
+      const float4 v = a[i];
+      const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+      a[i] = h;
+      al[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+    }
+    fence_proxy_async();
+    __syncthreads();
+    int bad0 = 0;
+    if (tid == 0) {
+      tc_fence_after();
+      const uint64_t da = desc_sw128(sA(s)), dal = desc_sw128(sAl(s));
+      const uint64_t dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint32_t off = kk * 32;
+        mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
+        mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
+        mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+      }
+      mma_commit(&empty[s]);
+      if (issued < nch) {
+        if (!mbar_wait(&empty[s], ph)) bad0 = 1;
+        else issue(issued++);
+      }
+    }
+    if (__syncthreads_or(bad0)) {
+      bad = 1;
+      ++c;
+      break;
+    }
+  }
+  if (!bad) {
+    if (tid == 0) mma_commit(done);
+    if (__syncthreads_or(!mbar_wait(done, 0))) bad = 1;
+  }
+  if (bad) {
+    // drain what this CTA issued (bounded), free TMEM, report
+    if (tid == 0) {
+      atomicExch(err, 1);
+      mma_commit(done);
+      mbar_wait(done, 0, 1u << 20);
+      for (int k = c; k < issued; ++k) mbar_wait(&full[k % WT_STAGES], (uint32_t)(k / WT_STAGES) & 1u, 1u << 20);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, P::NCOL);
+    return;
+  }
+  tc_fence_after();
+  float* sR = reinterpret_cast<float*>(sm);  // [NB][128]
+  const int row = 32 * warp + lane;
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+  if (NB >= 32) {
+    float v[32];
+    tmem_ld32(trow, v);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) sR[j * 128 + row] = v[j];
+  }
+  if (NB == 16 || NB == 48) {
+    float v[16];
+    tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * 128 + row] = v[j];
+  }
+  float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NB * 128 * sizeof(float));
+  const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
+  for (int idx = tid; idx < (Ny + 1) * 128; idx += 128) {
+    const int v = idx / 128, r = idx - v * 128;
+    long long m = ((long long)v * (y0 + r + oyc)) % Fy;
+    if (m < 0) m += Fy;
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)Fy, &sn, &cs);
+    sRT[idx] = make_float2(cs, -sn);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, P::NCOL);
+
+  const int KY = 2 * Ny + 1, NU = Nx + 1;
+  const float scale = 1.0f / ((float)Fx * (float)Fy);
+  float2* out = win_part + ((size_t)img * gridDim.x + rb) * KY * NU;
+  for (int o = tid; o < KY * NU; o += 128) {
+    const int vi = o / NU, u = o - vi * NU;
+    const int v = vi - Ny;
+    const int av = v < 0 ? -v : v;
+    const float ts = v < 0 ? -1.f : 1.f;
+    const float* rc = sR + u * 128;
+    const float* rs = sR + (Nx + u) * 128;
+    const float2* rt = sRT + av * 128;
+    float re = 0.f, im = 0.f;
+    if (u == 0) {
+      for (int r = 0; r < 128; ++r) {
+        const float2 t = rt[r];
+        re = fmaf(rc[r], t.x, re);
+        im = fmaf(rc[r], ts * t.y, im);
+      }
+    } else {
+      for (int r = 0; r < 128; ++r) {
+        const float2 t = rt[r];
+        const float ty = ts * t.y;
+        re = fmaf(rc[r], t.x, fmaf(-rs[r], ty, re));
+        im = fmaf(rc[r], ty, fmaf(rs[r], t.x, im));
+      }
+    }
+    out[o] = make_float2(re * scale, im * scale);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FI prep for the tensor-core contraction: TmT[img][X][KP] split hi/lo
+// ---------------------------------------------------------------------------
+constexpr int FPT_THREADS = 128;
+
+__global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ band_part, int ngroups,
+                                                                 int Lx, int Fx, int Nx, int Ny, int KP,
+                                                                 float* __restrict__ tmh, float* __restrict__ tml) {
+  extern __shared__ __align__(16) float2 fps[];
+  const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
+  float2* sS = fps;                                            // [BH][BW]
+  float2* sT = fps + BH * BW;                                  // [ND][128]
+  float* sO = reinterpret_cast<float*>(sT + ND * FPT_THREADS);  // [128][KP+1]
+  const int tid = threadIdx.x, img = blockIdx.y;
+  const int X0 = blockIdx.x * FPT_THREADS, X = X0 + tid;
+  const float2* B = band_part + (size_t)img * ngroups * BH * BW;
+  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) {
+    float re = 0.f, im = 0.f;
+    for (int gi = 0; gi < ngroups; ++gi) {
+      const float2 t = B[(size_t)gi * BH * BW + idx];
+      re += t.x;
+      im += t.y;
+    }
+    sS[idx] = make_float2(re, im);
+  }
+  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
+  for (int d = 0; d < ND; ++d) {
+    long long m = ((long long)d * xp) % Fx;
+    if (m < 0) m += Fx;
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)Fx, &sn, &cs);
+    sT[d * FPT_THREADS + tid] = make_float2(cs, sn);
+  }
+  __syncthreads();
+  float* o = sO + tid * (KP + 1);
+  for (int r = 4 * Ny + 1; r < KP; ++r) o[r] = 0.f;
+  for (int fy = 0; fy < BH; ++fy) {
+    const float2* S = sS + fy * BW + 2 * Nx;
+    float re = S[0].x, im = S[0].y;
+    for (int d = 1; d < ND; ++d) {
+      const float2 t = sT[d * FPT_THREADS + tid];
+      const float2 p = S[d], q = S[-d];
+      re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
+      im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+    }
+    if (fy == 0) {
+      o[0] = re;
+    } else {
+      o[fy] = re;
+      o[2 * Ny + fy] = im;
+    }
+  }
+  __syncthreads();
+  const size_t base = ((size_t)img * Lx + X0) * KP;
+  const int nrow = min(FPT_THREADS, Lx - X0);
+  for (int idx = tid; idx < nrow * KP; idx += FPT_THREADS) {
+    const int xr = idx / KP, r = idx - xr * KP;
+    const float v = sO[xr * (KP + 1) + r];
+    const float h = tf32_round(v);
+    tmh[base + idx] = h;
+    tml[base + idx] = v - h;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FI contraction on the tensor cores
+// ---------------------------------------------------------------------------
+template <int KBLK, int BN>
+struct FiTC {
+  static constexpr uint32_t A_KB = 128 * 128;     // 128 rows x 32 fp32
+  static constexpr uint32_t B_KB = BN * 128;      // BN rows x 32 fp32
+  static constexpr uint32_t A_BYTES = 2 * KBLK * A_KB;
+  static constexpr uint32_t B_BYTES = 2 * KBLK * B_KB;
+  static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
+  static constexpr size_t SMEM = 1024 + A_BYTES + 2 * (size_t)B_BYTES + 2 * OUT_B + 256;
+};
+
+template <int KBLK, int BN>
+__global__ void __launch_bounds__(128, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
+                                                       const __grid_constant__ CUtensorMap tmCl,
+                                                       const __grid_constant__ CUtensorMap tmTh,
+                                                       const __grid_constant__ CUtensorMap tmTl,
+                                                       const __grid_constant__ CUtensorMap tmOut, int Lx,
+                                                       int* __restrict__ err) {
+  using P = FiTC<KBLK, BN>;
+  extern __shared__ unsigned char smraw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sAh = sm;
+  unsigned char* sAl = sm + KBLK * P::A_KB;
+  unsigned char* sB = sm + P::A_BYTES;                            // [2][hi kb..., lo kb...]
+  unsigned char* sOut = sB + 2 * P::B_BYTES;                      // [2][OUT_B]
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(sOut + 2 * P::OUT_B);
+  uint64_t* fullB = fullA + 1;  // [2]
+  uint64_t* mdone = fullA + 3;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(fullA + 4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int yb = blockIdx.x, img = blockIdx.y, y0 = yb * 128;
+  const int ntile = (Lx + BN - 1) / BN;
+
+  if (warp == 0) tmem_alloc(tslot, BN);
+  if (tid == 0) {
+    mbar_init(fullA, 1);
+    mbar_init(&fullB[0], 1);
+    mbar_init(&fullB[1], 1);
+    mbar_init(mdone, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  auto Bh = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)kb * P::B_KB; };
+  auto Bl = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)(KBLK + kb) * P::B_KB; };
+  auto issueB = [&](int t) {
+    const int b = t & 1;
+    mbar_arrive_expect_tx(&fullB[b], P::B_BYTES);
+    for (int kb = 0; kb < KBLK; ++kb) {
+      tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, t * BN, img);
+      tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, t * BN, img);
+    }
+  };
+  int issued = 0;
+  if (tid == 0) {
+    mbar_arrive_expect_tx(fullA, P::A_BYTES);
+    for (int kb = 0; kb < KBLK; ++kb) {
+      tma_load_2d(sAh + (size_t)kb * P::A_KB, &tmCh, fullA, 32 * kb, y0);
+      tma_load_2d(sAl + (size_t)kb * P::A_KB, &tmCl, fullA, 32 * kb, y0);
+    }
+    for (; issued < min(ntile, 2); ++issued) issueB(issued);
+  }
+  constexpr uint32_t IDESC = idesc_tf32(128, BN);
+  const int row = 32 * warp + lane;
+  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+  int bad = 0, t = 0;
+  bool a_ready = false;
+  for (; t < ntile; ++t) {
+    const int b = t & 1;
+    int bad0 = 0;
+    if (tid == 0) {
+      if (!a_ready) {
+        a_ready = mbar_wait(fullA, 0);
+        if (!a_ready) bad0 = 1;
+      }
+      if (!bad0 && !mbar_wait(&fullB[b], (uint32_t)(t >> 1) & 1u)) bad0 = 1;
+      if (!bad0) {
+        tc_fence_after();
+#pragma unroll
+        for (int kb = 0; kb < KBLK; ++kb) {
+          const uint64_t dah = desc_sw128(sAh + (size_t)kb * P::A_KB), dal = desc_sw128(sAl + (size_t)kb * P::A_KB);
+          const uint64_t dbh = desc_sw128(Bh(b, kb)), dbl = desc_sw128(Bl(b, kb));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint32_t off = kk * 32;
+            mma_tf32(tmem, desc_add(dah, off), desc_add(dbh, off), IDESC, (kb | kk) != 0 ? 1u : 0u);
+            mma_tf32(tmem, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
+            mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+          }
+        }
+        mma_commit(mdone);
+      }
+    }
+    if (__syncthreads_or(bad0)) {
+      bad = 1;
+      break;
+    }
+    if (__syncthreads_or(!mbar_wait(mdone, (uint32_t)t & 1u))) {
+      bad = 1;
+      break;
+    }
+    tc_fence_after();
+    // buffer b is free: prefetch tile t+2 into it
+    if (tid == 0 && issued < ntile) issueB(issued++);
+#pragma unroll 1
+    for (int slab = 0; slab < BN / 32; ++slab) {
+      float v[32];
+      tmem_ld32(trow + (uint32_t)(slab * 32), v);
+      unsigned char* st = sOut + (size_t)(slab & 1) * P::OUT_B;
+      if (tid == 0) bulk_wait_read0();
+      __syncthreads();
+      float4* rowp = reinterpret_cast<float4*>(st + (size_t)row * 128);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) rowp[q ^ (row & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tma_store_3d(&tmOut, st, t * BN + slab * 32, y0, img);
+        bulk_commit();
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (bad) atomicExch(err, 1);
+    bulk_wait0();
+    if (bad) {
+      mma_commit(mdone);
+      mbar_wait(mdone, (uint32_t)t & 1u, 1u << 20);
+      mbar_wait(fullA, 0, 1u << 20);
+      for (int k = t; k < issued; ++k) mbar_wait(&fullB[k & 1], (uint32_t)(k >> 1) & 1u, 1u << 20);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, BN);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (fn == nullptr) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// FP32 tensor map with a 128-byte swizzle and a {32, box1(, 1)} box.
+static int make_map(litho_ctx* ctx, CUtensorMap* m, const void* base, int rank, uint64_t d0, uint64_t d1,
+                    uint64_t d2, uint32_t box1) {
+  auto fn = encode_fn();
+  if (fn == nullptr) {
+    set_error(ctx, LITHO_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    return LITHO_ERR_CUDA;
+  }
+  cuuint64_t dims[3] = {d0, d1, d2};
+  cuuint64_t strides[2] = {d0 * 4, d0 * d1 * 4};
+  cuuint32_t box[3] = {32, box1, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<void*>(base), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error(ctx, LITHO_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return LITHO_ERR_CUDA;
+  }
+  return LITHO_OK;
+}
+
+static int nb_for(int Nx) {
+  const int nj = 2 * Nx + 1;
+  return nj <= 16 ? 16 : (nj <= 32 ? 32 : (nj <= 48 ? 48 : -1));
+}
+static int kblk_for(int Ny) { return (4 * Ny + 1 + 31) / 32; }
+
+bool tc_supported(const ImgGeom& g) {
+  return (g.Lx % 4) == 0 && g.Nx <= 16 && g.Ny <= 16 && nb_for(g.Nx) > 0 && kblk_for(g.Ny) <= 3;
+}
+
+static int tc_err_flag(litho_ctx* ctx, int** flag) {
+  if (ctx->mx_d.p == nullptr) {
+    LITHO_RET(ctx->mx_d.ensure(ctx, 256));
+    LITHO_CUDA_TRY(ctx, cudaMemsetAsync(ctx->mx_d.p, 0, 256, ctx->stream));
+  }
+  *flag = ctx->mx_d.as<int>();
+  return LITHO_OK;
+}
+
+// Read and clear the device-side timeout flag of the tensor-core kernels
+// (the caller has synchronised the stream).
+int tc_check_flag(litho_ctx* ctx) {
+  if (ctx->mx_d.p == nullptr) return LITHO_OK;
+  int v = 0;
+  LITHO_CUDA_TRY(ctx, cudaMemcpy(&v, ctx->mx_d.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v != 0) {
+    LITHO_CUDA_TRY(ctx, cudaMemset(ctx->mx_d.p, 0, 256));
+    set_error(ctx, LITHO_ERR_TIMEOUT, "a tensor-core pipeline wait gave up (bounded mbarrier wait)");
+    return LITHO_ERR_TIMEOUT;
+  }
+  return LITHO_OK;
+}
+
+static int cached_table(litho_ctx* ctx, std::tuple<int, int, int, int> key, size_t bytes, bool* fresh,
+                        float** out) {
+  auto it = ctx->twx_tables.find(key);
+  *fresh = false;
+  if (it == ctx->twx_tables.end()) {
+    DevBuf b;
+    LITHO_RET(b.ensure(ctx, bytes));
+    it = ctx->twx_tables.emplace(key, b).first;
+    *fresh = true;
+  }
+  *out = it->second.as<float>();
+  return LITHO_OK;
+}
+
+template <int NB>
+static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
+  const ImgGeom& g = p.g;
+  bool fresh = false;
+  float* tw = nullptr;
+  LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -NB), (size_t)2 * NB * g.Lx * sizeof(float), &fresh,
+                         &tw));
+  float* twh = tw;
+  float* twl = tw + (size_t)NB * g.Lx;
+  if (fresh) {
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    twT_init_kernel<<<dim3((g.Lx + 127) / 128, NB), 128, 0, ctx->stream>>>(twh, twl, g.Lx, g.Fx, g.Nx, NB);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  CUtensorMap mM, mBh, mBl;
+  LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
+  LITHO_RET(make_map(ctx, &mBh, twh, 2, g.Lx, NB, 1, NB));
+  LITHO_RET(make_map(ctx, &mBl, twl, 2, g.Lx, NB, 1, NB));
+  const size_t smem = WinTC<NB>::SMEM;
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+  dim3 grid((g.Ly + 127) / 128, p.batch);
+  StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
+  win_dft_tc_kernel<NB><<<grid, 128, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
+                                                           win_part, err);
+  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  return LITHO_OK;
+}
 
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
-  set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT not built");
-  return LITHO_ERR_UNSUPPORTED;
+  int* err = nullptr;
+  LITHO_RET(tc_err_flag(ctx, &err));
+  switch (nb_for(p.g.Nx)) {
+    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err);
+    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err);
+    case 48: return launch_win_tc<48>(ctx, p, masks, win_part, err);
+    default:
+      set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT supports Nx <= 16");
+      return LITHO_ERR_UNSUPPORTED;
+  }
+}
+
+template <int KBLK, int BN>
+static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, const float* cyl, const float* tmh,
+                        const float* tml, float* images, int* err) {
+  const ImgGeom& g = p.g;
+  const int KP = 32 * KBLK;
+  CUtensorMap mCh, mCl, mTh, mTl, mO;
+  LITHO_RET(make_map(ctx, &mCh, cyh, 2, KP, g.Ly, 1, 128));
+  LITHO_RET(make_map(ctx, &mCl, cyl, 2, KP, g.Ly, 1, 128));
+  LITHO_RET(make_map(ctx, &mTh, tmh, 3, KP, g.Lx, p.batch, BN));
+  LITHO_RET(make_map(ctx, &mTl, tml, 3, KP, g.Lx, p.batch, BN));
+  LITHO_RET(make_map(ctx, &mO, images, 3, g.Lx, g.Ly, p.batch, 128));
+  const size_t smem = FiTC<KBLK, BN>::SMEM;
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem));
+  dim3 grid((g.Ly + 127) / 128, p.batch);
+  StageScope sc(ctx, LITHO_STAGE_FI_OUT);
+  fi_tc_kernel<KBLK, BN><<<grid, 128, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, err);
+  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  return LITHO_OK;
 }
 
 int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images) {
-  set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core interpolation not built");
-  return LITHO_ERR_UNSUPPORTED;
+  const ImgGeom& g = p.g;
+  const int KBLK = kblk_for(g.Ny);
+  const int KP = 32 * KBLK;
+  int* err = nullptr;
+  LITHO_RET(tc_err_flag(ctx, &err));
+  // Cy table, cached per (Ly, Fy, Ny)
+  bool fresh = false;
+  float* cy = nullptr;
+  LITHO_RET(cached_table(ctx, std::make_tuple(g.Ly, g.Fy, g.Ny, -1000 - KP), (size_t)2 * g.Ly * KP * sizeof(float),
+                         &fresh, &cy));
+  float* cyh = cy;
+  float* cyl = cy + (size_t)g.Ly * KP;
+  if (fresh) {
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    cyT_init_kernel<<<dim3((g.Ly + 127) / 128, KP), 128, 0, ctx->stream>>>(cyh, cyl, g.Ly, g.Fy, g.Ny, KP);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  // TmT hi/lo: [batch][Lx][KP]
+  LITHO_RET(ctx->mx_b.ensure(ctx, (size_t)2 * p.batch * g.Lx * KP * sizeof(float)));
+  float* tmh = ctx->mx_b.as<float>();
+  float* tml = tmh + (size_t)p.batch * g.Lx * KP;
+  {
+    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
+    const size_t smem = ((size_t)BH * BW + (size_t)ND * FPT_THREADS) * sizeof(float2) +
+                        (size_t)FPT_THREADS * (KP + 1) * sizeof(float);
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_prep_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    StageScope sc(ctx, LITHO_STAGE_FI_PREP);
+    fi_prep_tc_kernel<<<dim3((g.Lx + FPT_THREADS - 1) / FPT_THREADS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
+        band_part, p.ngroups, g.Lx, g.Fx, g.Nx, g.Ny, KP, tmh, tml);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  (void)tm;
+  switch (KBLK) {
+    case 1: return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);
+    case 2: return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);
+    default: return launch_fi_tc<3, 64>(ctx, p, cyh, cyl, tmh, tml, images, err);
+  }
 }
 
 }  // namespace litho

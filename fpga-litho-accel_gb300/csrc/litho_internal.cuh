@@ -162,5 +162,6 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
 int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
 bool tc_supported(const ImgGeom& g);
+int tc_check_flag(litho_ctx* ctx);
 
 }  // namespace litho
