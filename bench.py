@@ -123,21 +123,50 @@ class Clocks:
 
 
 def setup_kernels(ctx):
-    """GPU TCC (FP64) + GPU FP64 eigensolver for the quasar source."""
+    """Kernels of both forms from this library's GPU path for the quasar source:
+    plain = FP64 TCC + FP64 eigensolve; mixed = split-BF16 tensor-core TCC + FP64 eigensolve."""
     import litho_gb300 as L
     from litho_gb300 import synth
     src, S, npts = synth.quasar_source(2000)
     sig = L.outer_sigma(src)
     nx = L.optics_n(NA, L_SIZE, sig, WAVELENGTH)
-    tcc = ctx.calc_tcc(src, sig, WAVELENGTH, NA, DEFOCUS, L_SIZE, L_SIZE, nx, nx)
-    krn, s32, s64 = ctx.calc_kernels(tcc, K_KERNELS)
-    return krn, s32, nx, npts
+    out = {"src": src, "sigma": sig, "nx": nx, "npts": npts}
+    for form, prec in (("plain", L.TCC_FP64), ("mixed", L.TCC_SPLIT_BF16)):
+        tcc = ctx.calc_tcc(src, sig, WAVELENGTH, NA, DEFOCUS, L_SIZE, L_SIZE, nx, nx, precision=prec)
+        krn, s32, s64 = ctx.calc_kernels(tcc, K_KERNELS)
+        out[form] = {"tcc": tcc, "krn": krn, "s32": s32, "s64": s64}
+    return out
 
 
-def cpu_sample(masks, krn, scales, nx, budget):
+def cpu_leg(setup, masks_h, gpu_images, budget):
+    """The reference CPU algorithm (FP64) on a bounded sample: timing, and the
+    GPU forms' errors vs FP64 for TCC, scales, kernels (per-cluster projectors) and image."""
+    import numpy as np
     from oracle import cpu_socs
-    ips, n, el, imgs = cpu_socs.time_images(masks, krn, scales, nx, nx, budget_s=budget)
-    return ips, n, el, imgs
+    from oracle import np_ref as R
+    nx = setup["nx"]
+    tcc = R.calc_tcc(setup["src"], setup["sigma"], WAVELENGTH, NA, DEFOCUS, L_SIZE, L_SIZE, nx, nx)
+    krn, s32, w64 = R.calc_kernels(tcc, K_KERNELS)
+    ips, n, el, ref = cpu_socs.time_images(masks_h, krn, s32, nx, nx, budget_s=budget)
+    w_all = np.linalg.eigvalsh(tcc)[::-1]
+    err = {}
+    for form, imgs in gpu_images.items():
+        f = setup[form]
+        proj = 0.0
+        i = 0
+        while i < K_KERNELS:   # clusters of (near-)equal eigenvalues inside the kept set
+            j = i + 1
+            while j < len(w_all) and abs(w_all[j - 1] - w_all[j]) <= 1e-6 * w_all[0]:
+                j += 1
+            if j <= K_KERNELS:
+                a, b = f["krn"][i:j].T, krn[i:j].T
+                proj = max(proj, float(np.linalg.norm(a @ a.conj().T - b @ b.conj().T)))
+            i = j
+        err[form] = {"image": max(R.rel_l2(imgs[k], ref[k]) for k in range(min(len(ref), len(imgs)))),
+                     "tcc": float(np.linalg.norm(f["tcc"] - tcc) / np.linalg.norm(tcc)),
+                     "scales": float(np.max(np.abs(f["s64"] - w64) / np.abs(w64))),
+                     "kernel_projector": proj}
+    return ips, n, el, err
 
 
 def run_reference(args, ws, rank):
@@ -194,57 +223,68 @@ def main():
     ctx = L.Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
-    krn, scales, nx, npts = setup_kernels(ctx)
-    ks = ctx.kernel_set(krn, scales, nx, nx)
+    setup = setup_kernels(ctx)
+    nx, npts = setup["nx"], setup["npts"]
+    ks = {f: ctx.kernel_set(setup[f]["krn"], setup[f]["s32"], nx, nx) for f in ("plain", "mixed")}
+    prec = {"plain": L.PREC_FP32, "mixed": L.PREC_MIXED}
+    head = "plain" if args.precision == "fp32" else "mixed"
     B = args.batch
     masks_h = make_masks(B)
     masks = torch.from_numpy(masks_h).cuda()
-    images = torch.empty_like(masks)
-    prec = {"auto": L.PREC_FP32, "fp32": L.PREC_FP32, "mixed": L.PREC_MIXED}[args.precision]
+    images = {f: torch.empty_like(masks) for f in ("plain", "mixed")}
     torch.cuda.synchronize()
 
-    def step():
-        ctx.image_batch(ks, masks, images, precision=prec)
+    def step(form):
+        ctx.image_batch(ks[form], masks, images[form], precision=prec[form])
 
-    for _ in range(max(args.warmup, 3)):
-        step()
+    def timed(form, steps):
+        """K steps bracketed by barrier + synchronize, CUDA events on the library's stream."""
+        ctx.stage_times(reset=True)
+        ctx.enable_timing(True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(form)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        ctx.enable_timing(False)
+        return ms, ctx.stage_times(reset=True)
+
+    for form in ("plain", "mixed"):
+        for _ in range(max(args.warmup, 3)):
+            step(form)
     torch.cuda.synchronize()
-    # clocks are sampled from here through the timed region and the e2e region;
+    # clocks are sampled from here through both timed regions and the e2e region;
     # a short untimed pre-roll keeps the GPU under load until the sampler is live
     clocks = Clocks(local)
     clocks.start()
     t_pre = time.perf_counter()
     while time.perf_counter() - t_pre < 0.6:
         for _ in range(8):
-            step()
+            step(head)
         torch.cuda.synchronize()
-    ctx.stage_times(reset=True)
-    ctx.enable_timing(True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ctx.enable_timing(False)
-    st = ctx.stage_times(reset=True)
+    other = "plain" if head == "mixed" else "mixed"
+    ms_o, st_o = timed(other, args.steps)
+    ms, st = timed(head, args.steps)
     value = ws * B * args.steps / (ms / 1e3)
+    value_o = ws * B * args.steps / (ms_o / 1e3)
     launches = sum(n for _, n in st.values())
 
     # roofline of the dominant kernel (algorithmic bytes per launch)
     img_bytes = 4 * L_SIZE * L_SIZE
-    alg = {"win_dft": B * img_bytes, "fi_out": B * img_bytes,
-           "socs": B * (K_KERNELS * (2 * nx + 1) ** 2 * 8 + 4 * K_KERNELS),
+    kb = K_KERNELS * (2 * nx + 1) ** 2 * 8 + 4 * K_KERNELS
+    alg = {"win_dft": B * img_bytes, "fi_out": B * img_bytes, "socs": B * kb,
            "fi_prep": B * (4 * nx + 1) * L_SIZE * 4}
-    dom = max(("win_dft", "socs", "fi_prep", "fi_out"), key=lambda s: st[s][0])
+    names = ("win_dft", "socs", "fi_prep", "fi_out")
+    dom = max(names, key=lambda s: st[s][0])
     dom_ms = st[dom][0] / max(1, st[dom][1])
     peaks = {}
     try:
@@ -253,22 +293,23 @@ def main():
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg[dom] / (dom_ms / 1e3) / 1e9
-    shares = {s: round(st[s][0] / max(1e-9, sum(st[k][0] for k in ("win_dft", "socs", "fi_prep", "fi_out"))), 4)
-              for s in ("win_dft", "socs", "fi_prep", "fi_out")}
+    tot = sum(st[k][0] for k in names)
+    shares = {s: round(st[s][0] / max(1e-9, tot), 4) for s in names}
+    kern_gbs = {s: alg[s] / (st[s][0] / max(1, st[s][1]) / 1e3) / 1e9 for s in ("win_dft", "fi_out")}
 
-    # e2e through the C ABI with pinned host buffers
+    # e2e through the C ABI with pinned host buffers (headline form)
     pin_in = torch.from_numpy(masks_h).pin_memory()
     pin_out = torch.empty_like(pin_in).pin_memory()
     hin, hout = pin_in.numpy(), pin_out.numpy()
     ctx.set_stream(None)
     for _ in range(2):
-        ctx.image_batch(ks, hin, hout, precision=prec)
+        ctx.image_batch(ks[head], hin, hout, precision=prec[head])
     if dist:
         dist.barrier()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(3, args.steps // 4)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.image_batch(ks, hin, hout, precision=prec)
+        ctx.image_batch(ks[head], hin, hout, precision=prec[head])
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
@@ -277,35 +318,44 @@ def main():
     e2e = ws * B * e2e_steps / e2e_s
     clk = clocks.stop()
 
+    forms = {head: {"images_per_s": value, "ms_per_step": ms / args.steps,
+                    "stage_ms_per_step": {s: st[s][0] / args.steps for s in names}},
+             other: {"images_per_s": value_o, "ms_per_step": ms_o / args.steps,
+                     "stage_ms_per_step": {s: st_o[s][0] / args.steps for s in names}}}
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if prec == L.PREC_FP32 else "tf32x3/f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": "tf32x3/f32" if head == "mixed" else "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "source_points": npts,
-                       "batch_per_step": B, "precision": "fp32" if prec == L.PREC_FP32 else "mixed",
+                       "batch_per_step": B, "form": head,
+                       "forms": "mixed = split-BF16 tcgen05 TCC + FP64 eigensolve + split-TF32 tcgen05 DFTs; "
+                                "plain = FP64 TCC + FP64 eigensolve + FP32 CUDA-core DFTs; both FP32 FFTs",
                        "l2": "inputs larger than L2 (256 MB in + 256 MB out per step)"},
             "gpu_launches": int(launches),
-            "stage_ms_per_step": {s: st[s][0] / args.steps for s in ("win_dft", "socs", "fi_prep", "fi_out")},
+            "forms": forms,
+            "mixed_over_plain": forms["mixed"]["images_per_s"] / forms["plain"]["images_per_s"],
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None, "peak_source": "measured (MEASURED_PEAKS.json)"
-                         if peaks else "fallback", "shares": shares,
-                         "bytes_per_image": 2 * img_bytes + K_KERNELS * (2 * nx + 1) ** 2 * 8 + 4 * K_KERNELS,
-                         "path_frac": value / ws * (2 * img_bytes + K_KERNELS * (2 * nx + 1) ** 2 * 8 +
-                                                    4 * K_KERNELS) / 1e9 / hbm},
+                         "frac": achieved / hbm, "traffic": None,
+                         "peak_source": "measured (MEASURED_PEAKS.json)" if peaks else "fallback",
+                         "shares": shares, "kernel_gbs": kern_gbs,
+                         "bytes_per_image": 2 * img_bytes + kb,
+                         "path_frac": value / ws * (2 * img_bytes + kb) / 1e9 / hbm},
             "e2e": {"value": e2e, "unit": "images/s", "h2d_bytes_per_step": int(masks_h.nbytes),
                     "d2h_bytes_per_step": int(masks_h.nbytes)},
             "clocks": clk}
 
     if rank == 0 and not args.no_cpu:
-        ips, n, el, ref_imgs = cpu_sample(masks_h[:16], krn, scales, nx, args.cpu_budget_s)
-        from oracle import np_ref as R
-        errs = [R.rel_l2(images[i].cpu().numpy(), ref_imgs[i]) for i in range(n)]
+        nsamp = min(16, B)
+        gpu_imgs = {f: images[f][:nsamp].cpu().numpy() for f in ("plain", "mixed")}
+        ips, n, el, err = cpu_leg(setup, masks_h[:nsamp], gpu_imgs, args.cpu_budget_s)
         line["cpu_baseline"] = {"value": ips, "unit": "images/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{n} of the step's masks in {el:.1f} s: FT_r2c_padded + calcSOCS "
-                                          "(128^2 conv grid) + FI in FP64, scipy.fft on all host cores"}
-        line["rel_l2_vs_fp64"] = max(errs)
+                                "sample": f"{n} images ({nsamp} distinct masks of the step) in {el:.1f} s: "
+                                          "FT_r2c_padded + calcSOCS (128^2 conv grid, embed 94) + FI in FP64, "
+                                          "scipy.fft on all host cores"}
+        line["rel_l2_vs_fp64"] = err
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ks.close()
+    for k in ks.values():
+        k.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()

@@ -524,6 +524,8 @@ static int tc_err_flag(litho_ctx* ctx, int** flag) {
   return LITHO_OK;
 }
 
+int tc_err_flag_public(litho_ctx* ctx, int** flag) { return tc_err_flag(ctx, flag); }
+
 // Read and clear the device-side timeout flag of the tensor-core kernels
 // (the caller has synchronised the stream).
 int tc_check_flag(litho_ctx* ctx) {

@@ -132,6 +132,39 @@ def test_full_path_tcc_kernels_image(ctx):
     assert R.rel_l2(img, ref) < 1e-5
 
 
+@pytest.mark.parametrize("case", ["annular21_512", "quasar_1024"])
+def test_tcc_split_bf16_close_to_fp64(ctx, L, case):
+    """Three-term BF16 split products with FP32 accumulation (tcgen05): ~1e-5 relative."""
+    from litho_gb300 import synth
+    src, L_ = (synth.annular_source(21, 0.6, 0.9), 512) if case == "annular21_512" else \
+        (synth.quasar_source(2000)[0], 1024)
+    sig = R.get_outer_sigma(src)
+    nx = R.optics_nx(0.8, L_, sig, 193.0)
+    ref = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx)
+    tcc = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
+    err = np.linalg.norm(tcc - ref) / np.linalg.norm(ref)
+    assert err < 5e-5, err
+    assert np.array_equal(tcc, tcc.conj().T)
+
+
+def test_mixed_chain_config2_vs_fp64(ctx, L):
+    """Split-BF16 TCC -> FP64 eigensolve -> split-TF32 imaging, vs the all-FP64 oracle: <= 1e-4."""
+    from litho_gb300 import synth
+    src = synth.quasar_source(2000)[0]
+    sig = R.get_outer_sigma(src)
+    nx = R.optics_nx(0.8, 1024, sig, 193.0)
+    tcc = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, 1024, 1024, nx, nx, precision=L.TCC_SPLIT_BF16)
+    krn, s32, _ = ctx.calc_kernels(tcc, 24)
+    mask = synth.manhattan_mask(1024, seed=77)
+    ks = ctx.kernel_set(krn, s32, nx, nx)
+    img = ctx.image_batch(ks, mask[None], precision=L.PREC_MIXED)[0]
+    ks.close()
+    tcc_r = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, 1024, 1024, nx, nx)
+    kr, sr, _ = R.calc_kernels(tcc_r, 24)
+    ref = R.mask_to_image(mask, kr, sr, nx, nx)
+    assert R.rel_l2(img, ref) < 1e-4
+
+
 def test_tcc_and_kernel_errors(ctx, golden_optics, L):
     g = golden_optics
     with pytest.raises(L.LithoError) as e:   # Nx too small for the pupil support
