@@ -90,7 +90,7 @@ template <int NJT, bool VEC>
 __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __restrict__ masks, int Lx, int Ly,
                                                              int Fx, int Fy, int Nx, int Ny,
                                                              const float* __restrict__ twx,
-                                                             float2* __restrict__ win_part) {
+                                                             float2* __restrict__ win_part, int part_stride) {
   extern __shared__ __align__(16) float sm[];
   float* sA = sm;                    // [WD_BK][WD_SA]   mask chunk, transposed
   float* sB = sA + WD_BK * WD_SA;    // [WD_BK][NJT]     column twiddles of the chunk
@@ -218,7 +218,10 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
 
   const int KY = 2 * Ny + 1, NU = Nx + 1;
   const float scale = 1.0f / ((float)Fx * (float)Fy);
-  float2* out = win_part + ((size_t)img * nparts + part) * KY * NU;
+  // part_stride > 0: images of this launch sit in a larger per-class array with
+  // that many parts per image (the unused parts are zero)
+  const int nps = part_stride > 0 ? part_stride : nparts;
+  float2* out = win_part + ((size_t)img * nps + part) * KY * NU;
   for (int o = tid; o < KY * NU; o += WD_THREADS) {
     const int vi = o / NU, u = o - vi * NU;
     const int v = vi - Ny;
@@ -635,11 +638,11 @@ static int launch_win_dft_t(litho_ctx* ctx, const ImgPlan& p, const float* masks
   if ((g.Lx & 3) == 0) {
     auto k = win_dft_kernel<NJT, true>;
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part, p.part_stride);
   } else {
     auto k = win_dft_kernel<NJT, false>;
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+    k<<<grid, WD_THREADS, smem, ctx->stream>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part, p.part_stride);
   }
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
@@ -789,7 +792,7 @@ static cudaError_t noctx_win_dft_t(cudaStream_t s, const ImgPlan& p, const float
   auto k = (g.Lx & 3) == 0 ? win_dft_kernel<NJT, true> : win_dft_kernel<NJT, false>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<grid, WD_THREADS, smem, s>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part);
+  k<<<grid, WD_THREADS, smem, s>>>(masks, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, twx, win_part, 0);
   return cudaGetLastError();
 }
 

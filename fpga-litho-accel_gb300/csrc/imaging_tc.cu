@@ -9,18 +9,25 @@
 // dropped Al*Bl term and the TF32 rounding of Xl leave a relative error of about
 // 2^-22 per product.
 //
+// Both kernels are warp-specialised (192 threads) and synchronised only by
+// mbarriers, so TMA traffic, tensor-core work and CUDA-core work overlap:
+//   warp 4  TMA producer (one lane)
+//   warp 5  MMA issuer   (one lane)
+//   warps 0-3  compute / epilogue (they own TMEM lanes 0-127)
+//
 // win_dft_tc_kernel   D[y][j] = sum_x mask[y][x] * T[x][j]  (M = 128 mask rows
 //                     per CTA, N = 2Nx+1 column twiddles padded to NB, K = Lx).
 //                     TMA streams 128 x 32 mask tiles (SWIZZLE_128B) through a
-//                     5-stage mbarrier ring; the CTA splits each landed tile into
-//                     Ah (in place) and Al; one thread issues 12 MMAs per tile.
-//                     The row-DFT epilogue is the FP32 kernel's.
+//                     5-stage ring; warps 0-3 split each landed tile into Ah (in
+//                     place) and Al; the MMA lane issues 12 MMAs per tile.  The
+//                     row-DFT epilogue is the FP32 kernel's.
 // fi_tc_kernel        image[Y][X] = sum_r Cy[Y][r] * Tm[r][X]  (M = 128 image
-//                     rows, N = 128 columns per tile, K = 4Ny+1 padded to 32*KBLK).
+//                     rows, N = BN columns per tile, K = 4Ny+1 padded to 32*KBLK).
 //                     Persistent over the X tiles of one row band: A (the Cy
-//                     table) is loaded once, B (Tm^T) is double-buffered, and the
-//                     accumulator leaves TMEM through a swizzled staging tile and
-//                     TMA bulk stores (the image is written exactly once).
+//                     table) is loaded once, B (Tm^T) and the TMEM accumulator are
+//                     double-buffered, and the epilogue drains each accumulator
+//                     through two swizzled staging tiles with TMA bulk stores
+//                     (the image is written exactly once).
 #include "litho_internal.cuh"
 #include "tc_common.cuh"
 
@@ -81,6 +88,7 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // window DFT on the tensor cores
 // ---------------------------------------------------------------------------
 constexpr int WT_STAGES = 5;
+constexpr int TC_THREADS = 192;
 
 template <int NB>
 struct WinTC {
@@ -92,18 +100,22 @@ struct WinTC {
 };
 
 template <int NB>
-__global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
-                                                            const __grid_constant__ CUtensorMap tmBh,
-                                                            const __grid_constant__ CUtensorMap tmBl, int Lx,
-                                                            int Ly, int Fx, int Fy, int Nx, int Ny,
-                                                            float2* __restrict__ win_part, int* __restrict__ err) {
+__global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
+                                                                   const __grid_constant__ CUtensorMap tmBh,
+                                                                   const __grid_constant__ CUtensorMap tmBl,
+                                                                   int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
+                                                                   float2* __restrict__ win_part, int part_stride,
+                                                                   int* __restrict__ err) {
   using P = WinTC<NB>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + WT_STAGES * P::STAGE_B);
-  uint64_t* empty = full + WT_STAGES;
+  uint64_t* ready = full + WT_STAGES;
+  uint64_t* empty = ready + WT_STAGES;
   uint64_t* done = empty + WT_STAGES;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [WT_STAGES]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
   const int nch = (Lx + 31) / 32;
@@ -112,9 +124,12 @@ __global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constan
   if (tid == 0) {
     for (int s = 0; s < WT_STAGES; ++s) {
       mbar_init(&full[s], 1);
+      mbar_init(&ready[s], 128);
       mbar_init(&empty[s], 1);
+      last_issued[s] = -1;
     }
     mbar_init(done, 1);
+    *abort = 0;
     fence_mbar_init();
   }
   tc_fence_before();
@@ -126,74 +141,74 @@ __global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constan
   auto sAl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
   auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B; };
   auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B + P::B_B; };
-  auto issue = [&](int c) {
-    const int s = c % WT_STAGES;
-    mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
-    tma_load_3d(sA(s), &tmM, &full[s], 32 * c, y0, img);
-    tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
-    tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
-  };
-  int issued = 0;
-  if (tid == 0)
-    for (; issued < min(nch, WT_STAGES); ++issued) issue(issued);
 
-  constexpr uint32_t IDESC = idesc_tf32(128, NB);
-  int bad = 0, c = 0;
-  for (; c < nch; ++c) {
-    const int s = c % WT_STAGES;
-    const uint32_t ph = (uint32_t)(c / WT_STAGES) & 1u;
-    const bool okw = mbar_wait(&full[s], ph);
-    if (__syncthreads_or(!okw)) {
-      bad = 1;
-      break;
+  if (warp == 4) {
+    if (lane == 0) {  // TMA producer
+      for (int c = 0; c < nch; ++c) {
+        const int s = c % WT_STAGES;
+        if (c >= WT_STAGES && !mbar_wait_ab(&empty[s], (uint32_t)((c - WT_STAGES) / WT_STAGES) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
+        tma_load_3d(sA(s), &tmM, &full[s], 32 * c, y0, img);
+        tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
+        tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
+        last_issued[s] = c;
+      }
     }
-    float4* a = reinterpret_cast<float4*>(sA(s));
-    float4* al = reinterpret_cast<float4*>(sAl(s));
-#pragma unroll 4
-    for (int i = tid; i < (int)(P::A_B / 16); i += 128) {
-      const float4 v = a[i];
-      const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
-      a[i] = h;
-      al[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-    }
-    fence_proxy_async();
-    __syncthreads();
-    int bad0 = 0;
-    if (tid == 0) {
-      tc_fence_after();
-      const uint64_t da = desc_sw128(sA(s)), dal = desc_sw128(sAl(s));
-      const uint64_t dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
+  } else if (warp == 5) {
+    if (lane == 0) {  // MMA issuer
+      constexpr uint32_t IDESC = idesc_tf32(128, NB);
+      for (int c = 0; c < nch; ++c) {
+        const int s = c % WT_STAGES;
+        if (!mbar_wait_ab(&ready[s], (uint32_t)(c / WT_STAGES) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t da = desc_sw128(sA(s)), dal = desc_sw128(sAl(s));
+        const uint64_t dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const uint32_t off = kk * 32;
-        mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
-        mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
-        mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint32_t off = kk * 32;
+          mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
+          mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
+          mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+        }
+        mma_commit(&empty[s]);
       }
-      mma_commit(&empty[s]);
-      if (issued < nch) {
-        if (!mbar_wait(&empty[s], ph)) bad0 = 1;
-        else issue(issued++);
-      }
+      mma_commit(done);  // arrives once everything issued above has completed
     }
-    if (__syncthreads_or(bad0)) {
-      bad = 1;
-      ++c;
-      break;
+  } else {  // warps 0-3: split the landed tile into hi (in place) and lo
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % WT_STAGES;
+      if (!mbar_wait_ab(&full[s], (uint32_t)(c / WT_STAGES) & 1u, abort)) {
+        *abort = 1;
+        break;
+      }
+      float4* a = reinterpret_cast<float4*>(sA(s));
+      float4* al = reinterpret_cast<float4*>(sAl(s));
+#pragma unroll 4
+      for (int i = tid; i < (int)(P::A_B / 16); i += 128) {
+        const float4 v = a[i];
+        const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+        a[i] = h;
+        al[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      fence_proxy_async();
+      mbar_arrive(&ready[s]);
     }
   }
-  if (!bad) {
-    if (tid == 0) mma_commit(done);
-    if (__syncthreads_or(!mbar_wait(done, 0))) bad = 1;
-  }
-  if (bad) {
-    // drain what this CTA issued (bounded), free TMEM, report
-    if (tid == 0) {
-      atomicExch(err, 1);
-      mma_commit(done);
-      mbar_wait(done, 0, 1u << 20);
-      for (int k = c; k < issued; ++k) mbar_wait(&full[k % WT_STAGES], (uint32_t)(k / WT_STAGES) & 1u, 1u << 20);
-    }
+  // the MMA lane always commits `done`; everyone waits for the tensor cores to drain
+  if (!mbar_wait(done, 0)) *abort = 1;
+  __syncthreads();
+  if (*abort) {
+    if (tid == 160) mbar_wait(done, 0, 1u << 20);  // the MMA lane's final commit covers all it issued
+    if (tid == 128)  // warp 4 lane 0: wait for the last load of every stage (bounded)
+      for (int s = 0; s < WT_STAGES; ++s)
+        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / WT_STAGES) & 1u, 1u << 20);
+    if (tid == 0) atomicExch(err, 1);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, P::NCOL);
@@ -201,23 +216,25 @@ __global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constan
   }
   tc_fence_after();
   float* sR = reinterpret_cast<float*>(sm);  // [NB][128]
-  const int row = 32 * warp + lane;
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-  if (NB >= 32) {
-    float v[32];
-    tmem_ld32(trow, v);
+  if (warp < 4) {
+    const int row = 32 * warp + lane;
+    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+    if (NB >= 32) {
+      float v[32];
+      tmem_ld32(trow, v);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) sR[j * 128 + row] = v[j];
-  }
-  if (NB == 16 || NB == 48) {
-    float v[16];
-    tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
+      for (int j = 0; j < 32; ++j) sR[j * 128 + row] = v[j];
+    }
+    if (NB == 16 || NB == 48) {
+      float v[16];
+      tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
 #pragma unroll
-    for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * 128 + row] = v[j];
+      for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * 128 + row] = v[j];
+    }
   }
   float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NB * 128 * sizeof(float));
   const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
-  for (int idx = tid; idx < (Ny + 1) * 128; idx += 128) {
+  for (int idx = tid; idx < (Ny + 1) * 128; idx += TC_THREADS) {
     const int v = idx / 128, r = idx - v * 128;
     long long m = ((long long)v * (y0 + r + oyc)) % Fy;
     if (m < 0) m += Fy;
@@ -231,8 +248,9 @@ __global__ void __launch_bounds__(128, 1) win_dft_tc_kernel(const __grid_constan
 
   const int KY = 2 * Ny + 1, NU = Nx + 1;
   const float scale = 1.0f / ((float)Fx * (float)Fy);
-  float2* out = win_part + ((size_t)img * gridDim.x + rb) * KY * NU;
-  for (int o = tid; o < KY * NU; o += 128) {
+  const int nps = part_stride > 0 ? part_stride : (int)gridDim.x;
+  float2* out = win_part + ((size_t)img * nps + rb) * KY * NU;
+  for (int o = tid; o < KY * NU; o += TC_THREADS) {
     const int vi = o / NU, u = o - vi * NU;
     const int v = vi - Ny;
     const int av = v < 0 ? -v : v;
@@ -337,75 +355,87 @@ struct FiTC {
 };
 
 template <int KBLK, int BN>
-__global__ void __launch_bounds__(128, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
-                                                       const __grid_constant__ CUtensorMap tmCl,
-                                                       const __grid_constant__ CUtensorMap tmTh,
-                                                       const __grid_constant__ CUtensorMap tmTl,
-                                                       const __grid_constant__ CUtensorMap tmOut, int Lx,
-                                                       int* __restrict__ err) {
+__global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
+                                                              const __grid_constant__ CUtensorMap tmCl,
+                                                              const __grid_constant__ CUtensorMap tmTh,
+                                                              const __grid_constant__ CUtensorMap tmTl,
+                                                              const __grid_constant__ CUtensorMap tmOut, int Lx,
+                                                              int* __restrict__ err) {
   using P = FiTC<KBLK, BN>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   unsigned char* sAh = sm;
   unsigned char* sAl = sm + KBLK * P::A_KB;
-  unsigned char* sB = sm + P::A_BYTES;                            // [2][hi kb..., lo kb...]
-  unsigned char* sOut = sB + 2 * P::B_BYTES;                      // [2][OUT_B]
+  unsigned char* sB = sm + P::A_BYTES;               // [2][hi kb..., lo kb...]
+  unsigned char* sOut = sB + 2 * P::B_BYTES;         // [2][OUT_B]
   uint64_t* fullA = reinterpret_cast<uint64_t*>(sOut + 2 * P::OUT_B);
-  uint64_t* fullB = fullA + 1;  // [2]
-  uint64_t* mdone = fullA + 3;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(fullA + 4);
+  uint64_t* fullB = fullA + 1;     // [2]
+  uint64_t* emptyB = fullA + 3;    // [2]
+  uint64_t* accFull = fullA + 5;   // [2]
+  uint64_t* accEmpty = fullA + 7;  // [2]
+  uint64_t* drain = fullA + 9;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(fullA + 10);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [2]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int yb = blockIdx.x, img = blockIdx.y, y0 = yb * 128;
   const int ntile = (Lx + BN - 1) / BN;
 
-  if (warp == 0) tmem_alloc(tslot, BN);
+  if (warp == 0) tmem_alloc(tslot, 2 * BN);
   if (tid == 0) {
     mbar_init(fullA, 1);
-    mbar_init(&fullB[0], 1);
-    mbar_init(&fullB[1], 1);
-    mbar_init(mdone, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&fullB[b], 1);
+      mbar_init(&emptyB[b], 1);
+      mbar_init(&accFull[b], 1);
+      mbar_init(&accEmpty[b], 128);
+      last_issued[b] = -1;
+    }
+    mbar_init(drain, 1);
+    *abort = 0;
     fence_mbar_init();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-
   auto Bh = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)kb * P::B_KB; };
   auto Bl = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)(KBLK + kb) * P::B_KB; };
-  auto issueB = [&](int t) {
-    const int b = t & 1;
-    mbar_arrive_expect_tx(&fullB[b], P::B_BYTES);
-    for (int kb = 0; kb < KBLK; ++kb) {
-      tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, t * BN, img);
-      tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, t * BN, img);
-    }
-  };
-  int issued = 0;
-  if (tid == 0) {
-    mbar_arrive_expect_tx(fullA, P::A_BYTES);
-    for (int kb = 0; kb < KBLK; ++kb) {
-      tma_load_2d(sAh + (size_t)kb * P::A_KB, &tmCh, fullA, 32 * kb, y0);
-      tma_load_2d(sAl + (size_t)kb * P::A_KB, &tmCl, fullA, 32 * kb, y0);
-    }
-    for (; issued < min(ntile, 2); ++issued) issueB(issued);
-  }
-  constexpr uint32_t IDESC = idesc_tf32(128, BN);
-  const int row = 32 * warp + lane;
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-  int bad = 0, t = 0;
-  bool a_ready = false;
-  for (; t < ntile; ++t) {
-    const int b = t & 1;
-    int bad0 = 0;
-    if (tid == 0) {
-      if (!a_ready) {
-        a_ready = mbar_wait(fullA, 0);
-        if (!a_ready) bad0 = 1;
+
+  if (warp == 4) {
+    if (lane == 0) {  // TMA producer
+      mbar_arrive_expect_tx(fullA, P::A_BYTES);
+      for (int kb = 0; kb < KBLK; ++kb) {
+        tma_load_2d(sAh + (size_t)kb * P::A_KB, &tmCh, fullA, 32 * kb, y0);
+        tma_load_2d(sAl + (size_t)kb * P::A_KB, &tmCl, fullA, 32 * kb, y0);
       }
-      if (!bad0 && !mbar_wait(&fullB[b], (uint32_t)(t >> 1) & 1u)) bad0 = 1;
-      if (!bad0) {
+      for (int t = 0; t < ntile; ++t) {
+        const int b = t & 1;
+        if (t >= 2 && !mbar_wait_ab(&emptyB[b], (uint32_t)((t - 2) >> 1) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        mbar_arrive_expect_tx(&fullB[b], P::B_BYTES);
+        for (int kb = 0; kb < KBLK; ++kb) {
+          tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, t * BN, img);
+          tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, t * BN, img);
+        }
+        last_issued[b] = t;
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {  // MMA issuer
+      constexpr uint32_t IDESC = idesc_tf32(128, BN);
+      bool ok = mbar_wait_ab(fullA, 0, abort);
+      for (int t = 0; ok && t < ntile; ++t) {
+        const int b = t & 1;
+        if (!mbar_wait_ab(&fullB[b], (uint32_t)(t >> 1) & 1u, abort) ||
+            (t >= 2 && !mbar_wait_ab(&accEmpty[b], (uint32_t)((t - 2) >> 1) & 1u, abort))) {
+          ok = false;
+          break;
+        }
         tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * BN);
 #pragma unroll
         for (int kb = 0; kb < KBLK; ++kb) {
           const uint64_t dah = desc_sw128(sAh + (size_t)kb * P::A_KB), dal = desc_sw128(sAl + (size_t)kb * P::A_KB);
@@ -413,58 +443,66 @@ __global__ void __launch_bounds__(128, 1) fi_tc_kernel(const __grid_constant__ C
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint32_t off = kk * 32;
-            mma_tf32(tmem, desc_add(dah, off), desc_add(dbh, off), IDESC, (kb | kk) != 0 ? 1u : 0u);
-            mma_tf32(tmem, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
-            mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+            mma_tf32(acc, desc_add(dah, off), desc_add(dbh, off), IDESC, (kb | kk) != 0 ? 1u : 0u);
+            mma_tf32(acc, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
+            mma_tf32(acc, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
           }
         }
-        mma_commit(mdone);
+        mma_commit(&emptyB[b]);
+        mma_commit(&accFull[b]);
       }
+      if (!ok) *abort = 1;
     }
-    if (__syncthreads_or(bad0)) {
-      bad = 1;
-      break;
-    }
-    if (__syncthreads_or(!mbar_wait(mdone, (uint32_t)t & 1u))) {
-      bad = 1;
-      break;
-    }
-    tc_fence_after();
-    // buffer b is free: prefetch tile t+2 into it
-    if (tid == 0 && issued < ntile) issueB(issued++);
+  } else {  // warps 0-3: epilogue
+    const int row = 32 * warp + lane;
+    int slab_count = 0;
+    for (int t = 0; t < ntile; ++t) {
+      const int b = t & 1;
+      if (!mbar_wait_ab(&accFull[b], (uint32_t)(t >> 1) & 1u, abort)) {
+        *abort = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
-    for (int slab = 0; slab < BN / 32; ++slab) {
-      float v[32];
-      tmem_ld32(trow + (uint32_t)(slab * 32), v);
-      unsigned char* st = sOut + (size_t)(slab & 1) * P::OUT_B;
-      if (tid == 0) bulk_wait_read0();
-      __syncthreads();
-      float4* rowp = reinterpret_cast<float4*>(st + (size_t)row * 128);
+      for (int slab = 0; slab < BN / 32; ++slab, ++slab_count) {
+        float v[32];
+        tmem_ld32(trow + (uint32_t)(slab * 32), v);
+        unsigned char* st = sOut + (size_t)(slab_count & 1) * P::OUT_B;
+        if (tid == 0) bulk_wait_read1();  // the store that used this staging tile has read it
+        named_bar(1, 128);
+        float4* rowp = reinterpret_cast<float4*>(st + (size_t)row * 128);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) rowp[q ^ (row & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-      fence_proxy_async();
-      __syncthreads();
-      if (tid == 0) {
-        tma_store_3d(&tmOut, st, t * BN + slab * 32, y0, img);
-        bulk_commit();
+        for (int q = 0; q < 8; ++q)
+          rowp[q ^ (row & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        fence_proxy_async();
+        named_bar(1, 128);
+        if (tid == 0) {
+          tma_store_3d(&tmOut, st, t * BN + slab * 32, y0, img);
+          bulk_commit();
+        }
       }
+      tc_fence_before();
+      mbar_arrive(&accEmpty[b]);
     }
-    tc_fence_before();
-    __syncthreads();
+    if (tid == 0) bulk_wait0();
   }
-  if (tid == 0) {
-    if (bad) atomicExch(err, 1);
-    bulk_wait0();
-    if (bad) {
-      mma_commit(mdone);
-      mbar_wait(mdone, (uint32_t)t & 1u, 1u << 20);
-      mbar_wait(fullA, 0, 1u << 20);
-      for (int k = t; k < issued; ++k) mbar_wait(&fullB[k & 1], (uint32_t)(k >> 1) & 1u, 1u << 20);
+  __syncthreads();
+  if (*abort) {
+    if (tid == 160) {
+      mma_commit(drain);
+      mbar_wait(drain, 0, 1u << 20);
     }
+    if (tid == 128) {
+      mbar_wait(fullA, 0, 1u << 20);
+      for (int b = 0; b < 2; ++b)
+        if (last_issued[b] >= 0) mbar_wait(&fullB[b], (uint32_t)(last_issued[b] >> 1) & 1u, 1u << 20);
+    }
+    if (tid == 0) atomicExch(err, 1);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, BN);
+  if (warp == 0) tmem_dealloc(tmem, 2 * BN);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,8 +615,8 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
                                            (int)smem));
   dim3 grid((g.Ly + 127) / 128, p.batch);
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
-  win_dft_tc_kernel<NB><<<grid, 128, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
-                                                           win_part, err);
+  win_dft_tc_kernel<NB><<<grid, TC_THREADS, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
+                                                                  win_part, p.part_stride, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
@@ -612,7 +650,7 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
                                            (int)smem));
   dim3 grid((g.Ly + 127) / 128, p.batch);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);
-  fi_tc_kernel<KBLK, BN><<<grid, 128, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, err);
+  fi_tc_kernel<KBLK, BN><<<grid, TC_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
