@@ -604,7 +604,8 @@ ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count) {
   int cs = (want + p.rowBlocks * batch - 1) / (p.rowBlocks * batch);
   cs = std::max(1, std::min(cs, std::max(1, nch / 2)));
   p.colSplits = cs;
-  int ng = (sm_count + batch - 1) / batch;
+  // SOCS is latency-bound (warp-shuffle FFT chains): aim for >= 4 CTAs (32 warps) per SM
+  int ng = (4 * sm_count + batch - 1) / batch;
   ng = std::max(1, std::min(ng, g.nk));
   p.kpg = (g.nk + ng - 1) / ng;
   p.ngroups = (g.nk + p.kpg - 1) / p.kpg;
@@ -884,7 +885,7 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
   w.part = ctx->win_part.as<float2>();
   w.nparts = p.nparts();
   LITHO_RET(run_socs(ctx, p, w, krn, scales, ctx->band_part.as<float2>(), nullptr));
-  if (tc) return run_fi_tc(ctx, p, ctx->band_part.as<float2>(), ctx->tm.as<float>(), images);
+  if (tc) return run_fi_tc(ctx, p, ctx->band_part.as<float2>(), nullptr, images);
   return run_fi(ctx, p, ctx->band_part.as<float2>(), ctx->tm.as<float>(), images);
 }
 

@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [WT_STAGES]
+  int* nzflag = last_issued + WT_STAGES;                  // [WT_STAGES] tile has a nonzero TF32 residual
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
   const int nch = (Lx + 31) / 32;
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
       mbar_init(&ready[s], 128);
       mbar_init(&empty[s], 1);
       last_issued[s] = -1;
+      nzflag[s] = 0;
     }
     mbar_init(done, 1);
     *abort = 0;
@@ -167,6 +169,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
           break;
         }
         tc_fence_after();
+        // the consumers' vote: an all-zero residual (e.g. a 0/1 mask tile) makes Al*Bh exactly zero
+        const bool lo_term = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
+        nzflag[s] = 0;  // the next writers (consumers of chunk c+S) start after this stage's refill
         const uint64_t da = desc_sw128(sA(s)), dal = desc_sw128(sAl(s));
         const uint64_t dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
 #pragma unroll
@@ -174,7 +179,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
           const uint32_t off = kk * 32;
           mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
           mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
-          mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+          if (lo_term) mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
         }
         mma_commit(&empty[s]);
       }
@@ -189,15 +194,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
       }
       float4* a = reinterpret_cast<float4*>(sA(s));
       float4* al = reinterpret_cast<float4*>(sAl(s));
+      bool nz = false;
 #pragma unroll 4
       for (int i = tid; i < (int)(P::A_B / 16); i += 128) {
         const float4 v = a[i];
         const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
+        const float4 l = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
         a[i] = h;
-        al[i] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        al[i] = l;
+        nz |= (l.x != 0.f) | (l.y != 0.f) | (l.z != 0.f) | (l.w != 0.f);
       }
+      if (__any_sync(0xffffffffu, nz) && lane == 0) atomicOr(&nzflag[s], 1);
       fence_proxy_async();
-      mbar_arrive(&ready[s]);
+      mbar_arrive(&ready[s]);  // release: the flag and both tiles are visible to the MMA lane
     }
   }
   // the MMA lane always commits `done`; everyone waits for the tensor cores to drain
@@ -282,14 +291,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
 // ---------------------------------------------------------------------------
 constexpr int FPT_THREADS = 128;
 
+template <int MAXD>
 __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ band_part, int ngroups,
                                                                  int Lx, int Fx, int Nx, int Ny, int KP,
                                                                  float* __restrict__ tmh, float* __restrict__ tml) {
   extern __shared__ __align__(16) float2 fps[];
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
-  float2* sS = fps;                                            // [BH][BW]
-  float2* sT = fps + BH * BW;                                  // [ND][128]
-  float* sO = reinterpret_cast<float*>(sT + ND * FPT_THREADS);  // [128][KP+1]
+  float2* sS = fps;                                     // [BH][BW]
+  float* sO = reinterpret_cast<float*>(fps + BH * BW);  // [128][KP+1]
   const int tid = threadIdx.x, img = blockIdx.y;
   const int X0 = blockIdx.x * FPT_THREADS, X = X0 + tid;
   const float2* B = band_part + (size_t)img * ngroups * BH * BW;
@@ -303,12 +312,14 @@ __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* _
     sS[idx] = make_float2(re, im);
   }
   const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
-  for (int d = 0; d < ND; ++d) {
+  float2 tw[MAXD];
+#pragma unroll
+  for (int d = 0; d < MAXD; ++d) {
     long long m = ((long long)d * xp) % Fx;
     if (m < 0) m += Fx;
     float sn, cs;
     sincospif(2.0f * (float)m / (float)Fx, &sn, &cs);
-    sT[d * FPT_THREADS + tid] = make_float2(cs, sn);
+    tw[d] = d < ND ? make_float2(cs, sn) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   float* o = sO + tid * (KP + 1);
@@ -316,11 +327,14 @@ __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* _
   for (int fy = 0; fy < BH; ++fy) {
     const float2* S = sS + fy * BW + 2 * Nx;
     float re = S[0].x, im = S[0].y;
-    for (int d = 1; d < ND; ++d) {
-      const float2 t = sT[d * FPT_THREADS + tid];
-      const float2 p = S[d], q = S[-d];
-      re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
-      im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+#pragma unroll
+    for (int d = 1; d < MAXD; ++d) {
+      if (d < ND) {
+        const float2 t = tw[d];
+        const float2 p = S[d], q = S[-d];
+        re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
+        im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+      }
     }
     if (fy == 0) {
       o[0] = re;
@@ -655,7 +669,13 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   return LITHO_OK;
 }
 
-int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images) {
+size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch) {
+  return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float);
+}
+
+// tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
+// nullptr to use the context's grow-only buffer.
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images) {
   const ImgGeom& g = p.g;
   const int KBLK = kblk_for(g.Ny);
   const int KP = 32 * KBLK;
@@ -674,20 +694,23 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   // TmT hi/lo: [batch][Lx][KP]
-  LITHO_RET(ctx->mx_b.ensure(ctx, (size_t)2 * p.batch * g.Lx * KP * sizeof(float)));
-  float* tmh = ctx->mx_b.as<float>();
+  float* tmh = tmT;
+  if (tmh == nullptr) {
+    LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(g, p.batch)));
+    tmh = ctx->mx_b.as<float>();
+  }
   float* tml = tmh + (size_t)p.batch * g.Lx * KP;
   {
     const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
-    const size_t smem = ((size_t)BH * BW + (size_t)ND * FPT_THREADS) * sizeof(float2) +
-                        (size_t)FPT_THREADS * (KP + 1) * sizeof(float);
-    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_prep_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = (size_t)BH * BW * sizeof(float2) + (size_t)FPT_THREADS * (KP + 1) * sizeof(float);
+    auto k = ND <= 5 ? fi_prep_tc_kernel<5> : ND <= 9 ? fi_prep_tc_kernel<9> : ND <= 17 ? fi_prep_tc_kernel<17>
+                                                                                        : fi_prep_tc_kernel<33>;
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     StageScope sc(ctx, LITHO_STAGE_FI_PREP);
-    fi_prep_tc_kernel<<<dim3((g.Lx + FPT_THREADS - 1) / FPT_THREADS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
+    k<<<dim3((g.Lx + FPT_THREADS - 1) / FPT_THREADS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
         band_part, p.ngroups, g.Lx, g.Fx, g.Nx, g.Ny, KP, tmh, tml);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  (void)tm;
   switch (KBLK) {
     case 1: return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);
     case 2: return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);

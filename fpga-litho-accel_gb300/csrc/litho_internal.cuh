@@ -161,7 +161,8 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
-int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images);
+size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch);
 bool tc_supported(const ImgGeom& g);
 int tc_check_flag(litho_ctx* ctx);
 
