@@ -213,10 +213,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
   if (!mbar_wait(done, 0)) *abort = 1;
   __syncthreads();
   if (*abort) {
-    if (tid == 160) mbar_wait(done, 0, 1u << 20);  // the MMA lane's final commit covers all it issued
+    if (tid == 160) mbar_wait(done, 0, 200u);  // the MMA lane's final commit covers all it issued
     if (tid == 128)  // warp 4 lane 0: wait for the last load of every stage (bounded)
       for (int s = 0; s < WT_STAGES; ++s)
-        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / WT_STAGES) & 1u, 1u << 20);
+        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / WT_STAGES) & 1u, 200u);
     if (tid == 0) atomicExch(err, 1);
     tc_fence_before();
     __syncthreads();
@@ -505,12 +505,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_const
   if (*abort) {
     if (tid == 160) {
       mma_commit(drain);
-      mbar_wait(drain, 0, 1u << 20);
+      mbar_wait(drain, 0, 200u);
     }
     if (tid == 128) {
-      mbar_wait(fullA, 0, 1u << 20);
+      mbar_wait(fullA, 0, 200u);
       for (int b = 0; b < 2; ++b)
-        if (last_issued[b] >= 0) mbar_wait(&fullB[b], (uint32_t)(last_issued[b] >> 1) & 1u, 1u << 20);
+        if (last_issued[b] >= 0) mbar_wait(&fullB[b], (uint32_t)(last_issued[b] >> 1) & 1u, 200u);
     }
     if (tid == 0) atomicExch(err, 1);
   }

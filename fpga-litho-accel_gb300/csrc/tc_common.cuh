@@ -43,20 +43,30 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 23) {
-  for (uint32_t i = 0; i < limit; ++i) {
-    if (mbar_test(bar, parity)) return true;
-    if (i > 32) __nanosleep(64);
-  }
+// try_wait suspends the thread until the phase completes or `hint_ns` elapses,
+// so a waiting role wakes as soon as its data is there (no sleep/poll latency).
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+// bounded: at most `limit` suspensions of <= 1 ms each
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1000) {
+  for (uint32_t i = 0; i < limit; ++i)
+    if (mbar_try(bar, parity, 1000000u)) return true;
   return false;
 }
-// As mbar_wait, but also gives up as soon as *abort (shared, set by another role) is non-zero.
+// As mbar_wait, but also gives up as soon as *abort (shared, set by another role)
+// is non-zero; suspensions are 20 us so the flag is looked at regularly.
 __device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, uint32_t parity, volatile int* abort,
-                                             uint32_t limit = 1u << 23) {
+                                             uint32_t limit = 50000) {
   for (uint32_t i = 0; i < limit; ++i) {
-    if (mbar_test(bar, parity)) return true;
+    if (mbar_try(bar, parity, 20000u)) return true;
     if (*abort) return false;
-    if (i > 32) __nanosleep(64);
   }
   return false;
 }

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
     if (!mbar_wait(done, 0)) bad = 1;
     if (bad) {
       atomicExch(err, 1);
-      for (int k = c; k < issued; ++k) mbar_wait(&full[k % GB_STAGES], (uint32_t)(k / GB_STAGES) & 1u, 1u << 20);
+      for (int k = c; k < issued; ++k) mbar_wait(&full[k % GB_STAGES], (uint32_t)(k / GB_STAGES) & 1u, 200u);
     }
   }
   if (__syncthreads_or(bad)) {

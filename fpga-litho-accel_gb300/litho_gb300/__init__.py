@@ -69,7 +69,27 @@ _SIGS = {
     "litho_calc_kernels": (_i, [_p, _p, _i, _i, _p, _p, _p, _p, _p, _i]),
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
+    "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
+    "litho_batch_plan_mask": (_p, [_p, _i]),
+    "litho_batch_plan_image": (_p, [_p, _i]),
+    "litho_batch_plan_run": (_i, [_p]),
+    "litho_batch_plan_describe": (_i, [_p, C.c_char_p, _i]),
+    "litho_batch_plan_destroy": (_i, [_p]),
 }
+BATCH_AUTOTUNE = 1
+BATCH_GRAPH = 2
+
+
+class _BatchItem(C.Structure):
+    _fields_ = [("cls", C.c_int), ("mLx", C.c_int), ("mLy", C.c_int)]
+
+
+class _DevArray:
+    """A raw device buffer exposed through __cuda_array_interface__ (float32, C order)."""
+
+    def __init__(self, ptr: int, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
 STAGES = ("win_dft", "socs", "fi_prep", "fi_out", "fft_mask", "tcc", "eig", "upload")
 for _name, (_res, _args) in _SIGS.items():
     _fn = getattr(_lib, _name)
@@ -139,6 +159,58 @@ class KernelSet:
     def close(self):
         if self.h:
             _lib.litho_kernel_set_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchPlan:
+    """Masks of uneven sizes imaged per size class in one CUDA graph (litho_batch_plan_*).
+
+    ``sets``/``periods``: one KernelSet and power-of-two period per size class;
+    ``items``: (cls, mLx, mLy) per mask.  ``mask(i)``/``image(i)`` return torch
+    views of the plan's device slots.
+    """
+
+    def __init__(self, ctx: "Context", sets, periods, items, precision: int = PREC_FP32,
+                 flags: int = BATCH_AUTOTUNE | BATCH_GRAPH):
+        self.ctx = ctx
+        self.items = [tuple(int(v) for v in it) for it in items]
+        self.periods = [int(p) for p in periods]
+        hs = (C.c_void_p * len(sets))(*[s.h for s in sets])
+        ps = (C.c_int * len(periods))(*self.periods)
+        arr = (_BatchItem * len(items))(*[_BatchItem(c, x, y) for c, x, y in self.items])
+        h = C.c_void_p()
+        ctx._check(_lib.litho_batch_plan_create(ctx.h, C.cast(hs, C.c_void_p), C.cast(ps, C.c_void_p), len(sets),
+                                                C.cast(arr, C.c_void_p), len(items), precision, flags, C.byref(h)))
+        self.h = h
+
+    def mask(self, i: int):
+        import torch
+        c, x, y = self.items[i]
+        return torch.as_tensor(_DevArray(_lib.litho_batch_plan_mask(self.h, i), (y, x)), device="cuda")
+
+    def image(self, i: int):
+        import torch
+        L_ = self.periods[self.items[i][0]]
+        return torch.as_tensor(_DevArray(_lib.litho_batch_plan_image(self.h, i), (L_, L_)), device="cuda")
+
+    def run(self):
+        self.ctx._check(_lib.litho_batch_plan_run(self.h))
+
+    def describe(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        _lib.litho_batch_plan_describe(self.h, buf, len(buf))
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if self.h:
+            _lib.litho_batch_plan_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -152,6 +152,35 @@ int litho_kernel_set_destroy(litho_kernel_set* ks);
 int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* masks,
                       int batch, int Lx, int Ly, float* images, int precision, int mem);
 
+/* ---- batched imaging of masks of uneven sizes in one CUDA graph -----------
+ * No single reference function: the reference images one mask per litho run
+ * (validation/batch_test_runner.py:30-171 loops over masks).  Each item names
+ * a size class (a kernel set and its period L, a power of two) and its mask
+ * size mLx x mLy <= L; as common/mask.cpp:31-60 createMask does, a smaller mask
+ * is centred in the period and the image is L x L.  The plan owns device slots
+ * for every mask and image, chooses per size class the conv grid (FFT plan),
+ * the kernels per CTA and the window-DFT split by timing candidates on the
+ * device (LITHO_BATCH_AUTOTUNE), and captures all stages of all classes in one
+ * CUDA graph (LITHO_BATCH_GRAPH) that litho_batch_plan_run launches. */
+typedef struct {
+  int cls;        /* index into the kernel-set / period arrays */
+  int mLx, mLy;   /* mask size, <= the class period */
+} litho_batch_item;
+typedef struct litho_batch_plan litho_batch_plan;
+#define LITHO_BATCH_AUTOTUNE 1
+#define LITHO_BATCH_GRAPH    2
+int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets, const int* periods, int nsets,
+                            const litho_batch_item* items, int n, int precision, int flags,
+                            litho_batch_plan** out);
+/* device slot of item i's mask (mLy x mLx float32) and image (L x L float32) */
+float* litho_batch_plan_mask(litho_batch_plan* plan, int i);
+float* litho_batch_plan_image(litho_batch_plan* plan, int i);
+/* image every item: one graph launch (or the plain launch sequence) on the context's stream */
+int litho_batch_plan_run(litho_batch_plan* plan);
+/* JSON description of the tuned choices per size class; returns the length written */
+int litho_batch_plan_describe(const litho_batch_plan* plan, char* buf, int cap);
+int litho_batch_plan_destroy(litho_batch_plan* plan);
+
 /* ---- mask -> image with no device allocation ------------------------------
  * No counterpart in the reference.  For callers that cannot let a library call
  * cudaMalloc/cudaFree: those calls synchronise the whole device (a latency-

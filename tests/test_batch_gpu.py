@@ -1,0 +1,82 @@
+"""Batched imaging of masks of uneven sizes in one CUDA graph (litho_batch_plan_*).
+
+Each mask is imaged in the period of its size class; a mask smaller than the
+period is centred in it (common/mask.cpp:31-60 createMask), so the oracle is
+create_mask + FT_r2c_padded + calcSOCS on the padded mask.
+"""
+import numpy as np
+import pytest
+
+from oracle import np_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def L():
+    import litho_gb300
+    return litho_gb300
+
+
+@pytest.fixture(scope="module")
+def ctx(L):
+    c = L.Context(0)
+    yield c
+    c.close()
+
+
+def _kernels(Lp, src, K):
+    sig = R.get_outer_sigma(src)
+    nx = R.optics_nx(0.8, Lp, sig, 193.0)
+    tcc = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, Lp, Lp, nx, nx)
+    krns, scales, _ = R.calc_kernels(tcc, K)
+    return krns, scales, nx
+
+
+@pytest.fixture(scope="module")
+def classes():
+    from litho_gb300 import synth
+    k0 = _kernels(512, synth.annular_source(21, 0.6, 0.9), 8)
+    k1 = _kernels(1024, synth.quasar_source(2000)[0], 12)
+    return [(512, k0), (1024, k1)]
+
+
+@pytest.mark.parametrize("prec_name,tol", [("fp32", 1e-5), ("mixed", 1e-4)])
+def test_batch_plan_uneven_sizes(ctx, L, classes, prec_name, tol):
+    import torch
+    from litho_gb300 import synth
+    prec = L.PREC_FP32 if prec_name == "fp32" else L.PREC_MIXED
+    sets = [ctx.kernel_set(k[0], k[1], k[2], k[2]) for _, k in classes]
+    periods = [p for p, _ in classes]
+    items = [(0, 256, 256), (1, 512, 512), (0, 512, 512), (1, 1024, 1024), (1, 768, 768), (0, 256, 256)]
+    plan = L.BatchPlan(ctx, sets, periods, items, precision=prec)
+    masks = [synth.density_rect_mask(m, 0.2 + 0.08 * i, seed=60 + i) for i, (_, m, _) in enumerate(items)]
+    for i, m in enumerate(masks):
+        plan.mask(i).copy_(torch.from_numpy(m))
+    torch.cuda.synchronize()
+    for rep in range(2):   # the captured graph is replayed
+        plan.run()
+        ctx.synchronize()
+        for i, (c, m, _) in enumerate(items):
+            Lp = periods[c]
+            krns, scales, nx = classes[c][1]
+            ref = R.mask_to_image(R.create_mask(masks[i], Lp, Lp), krns, scales, nx, nx)
+            got = plan.image(i).cpu().numpy()
+            assert R.rel_l2(got, ref) < tol, (prec_name, rep, i)
+    info = plan.describe()
+    assert info["graph"] is True
+    assert {c["period"] for c in info["classes"]} == {512, 1024}
+    assert all(c["candidates"] >= 0 and c["conv_n"] >= 32 for c in info["classes"])
+    plan.close()
+    for s in sets:
+        s.close()
+
+
+def test_batch_plan_rejects_bad_items(ctx, L, classes):
+    sets = [ctx.kernel_set(k[0], k[1], k[2], k[2]) for _, k in classes]
+    with pytest.raises(L.LithoError):
+        L.BatchPlan(ctx, sets, [512, 1024], [(0, 1024, 1024)])    # mask larger than its period
+    with pytest.raises(L.LithoError):
+        L.BatchPlan(ctx, sets, [500, 1024], [(0, 256, 256)])      # period not a power of two
+    for s in sets:
+        s.close()
