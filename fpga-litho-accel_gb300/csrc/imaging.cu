@@ -158,14 +158,6 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
     }
     __syncthreads();
     if (ch + 1 < ch1) loadA(ch + 1);
-    if (VEC && ch + 4 < ch1) {  // keep more of the mask stream in flight: L2 prefetch 4 chunks ahead
-      const int x0 = (ch + 4) * WD_BK + lc4;
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int row = y0 + lr + 16 * i;
-        if (row < Ly && x0 + 3 < Lx) asm volatile("prefetch.global.L2 [%0];" ::"l"(M + (size_t)row * Lx + x0));
-      }
-    }
 #pragma unroll 2
     for (int kk = 0; kk < WD_BK / 8; ++kk) {
       const int k = warp * (WD_BK / 8) + kk;

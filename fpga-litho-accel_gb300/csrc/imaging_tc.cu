@@ -146,11 +146,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
 
   if (warp == 4) {
     if (lane == 0) {  // TMA producer
-      constexpr int PF = 2 * WT_STAGES;  // L2 prefetch distance in chunks
-      for (int c = 0; c < min(nch, PF); ++c) tma_prefetch_3d(&tmM, 32 * c, y0, img);
       for (int c = 0; c < nch; ++c) {
         const int s = c % WT_STAGES;
-        if (c + PF < nch) tma_prefetch_3d(&tmM, 32 * (c + PF), y0, img);
         if (c >= WT_STAGES && !mbar_wait_ab(&empty[s], (uint32_t)((c - WT_STAGES) / WT_STAGES) & 1u, abort)) {
           *abort = 1;
           break;

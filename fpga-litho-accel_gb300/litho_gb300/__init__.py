@@ -67,6 +67,7 @@ _SIGS = {
     "litho_image_batch": (_i, [_p, _p, _p, _i, _i, _i, _p, _i, _i]),
     "litho_calc_tcc": (_i, [_p, _p, _i, _f, _f, _f, _f, _i, _i, _i, _i, _p, _i, _i]),
     "litho_calc_kernels": (_i, [_p, _p, _i, _i, _p, _p, _p, _p, _p, _i]),
+    "litho_calc_image": (_i, [_p, _p, _p, _i, _i, _p, _i, _i, _i, _i, _i, _p, _i]),
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
@@ -308,6 +309,16 @@ class Context:
                                          _ptr(kr), _ptr(ki), _ptr(s), nk, Nx, Ny, phys_x, phys_y,
                                          _ptr(image), _ptr(tmp), conv_n, MEM_HOST))
         return (image, tmp) if want_tmpimgp else image
+
+    # -- calcImage (TCC-direct) ------------------------------------------------
+    def calc_image(self, mskf_r, mskf_i, tcc, Nx: int, Ny: int, phys_x: int, phys_y: int):
+        """calcImage + FT_c2r_padded (litho.cpp:522-566, 358-408): TCC-direct image."""
+        Fy, Fx = mskf_r.shape
+        t = np.ascontiguousarray(tcc, dtype=np.complex128)
+        out = np.empty((phys_y, phys_x), np.float32)
+        self._check(_lib.litho_calc_image(self.h, _ptr(_host_f32(mskf_r)), _ptr(_host_f32(mskf_i)), Fx, Fy,
+                                          _ptr(t), t.shape[0], Nx, Ny, phys_x, phys_y, _ptr(out), MEM_HOST))
+        return out
 
     # -- fused mask -> image ---------------------------------------------------
     def image(self, mask, krn, scales, Nx: int, Ny: int, precision: int = PREC_FP32):

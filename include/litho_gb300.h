@@ -132,6 +132,12 @@ int litho_calc_socs(litho_ctx* ctx, const float* mskf_r, const float* mskf_i,
                     const float* scales, int nk, int Nx, int Ny, int physLx, int physLy,
                     float* image, float* tmpImgp, int convN, int mem);
 
+/* ---- TCC-direct image (litho.cpp:522-566 calcImage + 358-408 FT_c2r_padded)
+ * mskf planes (fftLy x fftLx) and the interleaved float64 TCC -> physLy x physLx
+ * image, accumulated in FP64 exactly as calcImage orders the terms. */
+int litho_calc_image(litho_ctx* ctx, const float* mskf_r, const float* mskf_i, int fftLx, int fftLy,
+                     const double* tcc, int tccSize, int Nx, int Ny, int physLx, int physLy, float* image, int mem);
+
 /* ---- fused mask -> aerial image (FT_r2c_padded + calcSOCS, litho.cpp:1318-1451)
  * One mask (Ly x Lx) to one image (Ly x Lx).  Only the (2Ny+1)x(2Nx+1) window
  * of the spectrum is formed (a partial DFT), so the full spectrum never
