@@ -135,6 +135,10 @@ struct ImgPlan {
 
 ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count);
 
+int calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength, float NA,
+                  float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision, int mem, int sh_in,
+                  int oSgm_in);
+
 // Host input -> device staging buffer (device input passes through).
 int stage_in(litho_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem, const void** dev);
 

@@ -130,10 +130,16 @@ __global__ void __launch_bounds__(256) tcc_fp64_kernel(const float2* __restrict_
 // Host side: enumerate lit source points in the reference's loop order and
 // check that every pupil point the reference would store lies on the grid.
 int tcc_sources(litho_ctx* ctx, const float* src_h, int S, float outerSigma, float wavelength, float NA,
-                float defocus, int Lx, int Ly, int Nx, int Ny, std::vector<SrcPt>& pts, PupilParams& pp) {
-  const int sh = (int)((S - 1) / 2.0);
+                float defocus, int Lx, int Ly, int Nx, int Ny, std::vector<SrcPt>& pts, PupilParams& pp,
+                int sh_in = -1, int oSgm_in = -1) {
+  // litho.cpp:429-430; the FPGA top (calc_tcc.cpp:34-42) receives sh and oSgm from its caller instead
+  const int sh = sh_in >= 0 ? sh_in : (int)((S - 1) / 2.0);
   volatile float osf = (float)sh * outerSigma;
-  const int oSgm = (int)std::ceil((float)osf);
+  const int oSgm = oSgm_in >= 0 ? oSgm_in : (int)std::ceil((float)osf);
+  if (sh <= 0) {
+    set_error(ctx, LITHO_ERR_ARG, "source grid %d too small (sh = %d)", S, sh);
+    return LITHO_ERR_ARG;
+  }
   volatile float nana = NA * NA;
   volatile float q0 = nana / wavelength;
   volatile float dz = defocus / q0;
@@ -209,9 +215,11 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
 
 using namespace litho;
 
-extern "C" int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength,
-                              float NA, float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision,
-                              int mem) {
+// sh_in / oSgm_in >= 0 override the source half-size and loop bound (the FPGA
+// top receives them from its caller); -1 derives them as litho.cpp:429-430.
+int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength,
+                         float NA, float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision,
+                         int mem, int sh_in, int oSgm_in) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_ARG_CHECK(ctx, src && tcc, "null pointer");
   LITHO_ARG_CHECK(ctx, srcSize >= 1 && srcSize <= 4097, "srcSize %d outside [1, 4097]", srcSize);
@@ -232,7 +240,8 @@ extern "C" int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, flo
   }
   std::vector<SrcPt> pts;
   PupilParams pp;
-  LITHO_RET(tcc_sources(ctx, sh, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, pts, pp));
+  LITHO_RET(tcc_sources(ctx, sh, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, pts, pp, sh_in,
+                        oSgm_in));
   const int n = pp.tccSize, ns = pp.ns;
   const int ldp = ((ns + 63) / 64) * 64 + 64;  // padded, multiple of 64 (tensor-core K tiles)
   LITHO_RET(ctx->tcc_a.ensure(ctx, (size_t)n * ldp * sizeof(float2)));
@@ -270,4 +279,11 @@ extern "C" int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, flo
       }
   }
   return LITHO_OK;
+}
+
+extern "C" int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength,
+                              float NA, float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision,
+                              int mem) {
+  return litho::calc_tcc_impl(ctx, src, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, tcc,
+                              tccPrecision, mem, -1, -1);
 }

@@ -112,6 +112,28 @@ float litho_outer_sigma(const float* src, int srcSize);
 /* Nx = floor(NA * L * (1 + outerSigma) / lambda) evaluated in float32. */
 int litho_optics_n(float NA, int L, float outerSigma, float wavelength);
 
+/* ---- sources, masks and files (host only; validation/golden/src/common/) --- */
+#define LITHO_SRC_ANNULAR          0  /* params: innerRadius, outerRadius          source.cpp:5-23  */
+#define LITHO_SRC_DIPOLE           1  /* params: radius, offset, onXAxis (0/1)     source.cpp:58-87 */
+#define LITHO_SRC_CROSS_QUADRUPOLE 2  /* params: radius, offset                    source.cpp:25-56 */
+#define LITHO_SRC_POINT            3  /* params: x, y                              source.cpp:121-128 */
+#define LITHO_SRC_KEEP             4  /* reserved: an imported source is normalised with litho_normalize_source */
+/* createSource (source.cpp:105-141): fill src (S x S) and, if normalize, scale to
+ * unit sum with the reference's sequential float32 sum. */
+int litho_create_source(float* src, int srcSize, int type, const float* params, int normalize);
+int litho_normalize_source(float* src, int srcSize);
+/* generateLineSpace (mask.cpp:5-29) */
+int litho_create_linespace(float* mask, int sizeX, int sizeY, int lineWidth, int spaceWidth, int horizontal);
+/* createMask placement (mask.cpp:52-59): centre maskX x maskY in the Lx x Ly period, times dose */
+int litho_place_mask(const float* in, int maskX, int maskY, float dose, float* out, int Lx, int Ly);
+/* BIN files (file_io.cpp:137-150, 232-259): raw float32; reading a file of the
+ * wrong size warns and truncates / zero-pads, as the reference does */
+int litho_write_bin(const char* path, const float* data, long long n);
+int litho_read_bin(const char* path, float* data, long long n);
+/* kernels/kernel_info.txt (file_io.cpp:262-307) */
+int litho_write_kernel_info(const char* path, int krnX, int krnY, int nk, const float* scales);
+int litho_read_kernel_info(const char* path, int* krnX, int* krnY, int* nk, float* scales, int cap);
+
 /* ---- mask spectrum (litho.cpp:242-318 FT_r2c_padded) --------------------
  * mask: Ly x Lx.  Outputs fftLy x fftLx planes with fftL = nextPow2(L); DC at
  * (fftLy/2, fftLx/2), divided by fftLx*fftLy. */
