@@ -87,45 +87,60 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // ---------------------------------------------------------------------------
 // window DFT on the tensor cores
 // ---------------------------------------------------------------------------
-constexpr int WT_STAGES = 5;
 constexpr int TC_THREADS = 192;
 
 template <int NB>
 struct WinTC {
-  static constexpr uint32_t A_B = 128 * 128;   // 128 rows x 32 fp32
-  static constexpr uint32_t B_B = NB * 128;    // NB rows x 32 fp32
-  static constexpr uint32_t STAGE_B = 2 * A_B + 2 * B_B;
+  static constexpr int STAGES = NB <= 32 ? 4 : 3;  // two CTAs per SM fit in shared memory
+  static constexpr uint32_t A_B = 128 * 128;       // 128 rows x 32 fp32 (split in place: hi, then lo)
+  static constexpr uint32_t B_B = NB * 128;        // NB rows x 32 fp32
+  static constexpr uint32_t STAGE_B = A_B + 2 * B_B;
   static constexpr uint32_t NCOL = NB <= 32 ? 32 : 64;
-  static constexpr size_t SMEM = 1024 + (size_t)WT_STAGES * STAGE_B + 256;
+  static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_B + 512;
 };
 
+// Per stage s and chunk c (parity ph = (c / STAGES) & 1):
+//   producer  : [wait empty[s]] -> TMA mask tile + twiddle hi/lo tiles -> full[s]
+//   consumers : wait full[s]; keep the tile in registers; write Ah = round_tf32(A)
+//               in place; vote whether the residual A - Ah is non-zero (nzflag);
+//               arrive ready[s]; if it is: wait hidone[s], overwrite the tile with
+//               the residual Al, arrive ready2[s]
+//   MMA lane  : wait ready[s]; Ah*Bh + Ah*Bl; if residual: commit hidone[s], wait
+//               ready2[s], Al*Bh; commit empty[s]
+// hidone/ready2 only complete on chunks with a residual, so their parities are
+// tracked per stage in a bit mask that both sides flip identically.
 template <int NB>
-__global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
+__global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
                                                                    const __grid_constant__ CUtensorMap tmBh,
                                                                    const __grid_constant__ CUtensorMap tmBl,
                                                                    int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
                                                                    float2* __restrict__ win_part, int part_stride,
                                                                    int* __restrict__ err) {
   using P = WinTC<NB>;
+  constexpr int S = P::STAGES;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + WT_STAGES * P::STAGE_B);
-  uint64_t* ready = full + WT_STAGES;
-  uint64_t* empty = ready + WT_STAGES;
-  uint64_t* done = empty + WT_STAGES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + S * P::STAGE_B);
+  uint64_t* ready = full + S;
+  uint64_t* hidone = ready + S;
+  uint64_t* ready2 = hidone + S;
+  uint64_t* empty = ready2 + S;
+  uint64_t* done = empty + S;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
-  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [WT_STAGES]
-  int* nzflag = last_issued + WT_STAGES;                  // [WT_STAGES] tile has a nonzero TF32 residual
+  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [S]
+  int* nzflag = last_issued + S;                          // [S]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
   const int nch = (Lx + 31) / 32;
 
   if (warp == 0) tmem_alloc(tslot, P::NCOL);
   if (tid == 0) {
-    for (int s = 0; s < WT_STAGES; ++s) {
+    for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&ready[s], 128);
+      mbar_init(&hidone[s], 1);
+      mbar_init(&ready2[s], 128);
       mbar_init(&empty[s], 1);
       last_issued[s] = -1;
       nzflag[s] = 0;
@@ -140,15 +155,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
   const uint32_t tmem = *tslot;
 
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
-  auto sAl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
-  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B; };
-  auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + 2 * P::A_B + P::B_B; };
+  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
+  auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B + P::B_B; };
 
   if (warp == 4) {
     if (lane == 0) {  // TMA producer
       for (int c = 0; c < nch; ++c) {
-        const int s = c % WT_STAGES;
-        if (c >= WT_STAGES && !mbar_wait_ab(&empty[s], (uint32_t)((c - WT_STAGES) / WT_STAGES) & 1u, abort)) {
+        const int s = c % S;
+        if (c >= S && !mbar_wait_ab(&empty[s], (uint32_t)((c - S) / S) & 1u, abort)) {
           *abort = 1;
           break;
         }
@@ -162,51 +176,77 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
   } else if (warp == 5) {
     if (lane == 0) {  // MMA issuer
       constexpr uint32_t IDESC = idesc_tf32(128, NB);
+      uint32_t ph2 = 0;  // per-stage parity of hidone / ready2
       for (int c = 0; c < nch; ++c) {
-        const int s = c % WT_STAGES;
-        if (!mbar_wait_ab(&ready[s], (uint32_t)(c / WT_STAGES) & 1u, abort)) {
+        const int s = c % S;
+        if (!mbar_wait_ab(&ready[s], (uint32_t)(c / S) & 1u, abort)) {
           *abort = 1;
           break;
         }
         tc_fence_after();
-        // the consumers' vote: an all-zero residual (e.g. a 0/1 mask tile) makes Al*Bh exactly zero
-        const bool lo_term = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
-        nzflag[s] = 0;  // the next writers (consumers of chunk c+S) start after this stage's refill
-        const uint64_t da = desc_sw128(sA(s)), dal = desc_sw128(sAl(s));
-        const uint64_t dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
+        const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
+        nzflag[s] = 0;  // every consumer read it before arriving on ready[s]
+        const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
           const uint32_t off = kk * 32;
           mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
           mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
-          if (lo_term) mma_tf32(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+        }
+        if (two) {
+          mma_commit(&hidone[s]);
+          if (!mbar_wait_ab(&ready2[s], (ph2 >> s) & 1u, abort)) {
+            *abort = 1;
+            break;
+          }
+          ph2 ^= 1u << s;
+          tc_fence_after();
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint32_t off = kk * 32;
+            mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, 1u);
+          }
         }
         mma_commit(&empty[s]);
       }
       mma_commit(done);  // arrives once everything issued above has completed
     }
-  } else {  // warps 0-3: split the landed tile into hi (in place) and lo
+  } else {  // warps 0-3: split the landed tile in place
+    uint32_t ph2 = 0;
     for (int c = 0; c < nch; ++c) {
-      const int s = c % WT_STAGES;
-      if (!mbar_wait_ab(&full[s], (uint32_t)(c / WT_STAGES) & 1u, abort)) {
+      const int s = c % S;
+      if (!mbar_wait_ab(&full[s], (uint32_t)(c / S) & 1u, abort)) {
         *abort = 1;
         break;
       }
       float4* a = reinterpret_cast<float4*>(sA(s));
-      float4* al = reinterpret_cast<float4*>(sAl(s));
+      float4 v[8];
       bool nz = false;
-#pragma unroll 4
-      for (int i = tid; i < (int)(P::A_B / 16); i += 128) {
-        const float4 v = a[i];
-        const float4 h = make_float4(tf32_round(v.x), tf32_round(v.y), tf32_round(v.z), tf32_round(v.w));
-        const float4 l = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
-        a[i] = h;
-        al[i] = l;
-        nz |= (l.x != 0.f) | (l.y != 0.f) | (l.z != 0.f) | (l.w != 0.f);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        v[i] = a[tid + 128 * i];
+        const float4 h = make_float4(tf32_round(v[i].x), tf32_round(v[i].y), tf32_round(v[i].z), tf32_round(v[i].w));
+        a[tid + 128 * i] = h;
+        nz |= (v[i].x != h.x) | (v[i].y != h.y) | (v[i].z != h.z) | (v[i].w != h.w);
       }
       if (__any_sync(0xffffffffu, nz) && lane == 0) atomicOr(&nzflag[s], 1);
       fence_proxy_async();
-      mbar_arrive(&ready[s]);  // release: the flag and both tiles are visible to the MMA lane
+      named_bar(1, 128);
+      const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
+      mbar_arrive(&ready[s]);  // release: Ah visible to the MMA lane
+      if (two) {
+        if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        ph2 ^= 1u << s;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          a[tid + 128 * i] = make_float4(v[i].x - tf32_round(v[i].x), v[i].y - tf32_round(v[i].y),
+                                         v[i].z - tf32_round(v[i].z), v[i].w - tf32_round(v[i].w));
+        fence_proxy_async();
+        mbar_arrive(&ready2[s]);
+      }
     }
   }
   // the MMA lane always commits `done`; everyone waits for the tensor cores to drain
@@ -214,9 +254,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) win_dft_tc_kernel(const __grid_
   __syncthreads();
   if (*abort) {
     if (tid == 160) mbar_wait(done, 0, 200u);  // the MMA lane's final commit covers all it issued
-    if (tid == 128)  // warp 4 lane 0: wait for the last load of every stage (bounded)
-      for (int s = 0; s < WT_STAGES; ++s)
-        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / WT_STAGES) & 1u, 200u);
+    if (tid == 128)                            // warp 4 lane 0: wait for the last load of every stage
+      for (int s = 0; s < S; ++s)
+        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / S) & 1u, 200u);
     if (tid == 0) atomicExch(err, 1);
     tc_fence_before();
     __syncthreads();
