@@ -13,7 +13,7 @@
 // Autotuning (LITHO_BATCH_AUTOTUNE) times, per class, every candidate of
 //   conv grid N in {nextPow2(4N+1), 2x that} (the FFT plan of the SOCS stage),
 //   kernels per CTA in {2, 3, 4, 6, 8, 12} (the SOCS tile), and
-//   window column splits in {1, 2} (FP32 window DFT only)
+//   window column splits in {1, 2}
 // with CUDA events on the context's stream and keeps the fastest; results are
 // cached on the context by (L, Nx, nk, images, precision).  The plan then
 // captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH).
@@ -90,7 +90,7 @@ static int run_class(litho_batch_plan* bp, int ci) {
     if (s.cls != ci) continue;
     ImgGeom gw{s.mLx, s.mLy, c.L, c.L, Nx, Ny, c.ks->nk, c.convN};
     ImgPlan pw = make_plan(gw, s.count, ctx->sm_count);
-    pw.colSplits = tc ? 1 : std::min(c.colSplits, std::max(1, (s.mLx + 63) / 64));
+    pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 31) / 32 / 4 : (s.mLx + 63) / 64));
     pw.part_stride = c.part_stride;
     float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
     if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));
@@ -153,8 +153,7 @@ static int tune_class(litho_batch_plan* bp, int ci) {
   for (int k : {2, 3, 4, 6, 8, 12})
     if (k <= c.ks->nk) kpgs.push_back(k);
   if (kpgs.empty()) kpgs.push_back(1);
-  std::vector<int> splits{1};
-  if (bp->precision != LITHO_PREC_MIXED) splits.push_back(2);
+  std::vector<int> splits{1, 2};
   TuneVal best{n0, kpgs[0], 1, 1e30};
   for (int cn : convs)
     for (int k : kpgs)
@@ -277,7 +276,7 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
   for (auto& c : bp->classes) {
     if (c.count == 0) continue;
     const int Nx = c.ks->Nx, Ny = c.ks->Ny, KY = 2 * Ny + 1;
-    c.part_stride = ((c.maxM + 127) / 128) * (precision == LITHO_PREC_MIXED ? 1 : 2);
+    c.part_stride = ((c.maxM + 127) / 128) * 2;  // row blocks x up to two column splits
     rc = c.win.ensure(ctx, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2));
     if (rc == LITHO_OK) rc = c.band.ensure(ctx, (size_t)c.count * c.ks->nk * KY * (4 * Nx + 1) * sizeof(float2));
     const ImgGeom g = class_geom(c, c.convN);

@@ -871,12 +871,17 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
                    const float* scales, float* images, int precision) {
   ImgPlan p = make_plan(g, batch, ctx->sm_count);
   const int KY = 2 * g.Ny + 1;
+  const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
+  if (tc) {
+    // tensor-core window: 32-column chunks, split so ~4 CTAs per SM are available
+    const int nch = (g.Lx + 31) / 32;
+    const int cs = (4 * ctx->sm_count + p.rowBlocks * batch - 1) / (p.rowBlocks * batch);
+    p.colSplits = std::max(1, std::min(cs, std::min(4, nch / 4)));
+  }
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->tm.ensure(ctx, (size_t)batch * (4 * g.Ny + 1) * g.Lx * sizeof(float)));
-  const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
   if (tc) {
-    p.colSplits = 1;
     LITHO_RET(run_win_dft_tc(ctx, p, masks, ctx->win_part.as<float2>()));
   } else {
     LITHO_RET(run_win_dft(ctx, p, masks, ctx->win_part.as<float2>()));

@@ -132,7 +132,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_
   int* nzflag = last_issued + S;                          // [S]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
-  const int nch = (Lx + 31) / 32;
+  // column split: CTA blockIdx.z sums chunks [cbeg, cbeg + nch) into its own part
+  const int nch_all = (Lx + 31) / 32, cs = blockIdx.z, ncs = gridDim.z;
+  const int cbeg = (int)((long long)nch_all * cs / ncs);
+  const int nch = (int)((long long)nch_all * (cs + 1) / ncs) - cbeg;
 
   if (warp == 0) tmem_alloc(tslot, P::NCOL);
   if (tid == 0) {
@@ -167,9 +170,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_
           break;
         }
         mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
-        tma_load_3d(sA(s), &tmM, &full[s], 32 * c, y0, img);
-        tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
-        tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
+        tma_load_3d(sA(s), &tmM, &full[s], 32 * (cbeg + c), y0, img);
+        tma_load_2d(sBh(s), &tmBh, &full[s], 32 * (cbeg + c), 0);
+        tma_load_2d(sBl(s), &tmBl, &full[s], 32 * (cbeg + c), 0);
         last_issued[s] = c;
       }
     }
@@ -297,8 +300,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_
 
   const int KY = 2 * Ny + 1, NU = Nx + 1;
   const float scale = 1.0f / ((float)Fx * (float)Fy);
-  const int nps = part_stride > 0 ? part_stride : (int)gridDim.x;
-  float2* out = win_part + ((size_t)img * nps + rb) * KY * NU;
+  const int nps = part_stride > 0 ? part_stride : (int)(gridDim.x * gridDim.z);
+  float2* out = win_part + ((size_t)img * nps + rb * ncs + cs) * KY * NU;
   for (int o = tid; o < KY * NU; o += TC_THREADS) {
     const int vi = o / NU, u = o - vi * NU;
     const int v = vi - Ny;
@@ -433,7 +436,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_const
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [2]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int yb = blockIdx.x, img = blockIdx.y, y0 = yb * 128;
-  const int ntile = (Lx + BN - 1) / BN;
+  // X split: CTA blockIdx.z writes tiles [t0, t0 + ntile) of the row band
+  const int ntile_all = (Lx + BN - 1) / BN;
+  const int t0 = (int)((long long)ntile_all * blockIdx.z / gridDim.z);
+  const int ntile = (int)((long long)ntile_all * (blockIdx.z + 1) / gridDim.z) - t0;
 
   if (warp == 0) tmem_alloc(tslot, 2 * BN);
   if (tid == 0) {
@@ -471,8 +477,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_const
         }
         mbar_arrive_expect_tx(&fullB[b], P::B_BYTES);
         for (int kb = 0; kb < KBLK; ++kb) {
-          tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, t * BN, img);
-          tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, t * BN, img);
+          tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, (t0 + t) * BN, img);
+          tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, (t0 + t) * BN, img);
         }
         last_issued[b] = t;
       }
@@ -532,7 +538,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_const
         fence_proxy_async();
         named_bar(1, 128);
         if (tid == 0) {
-          tma_store_3d(&tmOut, st, t * BN + slab * 32, y0, img);
+          tma_store_3d(&tmOut, st, (t0 + t) * BN + slab * 32, y0, img);
           bulk_commit();
         }
       }
@@ -667,7 +673,7 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   const size_t smem = WinTC<NB>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  dim3 grid((g.Ly + 127) / 128, p.batch);
+  dim3 grid((g.Ly + 127) / 128, p.batch, std::max(1, p.colSplits));
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
   win_dft_tc_kernel<NB><<<grid, TC_THREADS, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
                                                                   win_part, p.part_stride, err);
@@ -702,7 +708,11 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   const size_t smem = FiTC<KBLK, BN>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  dim3 grid((g.Ly + 127) / 128, p.batch);
+  // enough CTAs for ~4 waves of one CTA per SM (less tail loss), at least 2 tiles each
+  const int ntile = (g.Lx + BN - 1) / BN, rows = (g.Ly + 127) / 128;
+  int xs = (4 * ctx->sm_count + rows * p.batch - 1) / (rows * p.batch);
+  xs = std::max(1, std::min(xs, ntile / 2));
+  dim3 grid(rows, p.batch, xs);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);
   fi_tc_kernel<KBLK, BN><<<grid, TC_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
