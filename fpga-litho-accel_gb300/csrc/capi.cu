@@ -270,7 +270,7 @@ static int check_geom(litho_ctx* ctx, int Lx, int Ly, int Nx, int Ny, int nk) {
   return LITHO_OK;
 }
 
-static int default_conv_n(int Nx, int Ny) {
+int default_conv_n(int Nx, int Ny) {
   const int n = next_pow2(4 * (Nx > Ny ? Nx : Ny) + 1);
   return n < 32 ? 32 : n;
 }

@@ -873,9 +873,11 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
   const int KY = 2 * g.Ny + 1;
   const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
   if (tc) {
-    // tensor-core window: 32-column chunks, split so ~4 CTAs per SM are available
+    // tensor-core window: 32-column chunks; split the columns only when the row
+    // blocks alone leave SMs idle (each split adds a row-DFT epilogue and a partial)
     const int nch = (g.Lx + 31) / 32;
-    const int cs = (4 * ctx->sm_count + p.rowBlocks * batch - 1) / (p.rowBlocks * batch);
+    const int units = p.rowBlocks * batch;
+    const int cs = units < ctx->sm_count ? (2 * ctx->sm_count + units - 1) / units : 1;
     p.colSplits = std::max(1, std::min(cs, std::min(4, nch / 4)));
   }
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));

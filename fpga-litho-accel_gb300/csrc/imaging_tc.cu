@@ -708,9 +708,10 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   const size_t smem = FiTC<KBLK, BN>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  // enough CTAs for ~4 waves of one CTA per SM (less tail loss), at least 2 tiles each
+  // split the X tiles of a row block only when the row blocks alone leave SMs idle
   const int ntile = (g.Lx + BN - 1) / BN, rows = (g.Ly + 127) / 128;
-  int xs = (4 * ctx->sm_count + rows * p.batch - 1) / (rows * p.batch);
+  const int units = rows * p.batch;
+  int xs = units < ctx->sm_count ? (2 * ctx->sm_count + units - 1) / units : 1;
   xs = std::max(1, std::min(xs, ntile / 2));
   dim3 grid(rows, p.batch, xs);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);

@@ -135,6 +135,9 @@ struct ImgPlan {
 
 ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count);
 
+// SOCS conv grid used by the imaging entry points: pow2 >= 4 max(Nx, Ny) + 1, at least 32.
+int default_conv_n(int Nx, int Ny);
+
 int calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength, float NA,
                   float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision, int mem, int sh_in,
                   int oSgm_in);

@@ -76,8 +76,23 @@ _SIGS = {
     "litho_batch_plan_run": (_i, [_p]),
     "litho_batch_plan_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_destroy": (_i, [_p]),
+    "litho_surrogate_num_params": (C.c_longlong, []),
+    "litho_surrogate_create": (_i, [_p, _i, C.c_ulonglong, C.POINTER(_p)]),
+    "litho_surrogate_destroy": (None, [_p]),
+    "litho_surrogate_get_params": (_i, [_p, _p, C.c_longlong]),
+    "litho_surrogate_set_params": (_i, [_p, _p, C.c_longlong]),
+    "litho_surrogate_forward": (_i, [_p, _p, _i, _p]),
+    "litho_surrogate_loss_grad": (_i, [_p, _p, _p, _i, _p, _p]),
+    "litho_surrogate_train_step": (_i, [_p, _p, _p, _i, _f, _f, _p]),
+    "litho_rect_masks": (_i, [_p, C.c_ulonglong, C.c_longlong, _i, _i, _i, _i, _i, _i, _p]),
+    "litho_surrogate_set_alpha": (_i, [_p, _f]),
+    "litho_surrogate_get_alpha": (_f, [_p]),
+    "litho_surrogate_project": (_i, [_p, _i, _i, _p, _i, _p]),
+    "litho_surrogate_predict": (_i, [_p, _p, _p, _i, _p, _p]),
+    "litho_surrogate_image": (_i, [_p, _p, _p, _i, _f, _p, _p, _p]),
 }
 BATCH_AUTOTUNE = 1
+_CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 BATCH_GRAPH = 2
 
 
@@ -91,7 +106,7 @@ class _DevArray:
     def __init__(self, ptr: int, shape):
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (int(ptr), False),
                                          "version": 3, "strides": None}
-STAGES = ("win_dft", "socs", "fi_prep", "fi_out", "fft_mask", "tcc", "eig", "upload")
+STAGES = ("win_dft", "socs", "fi_prep", "fi_out", "fft_mask", "tcc", "eig", "upload", "surrogate")
 for _name, (_res, _args) in _SIGS.items():
     _fn = getattr(_lib, _name)
     _fn.restype = _res
@@ -255,7 +270,14 @@ class Context:
             raise LithoError(st, msg or _lib.litho_status_string(st).decode())
 
     def set_stream(self, stream_handle: Optional[int]):
-        self._check(_lib.litho_ctx_set_stream(self.h, C.c_void_p(stream_handle) if stream_handle else None))
+        """Queue work on a caller's stream (``torch.cuda.Stream.cuda_stream``); None restores the
+        context's own stream.  Handle 0 (torch's default stream) is the legacy default stream,
+        passed as cudaStreamLegacy since a NULL handle means the context's own stream."""
+        if stream_handle is None:
+            h = None
+        else:
+            h = C.c_void_p(int(stream_handle) if int(stream_handle) != 0 else _CUDA_STREAM_LEGACY)
+        self._check(_lib.litho_ctx_set_stream(self.h, h))
 
     def synchronize(self):
         self._check(_lib.litho_ctx_synchronize(self.h))

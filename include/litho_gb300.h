@@ -74,7 +74,7 @@ typedef struct litho_ctx litho_ctx;
 int litho_ctx_create(int device, litho_ctx** out);
 int litho_ctx_destroy(litho_ctx* ctx);
 /* Use a caller-owned stream (cudaStream_t passed as void*); NULL restores the
- * context's own stream. */
+ * context's own stream (pass cudaStreamLegacy for the legacy default stream). */
 int litho_ctx_set_stream(litho_ctx* ctx, void* stream);
 void* litho_ctx_get_stream(litho_ctx* ctx);
 /* Block until all work queued on the context's stream has finished. */
@@ -98,7 +98,8 @@ int litho_version(void);
 #define LITHO_STAGE_TCC       5  /* pupil build + TCC contraction                */
 #define LITHO_STAGE_EIG       6  /* Hermitian eigensolve                         */
 #define LITHO_STAGE_UPLOAD    7  /* kernel packing and other small helpers       */
-#define LITHO_STAGE_COUNT     8
+#define LITHO_STAGE_SURROGATE 8  /* FNO surrogate forward / backward / update    */
+#define LITHO_STAGE_COUNT     9
 int litho_ctx_enable_timing(litho_ctx* ctx, int enable);
 /* Synchronise the stream; fill ms[LITHO_STAGE_COUNT] (summed device time) and
  * launches[LITHO_STAGE_COUNT] (kernel launches) since the last reset; either
@@ -226,6 +227,65 @@ int litho_batch_plan_destroy(litho_batch_plan* plan);
  * and must be serialised by the caller. */
 int litho_image_noalloc(const float* mask, int Lx, int Ly, const float* krn_r, const float* krn_i,
                         const float* scales, int nk, int Nx, int Ny, float* image, void* stream);
+
+/* ---- learned surrogate (no reference counterpart) -------------------------
+ * FNO-2d (Li et al. 2021) of the SOCS map mask -> aerial image on an L x L
+ * grid: one input channel, LITHO_FNO_WIDTH channels, LITHO_FNO_MODES retained
+ * modes per axis, LITHO_FNO_LAYERS Fourier layers, a width -> HIDDEN -> 1
+ * projection.  FP32 master weights; GEMMs in BF16 on the tensor cores.
+ * Masks, images and targets are DEVICE pointers ([batch][L][L] float32),
+ * launched on the context's stream.  Parameters are one flat float32 vector:
+ *   Pw[32] Pb[32] | W[4][32 o][32 c] | Wb[4][32] |
+ *   R[4][32 ky-slot][16 kx][32 c][32 o][re,im] (ky = j for j < 16, L-32+j else) |
+ *   Q1[128][32] | q1b[128] | Q2[128] | q2b[1]                                    */
+#define LITHO_FNO_WIDTH  32
+#define LITHO_FNO_MODES  16
+#define LITHO_FNO_HIDDEN 128
+#define LITHO_FNO_LAYERS 4
+typedef struct litho_fno litho_fno;
+
+long long litho_surrogate_num_params(void);
+/* L in {64, 128, 256}; parameters initialised from `seed` (Kaiming-uniform
+ * linear layers, spectral weights U[0,1)/width^2). */
+int  litho_surrogate_create(litho_ctx* ctx, int L, unsigned long long seed, litho_fno** out);
+void litho_surrogate_destroy(litho_fno* f);
+int  litho_surrogate_get_params(litho_fno* f, float* host, long long n);
+/* also resets the Adam state */
+int  litho_surrogate_set_params(litho_fno* f, const float* host, long long n);
+int  litho_surrogate_forward(litho_fno* f, const float* masks, int batch, float* images);
+/* loss = mean_b ||F(m_b) - t_b|| / ||t_b|| (host float, optional) and its
+ * gradient (host copy into grad_host[num_params], optional). */
+int  litho_surrogate_loss_grad(litho_fno* f, const float* masks, const float* targets, int batch,
+                               float* loss, float* grad_host);
+/* one Adam step (beta 0.9/0.999, eps 1e-8, L2 weight decay added to the gradient). */
+int  litho_surrogate_train_step(litho_fno* f, const float* masks, const float* targets, int batch,
+                                float lr, float weight_decay, float* loss);
+/* Seeded rectangle masks first .. first+count-1 of the stream `seed`: nrect in
+ * [nmin, nmax] (<= 256) axis-aligned rectangles, sides in [wmin, wmax] (<= L),
+ * value 1 on 0.  SplitMix64 counters, so any sub-range is reproducible. */
+int  litho_rect_masks(litho_ctx* ctx, unsigned long long seed, long long first, int count, int L,
+                      int nmin, int nmax, int wmin, int wmax, float* masks);
+/* Band projection and error estimates.  Every SOCS image of kernels with half
+ * widths (Nx, Ny) is band-limited to |kx| <= 2 Nx, |ky| <= 2 Ny (in 1/L), so
+ * the surrogate's image is replaced by its band part (in place; the L2 error
+ * can only shrink).  litho_surrogate_project writes est[b] = alpha * ||removed
+ * part|| / ||band part||.  litho_surrogate_predict runs the network, the
+ * projection and the estimator: the image's coefficients at the lowest
+ * frequencies q in {-1,0,1}^2 are computed exactly from the mask's window
+ * spectrum and the kernels, I(q) = 1/L^2 sum_k s_k sum_f B_k(f+q) conj(B_k(f)),
+ * B_k = krn_k * DFT(mask), and est[b] = alpha * ||I_net(q) - I(q)|| / ||image||
+ * (Parseval-weighted).  Arrays are DEVICE pointers; 2 Nx, 2 Ny <= 15, nk <= 64. */
+int   litho_surrogate_set_alpha(litho_fno* f, float alpha);
+float litho_surrogate_get_alpha(const litho_fno* f);
+int   litho_surrogate_project(litho_fno* f, int Nx, int Ny, float* images, int batch, float* est);
+int   litho_surrogate_predict(litho_fno* f, const litho_kernel_set* ks, const float* masks, int batch,
+                              float* images, float* est);
+/* Surrogate imaging with fallback: litho_surrogate_predict, then masks whose
+ * estimate is above `threshold` (or NaN) are imaged by the plain FP32 SOCS
+ * path with the kernel set instead.  est_host[batch] and used_socs[batch]
+ * (host, optional) report the estimate and the choice. */
+int   litho_surrogate_image(litho_fno* f, const litho_kernel_set* ks, const float* masks, int batch,
+                            float threshold, float* images, float* est_host, int* used_socs);
 
 /* ---- TCC (litho.cpp:428-516 calcTCC) --------------------------------------
  * src: srcSize x srcSize normalised source (host or device per mem).
