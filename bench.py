@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--cpu-budget-s", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])
+    p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--surrogate-epochs", type=int, default=10)
     return p.parse_args()
 
 
@@ -206,6 +208,68 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def surrogate_leg(ctx, epochs):
+    """The FNO surrogate on its own workload: 256x256 seeded rectangle masks, the
+    quasar-source optics above (Nx=2), K=24.  A short training schedule (4096 GPU-SOCS
+    pairs) by the library's kernels, calibration of the error estimate on 256 masks,
+    512 held-out masks imaged with SOCS fallback and judged by SOCS, and throughput of
+    plain SOCS, the network path and the surrogate-with-fallback path on the same 256
+    masks (CUDA events)."""
+    import numpy as np
+    import torch
+    from litho_gb300 import surrogate as S
+    ctx.set_stream(None)
+    ks, info = S.c5_kernel_set(ctx)
+    L = S.C5["L"]
+    thr = 1e-2
+    tm, ti = S.make_pairs(ctx, ks, seed=11, first=0, count=4096, L=L)
+    cm, ci = S.make_pairs(ctx, ks, seed=12, first=0, count=256, L=L)
+    em, ei = S.make_pairs(ctx, ks, seed=13, first=0, count=512, L=L)
+    model = S.Surrogate(ctx, L=L, seed=5)
+    t0 = time.perf_counter()
+    S.train(model, tm, ti, epochs=epochs, batch=32, lr=1e-3, decay_every=max(1, epochs // 3))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    img, est = model.predict(ks, cm)
+    alpha = float(np.quantile(S.rel_l2_per_image(img, ci).cpu().numpy() / est.cpu().numpy(), 0.99))
+    model.set_alpha(alpha)
+    out, est, used = model.image(ks, em, thr)
+    err = S.rel_l2_per_image(out, ei).cpu().numpy()
+    net, _ = model.predict(ks, em)
+    nerr = S.rel_l2_per_image(net, ei).cpu().numpy()
+
+    def ms(fn, reps):
+        st = torch.cuda.current_stream()
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(reps):
+            fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    mb = em[:256].contiguous()
+    buf = torch.empty_like(mb)
+    with S.torch_stream(ctx):
+        t_socs = ms(lambda: ctx.image_batch(ks, mb, buf), 20)
+    t_net = ms(lambda: model.predict(ks, mb, buf), 10)
+    t_sur = ms(lambda: model.image(ks, mb, thr, buf), 10)
+    model.close()
+    ks.close()
+    served = ~used
+    return {"images_per_s": 256 / t_sur * 1e3, "network_images_per_s": 256 / t_net * 1e3,
+            "plain_socs_same_config_images_per_s": 256 / t_socs * 1e3, "vs_plain_same_config": t_socs / t_sur,
+            "config": {"L": L, "K": info["nk"], "Nx": info["Nx"], "masks": "seeded rectangles 8-32 of 8-64 px",
+                       "train_pairs": 4096, "epochs": epochs, "train_s": t_train, "threshold": thr,
+                       "alpha": alpha, "held_out": 512, "batch_timed": 256},
+            "served_fraction": float(served.mean()),
+            "network_rel_l2_median": float(np.median(nerr)), "network_rel_l2_max": float(nerr.max()),
+            "returned_rel_l2_max": float(err.max()),
+            "served_rel_l2_max": float(err[served].max()) if served.any() else None}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -352,6 +416,8 @@ def main():
                                           "FT_r2c_padded + calcSOCS (128^2 conv grid, embed 94) + FI in FP64, "
                                           "scipy.fft on all host cores"}
         line["rel_l2_vs_fp64"] = err
+    if rank == 0 and not args.no_surrogate:
+        line["forms"]["surrogate"] = surrogate_leg(ctx, args.surrogate_epochs)
     if rank == 0:
         print(json.dumps(line), flush=True)
     for k in ks.values():

@@ -709,6 +709,7 @@ __global__ void __launch_bounds__(1024) loss_kernel(int L, int B, const float* _
 //                      gvpw_l = g_z W_l (bf16)
 // ---------------------------------------------------------------------------
 enum { HEAD_PROJ = 0, HEAD_SPEC = 1, HEAD_LIFT = 2 };
+constexpr int NRED = 2 * H + 2 * C + 1;  // per-warp slots of the vector gradient partials
 
 struct RowBwd {
   int L, rows, layer;
@@ -748,7 +749,7 @@ struct BwdSmem {
     sT = sTT = 0;
     if (head != HEAD_PROJ) { sT = o; o += up16((size_t)L * SP * 2); }
     if (head != HEAD_LIFT) { sTT = o; o += up16(J * LP * 2); }
-    sRed = o; o += up16((2 * H + 2 * C + 1) * sizeof(float));
+    sRed = o; o += up16((size_t)(THREADS / 32) * NRED * sizeof(float));
     total = o;
   }
 };
@@ -795,7 +796,7 @@ __global__ void __launch_bounds__(THREADS, 1) row_bwd_kernel(const RowBwd a) {
       sQ1[h * SP + c] = v;
       sQ1T[c * HP + h] = v;
     }
-  for (int i = tid; i < 2 * H + 2 * C + 1; i += THREADS) sRed[i] = 0.f;
+  for (int i = tid; i < (THREADS / 32) * NRED; i += THREADS) sRed[i] = 0.f;
   float pw[2][4], pb[2][4];
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks) {
@@ -1043,13 +1044,15 @@ __global__ void __launch_bounds__(THREADS, 1) row_bwd_kernel(const RowBwd a) {
 
   // ---- per-CTA partials ----
   float* gp = a.gpart + (size_t)blockIdx.x * Dn::N;
-  // vector partials: reduce over g (lanes xor 4, 8, 16), then over warps in shared memory
+  // vector partials: reduce over g (lanes xor 4, 8, 16), then over warps in a fixed
+  // order (per-warp slots), so that the gradient is bitwise reproducible
   auto red_g = [&](float v) {
     v += __shfl_xor_sync(0xffffffffu, v, 4);
     v += __shfl_xor_sync(0xffffffffu, v, 8);
     v += __shfl_xor_sync(0xffffffffu, v, 16);
     return v;
   };
+  float* myRed = sRed + warp * NRED;
   __syncthreads();
 #pragma unroll
   for (int n = 0; n < 4; ++n)
@@ -1058,8 +1061,8 @@ __global__ void __launch_bounds__(THREADS, 1) row_bwd_kernel(const RowBwd a) {
       const float s0 = red_g(vb[n][e]);
       const float s1 = red_g(vw[n][e]);
       if (g == 0) {
-        atomicAdd(&sRed[8 * n + 2 * t + e], s0);
-        atomicAdd(&sRed[C + 8 * n + 2 * t + e], s1);
+        myRed[8 * n + 2 * t + e] = s0;
+        myRed[C + 8 * n + 2 * t + e] = s1;
       }
     }
   if (HEAD == HEAD_PROJ) {
@@ -1070,13 +1073,19 @@ __global__ void __launch_bounds__(THREADS, 1) row_bwd_kernel(const RowBwd a) {
         const float s0 = red_g(dq1b[nh][e]);
         const float s1 = red_g(dq2[nh][e]);
         if (g == 0) {
-          atomicAdd(&sRed[2 * C + 8 * nh + 2 * t + e], s0);
-          atomicAdd(&sRed[2 * C + H + 8 * nh + 2 * t + e], s1);
+          myRed[2 * C + 8 * nh + 2 * t + e] = s0;
+          myRed[2 * C + H + 8 * nh + 2 * t + e] = s1;
         }
       }
     float s = dq2b;
     for (int k = 16; k > 0; k >>= 1) s += __shfl_xor_sync(0xffffffffu, s, k);
-    if (lane == 0) atomicAdd(&sRed[2 * C + 2 * H], s);
+    if (lane == 0) myRed[2 * C + 2 * H] = s;
+  }
+  __syncthreads();
+  for (int i = tid; i < NRED; i += THREADS) {
+    float s = 0.f;
+    for (int w = 0; w < THREADS / 32; ++w) s += sRed[w * NRED + i];
+    sRed[i] = s;  // slot 0 of warp 0 is read only by this thread
   }
   __syncthreads();
   if (HEAD == HEAD_LIFT) {

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -171,6 +172,7 @@ class KernelSet:
         ctx._check(_lib.litho_kernel_set_create(ctx.h, _ptr(kr), _ptr(ki), _ptr(s), self.nk, self.Nx, self.Ny,
                                                 MEM_HOST, C.byref(h)))
         self.h = h
+        ctx._adopt(self)
 
     def close(self):
         if self.h:
@@ -204,6 +206,7 @@ class BatchPlan:
         ctx._check(_lib.litho_batch_plan_create(ctx.h, C.cast(hs, C.c_void_p), C.cast(ps, C.c_void_p), len(sets),
                                                 C.cast(arr, C.c_void_p), len(items), precision, flags, C.byref(h)))
         self.h = h
+        ctx._adopt(self)
 
     def mask(self, i: int):
         import torch
@@ -246,9 +249,21 @@ class Context:
             raise LithoError(st, f"litho_ctx_create(device={device}) failed")
         self.h = h
         self.device = device
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, obj):
+        """Objects made on this context (kernel sets, batch plans, surrogates) are closed with it."""
+        self._children.add(obj)
 
     def close(self):
         if self.h:
+            kids = list(self._children)
+            for k in kids:  # plans and surrogates before the kernel sets they may use
+                if not isinstance(k, KernelSet):
+                    k.close()
+            for k in kids:
+                if isinstance(k, KernelSet):
+                    k.close()
             _lib.litho_ctx_destroy(self.h)
             self.h = None
 

@@ -59,6 +59,7 @@ class Surrogate:
         ctx._check(_lib.litho_surrogate_create(ctx.h, int(L), int(seed), C.byref(h)))
         self.ctx, self.h, self.L = ctx, h, L
         self.n = num_params()
+        ctx._adopt(self)
 
     def close(self):
         if self.h:

@@ -193,3 +193,19 @@ def test_lowq_estimate_matches_numpy(ctx):
         print("est", est[b], "numpy", ref)
         assert abs(est[b] - ref) <= 1e-3 * ref
     model.close()
+
+
+def test_training_is_reproducible(ctx):
+    """Fixed-order reductions: two identical training runs give identical weights."""
+    import torch
+    from litho_gb300 import surrogate as S
+    L, N = 64, 32
+    masks = S.rect_masks(ctx, 8, 0, N, L, wmin=4, wmax=16)
+    tgt = torch.tensor(_targets(masks.cpu().numpy()), device=masks.device)
+    ps = []
+    for _ in range(2):
+        model = S.Surrogate(ctx, L=L, seed=6)
+        S.train(model, masks, tgt, epochs=3, batch=8, lr=1e-3)
+        ps.append(model.params())
+        model.close()
+    assert np.array_equal(ps[0], ps[1])
