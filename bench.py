@@ -40,6 +40,9 @@ sys.path.insert(0, os.path.join(ROOT, "fpga-litho-accel_gb300"))
 
 METRIC = "aerial images/s at 1024^2 K=24: mixed/batched/surrogate vs plain GPU at stated rel-L2"
 L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
+# DRAM bytes (read + write) per mask of the dominant kernel, from an ncu capture of one
+# win_dft_tc launch on 48 masks of this workload (the traffic scales with the masks).
+TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.772288e6 + 3.230464e6) / 48}
 WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
             "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
 
@@ -55,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])
     p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="warm-up + timed steps of both forms only (no clock sampling, e2e, CPU or surrogate legs)")
     p.add_argument("--surrogate-epochs", type=int, default=10)
     return p.parse_args()
 
@@ -301,10 +306,12 @@ def main():
     def step(form):
         ctx.image_batch(ks[form], masks, images[form], precision=prec[form])
 
-    def timed(form, steps):
-        """K steps bracketed by barrier + synchronize, CUDA events on the library's stream."""
+    def timed(form, steps, stages):
+        """K steps bracketed by barrier + synchronize, CUDA events on the library's stream.
+        stages=True also brackets every kernel launch with CUDA events (per-kernel durations);
+        the returned counts are launches either way."""
         ctx.stage_times(reset=True)
-        ctx.enable_timing(True)
+        ctx.enable_timing(stages)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -326,6 +333,13 @@ def main():
         for _ in range(max(args.warmup, 3)):
             step(form)
     torch.cuda.synchronize()
+    if args.profile:  # the launch sequence an ncu capture needs, nothing else
+        for form in ("plain", "mixed"):
+            for _ in range(args.steps):
+                step(form)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": True, "batch": B, "steps": args.steps}), flush=True)
+        return
     # clocks are sampled from here through both timed regions and the e2e region;
     # a short untimed pre-roll keeps the GPU under load until the sampler is live
     clocks = Clocks(local)
@@ -336,11 +350,15 @@ def main():
             step(head)
         torch.cuda.synchronize()
     other = "plain" if head == "mixed" else "mixed"
-    ms_o, st_o = timed(other, args.steps)
-    ms, st = timed(head, args.steps)
+    ms_o, _ = timed(other, args.steps, False)
+    ms, st_v = timed(head, args.steps, False)
     value = ws * B * args.steps / (ms / 1e3)
     value_o = ws * B * args.steps / (ms_o / 1e3)
-    launches = sum(n for _, n in st.values())
+    launches = sum(n for _, n in st_v.values())
+    # per-kernel durations: a shorter pass with every launch bracketed by CUDA events
+    ksteps = max(10, args.steps // 5)
+    _, st_o = timed(other, ksteps, True)
+    _, st = timed(head, ksteps, True)
 
     # roofline of the dominant kernel (algorithmic bytes per launch)
     img_bytes = 4 * L_SIZE * L_SIZE
@@ -383,9 +401,9 @@ def main():
     clk = clocks.stop()
 
     forms = {head: {"images_per_s": value, "ms_per_step": ms / args.steps,
-                    "stage_ms_per_step": {s: st[s][0] / args.steps for s in names}},
+                    "stage_ms_per_step_serial": {s: st[s][0] / ksteps for s in names}},
              other: {"images_per_s": value_o, "ms_per_step": ms_o / args.steps,
-                     "stage_ms_per_step": {s: st_o[s][0] / args.steps for s in names}}}
+                     "stage_ms_per_step_serial": {s: st_o[s][0] / ksteps for s in names}}}
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "tf32x3/f32" if head == "mixed" else "f32", "data": "synthetic",
@@ -398,7 +416,10 @@ def main():
             "forms": forms,
             "mixed_over_plain": forms["mixed"]["images_per_s"] / forms["plain"]["images_per_s"],
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm,
+                         "traffic": (B * TRAFFIC_PER_IMAGE[(head, dom)]) if (head, dom) in TRAFFIC_PER_IMAGE else None,
+                         "traffic_source": "ncu dram__bytes_read+write of one win_dft_tc launch at 1024^2, K=24, "
+                                           "48 masks, scaled per mask to the batch",
                          "peak_source": "measured (MEASURED_PEAKS.json)" if peaks else "fallback",
                          "shares": shares, "kernel_gbs": kern_gbs,
                          "bytes_per_image": 2 * img_bytes + kb,

@@ -288,13 +288,8 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
       const bool neg = u < 0;
       const int vv = neg ? -v : v, uu = neg ? -u : u;
       const float2* P = win_part + (size_t)img * nparts * KY * (Nx + 1) + (size_t)(vv + Ny) * (Nx + 1) + uu;
-      float re = 0.f, im = 0.f;
-      for (int p = 0; p < nparts; ++p) {
-        const float2 t = P[(size_t)p * KY * (Nx + 1)];
-        re += t.x;
-        im += t.y;
-      }
-      w = make_float2(re, neg ? -im : im);
+      const float2 t = sum_strided(P, (size_t)KY * (Nx + 1), nparts);
+      w = make_float2(t.x, neg ? -t.y : t.y);
     }
     win[idx] = w;
   }
@@ -401,15 +396,7 @@ __global__ void __launch_bounds__(FIP_THREADS) fi_prep_kernel(const float2* __re
   float2* sT = fs + BH * BW;       // [ND][FIP_THREADS]
   const int tid = threadIdx.x, img = blockIdx.y;
   const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-  for (int idx = tid; idx < BH * BW; idx += FIP_THREADS) {
-    float re = 0.f, im = 0.f;
-    for (int gi = 0; gi < ngroups; ++gi) {
-      const float2 t = B[(size_t)gi * BH * BW + idx];
-      re += t.x;
-      im += t.y;
-    }
-    sS[idx] = make_float2(re, im);
-  }
+  for (int idx = tid; idx < BH * BW; idx += FIP_THREADS) sS[idx] = sum_strided(B + idx, (size_t)BH * BW, ngroups);
   const int X = blockIdx.x * FIP_THREADS + tid;
   const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
   for (int d = 0; d < ND; ++d) sT[d * FIP_THREADS + tid] = cis_exact((long long)d * xp, Fx, 1.f);
@@ -882,10 +869,10 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
   }
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));
-  LITHO_RET(ctx->tm.ensure(ctx, (size_t)batch * (4 * g.Ny + 1) * g.Lx * sizeof(float)));
   if (tc) {
     LITHO_RET(run_win_dft_tc(ctx, p, masks, ctx->win_part.as<float2>()));
   } else {
+    LITHO_RET(ctx->tm.ensure(ctx, (size_t)batch * (4 * g.Ny + 1) * g.Lx * sizeof(float)));
     LITHO_RET(run_win_dft(ctx, p, masks, ctx->win_part.as<float2>()));
   }
   WindowSrc w;

@@ -345,15 +345,7 @@ __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* _
   const int tid = threadIdx.x, img = blockIdx.y;
   const int X0 = blockIdx.x * FPT_THREADS, X = X0 + tid;
   const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) {
-    float re = 0.f, im = 0.f;
-    for (int gi = 0; gi < ngroups; ++gi) {
-      const float2 t = B[(size_t)gi * BH * BW + idx];
-      re += t.x;
-      im += t.y;
-    }
-    sS[idx] = make_float2(re, im);
-  }
+  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) sS[idx] = sum_strided(B + idx, (size_t)BH * BW, ngroups);
   const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
   float2 tw[MAXD];
 #pragma unroll

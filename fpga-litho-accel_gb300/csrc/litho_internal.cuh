@@ -60,6 +60,32 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Sum of n float2 values p[0], p[stride], ... (partials written by an earlier
+// kernel): eight independent loads in flight and a fixed summation order.
+__device__ __forceinline__ float2 sum_strided(const float2* __restrict__ p, size_t stride, int n) {
+  float2 a[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) a[u] = make_float2(0.f, 0.f);
+  int i = 0;
+  for (; i + 8 <= n; i += 8) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const float2 t = __ldg(p + (size_t)(i + u) * stride);
+      a[u].x += t.x;
+      a[u].y += t.y;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 7; ++u)
+    if (i + u < n) {
+      const float2 t = __ldg(p + (size_t)(i + u) * stride);
+      a[u].x += t.x;
+      a[u].y += t.y;
+    }
+  return make_float2(((a[0].x + a[1].x) + (a[2].x + a[3].x)) + ((a[4].x + a[5].x) + (a[6].x + a[7].x)),
+                     ((a[0].y + a[1].y) + (a[2].y + a[3].y)) + ((a[4].y + a[5].y) + (a[6].y + a[7].y)));
+}
+
 inline int next_pow2(int x) {
   int p = 1;
   while (p < x) p <<= 1;

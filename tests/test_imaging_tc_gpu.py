@@ -102,3 +102,4 @@ def test_mixed_unsupported_geometry(ctx, L):
     with pytest.raises(L.LithoError) as e:
         _mixed(ctx, L, m[None], krns, scales, nx)
     assert e.value.status == L.LITHO_ERR_UNSUPPORTED
+
