@@ -9,18 +9,17 @@
 // dropped Al*Bl term and the TF32 rounding of Xl leave a relative error of about
 // 2^-22 per product.
 //
-// Both kernels are warp-specialised (192 threads) and synchronised only by
-// mbarriers, so TMA traffic, tensor-core work and CUDA-core work overlap:
-//   warp 4  TMA producer (one lane)
-//   warp 5  MMA issuer   (one lane)
-//   warps 0-3  compute / epilogue (they own TMEM lanes 0-127)
+// Both kernels are warp-specialised and synchronised only by mbarriers, so TMA
+// traffic, tensor-core work and CUDA-core work overlap (warp 4: TMA producer,
+// warp 5: MMA issuer, warps 0-3: compute; they own TMEM lanes 0-127).
 //
 // win_dft_tc_kernel   D[y][j] = sum_x mask[y][x] * T[x][j]  (M = 128 mask rows
-//                     per CTA, N = 2Nx+1 column twiddles padded to NB, K = Lx).
+//                     per tile, N = 2Nx+1 column twiddles padded to NB, K = the
+//                     tile's columns).  Persistent (one CTA per SM, 320 threads):
 //                     TMA streams 128 x 32 mask tiles (SWIZZLE_128B) through a
-//                     5-stage ring; warps 0-3 split each landed tile into Ah (in
-//                     place) and Al; the MMA lane issues 12 MMAs per tile.  The
-//                     row-DFT epilogue is the FP32 kernel's.
+//                     6-8 stage ring; warps 0-3 split each landed tile in place;
+//                     the accumulator is double-buffered in TMEM and warps 6-9
+//                     run each tile's row-DFT epilogue while the next tile streams.
 // fi_tc_kernel        image[Y][X] = sum_r Cy[Y][r] * Tm[r][X]  (M = 128 image
 //                     rows, N = BN columns per tile, K = 4Ny+1 padded to 32*KBLK).
 //                     Persistent over the X tiles of one row band: A (the Cy
@@ -62,6 +61,20 @@ __global__ void twT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
   lo[(size_t)j * Lx + x] = (float)(v - (double)h);
 }
 
+// ytab[v][y] = e^{-2 pi i v y'/Fy} (v = 0..Ny), y' = y + (Fy - Ly)/2 - Fy/2: the row
+// twiddles of the window DFT's epilogue
+__global__ void ytab_init_kernel(float2* __restrict__ yt, int Ly, int Fy) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = blockIdx.y;
+  if (y >= Ly) return;
+  const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
+  long long m = ((long long)v * (y + oyc)) % Fy;
+  if (m < 0) m += Fy;
+  float sn, cs;
+  sincospif(2.0f * (float)m / (float)Fy, &sn, &cs);
+  yt[(size_t)v * Ly + y] = make_float2(cs, -sn);
+}
+
 // CyT[Y][r] (KP columns): r = 0 -> 1; 1..2Ny -> 2cos(2 pi r y'/Fy); 2Ny+1..4Ny -> -2sin; else 0
 __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, int Ly, int Fy, int Ny, int KP) {
   const int Y = blockIdx.x * blockDim.x + threadIdx.x;
@@ -89,64 +102,86 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // ---------------------------------------------------------------------------
 constexpr int TC_THREADS = 192;
 
+// Persistent window DFT: one CTA per SM streams its tiles (image, 128-row block,
+// column range) through one TMA ring; the TMEM accumulator is double-buffered so
+// a tile's row-DFT epilogue (its own four warps) overlaps the next tile's loads
+// and MMAs.  Roles (448 threads):
+//   warps 0-7   check each landed mask tile for TF32-exactness (warp vote); only
+//               a tile with a residual is split in place (hi, then lo)
+//   warp 8      TMA producer (one lane), warp 9 MMA issuer (one lane)
+//   warps 10-13 epilogue: TMEM -> registers -> shared -> row DFT -> partials
+// Per stage s and running chunk q (parity (q / S) & 1):
+//   producer  : [wait empty[s]] -> TMA mask tile + twiddle hi/lo tiles -> full[s]
+//   consumers : wait full[s]; vote residual (nzflag); if any: Ah = round_tf32(A) in
+//               place; arrive ready[s]; if residual: wait hidone[s], write Al,
+//               arrive ready2[s]
+//   MMA lane  : [tile start: wait accempty[buf]]; wait ready[s]; Ah*Bh + Ah*Bl;
+//               if residual: commit hidone[s], wait ready2[s], Al*Bh; commit empty[s];
+//               [tile end: commit accfull[buf]]
+//   epilogue  : wait accfull[buf]; TMEM -> sR; arrive accempty[buf]; row DFT with
+//               one warp per output (lanes over rows, shuffle reduction)
+// hidone/ready2 complete only on chunks with a residual, so their parities are
+// tracked per stage in bit masks that both sides flip identically.
 template <int NB>
 struct WinTC {
-  static constexpr int STAGES = NB <= 32 ? 4 : 3;  // two CTAs per SM fit in shared memory
   static constexpr uint32_t A_B = 128 * 128;       // 128 rows x 32 fp32 (split in place: hi, then lo)
   static constexpr uint32_t B_B = NB * 128;        // NB rows x 32 fp32
   static constexpr uint32_t STAGE_B = A_B + 2 * B_B;
-  static constexpr uint32_t NCOL = NB <= 32 ? 32 : 64;
-  static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_B + 512;
+  static constexpr uint32_t NCOL = NB <= 32 ? 32 : 64;  // columns of one accumulator
+  static constexpr uint32_t EPI_B = NB * 129 * 4 + 17 * 129 * 8;  // sR [NB][129] + sRT [Ny+1 <= 17][129]
+  static constexpr int FIT = (int)((220u * 1024u - EPI_B - 2048u) / STAGE_B);
+  static constexpr int STAGES = FIT > 8 ? 8 : FIT;
+  static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_B + EPI_B + 1024;
 };
+constexpr int WP_THREADS = 448;  // warps 0-7 split, 8 TMA, 9 MMA, 10-13 epilogue
+constexpr int WP_CONS = 256;     // consumer threads
 
-// Per stage s and chunk c (parity ph = (c / STAGES) & 1):
-//   producer  : [wait empty[s]] -> TMA mask tile + twiddle hi/lo tiles -> full[s]
-//   consumers : wait full[s]; keep the tile in registers; write Ah = round_tf32(A)
-//               in place; vote whether the residual A - Ah is non-zero (nzflag);
-//               arrive ready[s]; if it is: wait hidone[s], overwrite the tile with
-//               the residual Al, arrive ready2[s]
-//   MMA lane  : wait ready[s]; Ah*Bh + Ah*Bl; if residual: commit hidone[s], wait
-//               ready2[s], Al*Bh; commit empty[s]
-// hidone/ready2 only complete on chunks with a residual, so their parities are
-// tracked per stage in a bit mask that both sides flip identically.
 template <int NB>
-__global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
+__global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
                                                                    const __grid_constant__ CUtensorMap tmBh,
                                                                    const __grid_constant__ CUtensorMap tmBl,
                                                                    int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
+                                                                   int rows, int batch, int ncs,
+                                                                   const float2* __restrict__ ytab,
                                                                    float2* __restrict__ win_part, int part_stride,
                                                                    int* __restrict__ err) {
   using P = WinTC<NB>;
   constexpr int S = P::STAGES;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + S * P::STAGE_B);
+  constexpr int RS = 129;  // padded row stride: per-thread row walks hit distinct banks
+  float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [NB][RS]
+  float2* sRT = reinterpret_cast<float2*>(sR + NB * RS);              // [Ny+1][RS]
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)S * P::STAGE_B + P::EPI_B);
   uint64_t* ready = full + S;
   uint64_t* hidone = ready + S;
   uint64_t* ready2 = hidone + S;
   uint64_t* empty = ready2 + S;
-  uint64_t* done = empty + S;
+  uint64_t* accfull = empty + S;
+  uint64_t* accempty = accfull + 2;
+  uint64_t* done = accempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [S]
   int* nzflag = last_issued + S;                          // [S]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int rb = blockIdx.x, img = blockIdx.y, y0 = rb * 128;
-  // column split: CTA blockIdx.z sums chunks [cbeg, cbeg + nch) into its own part
-  const int nch_all = (Lx + 31) / 32, cs = blockIdx.z, ncs = gridDim.z;
-  const int cbeg = (int)((long long)nch_all * cs / ncs);
-  const int nch = (int)((long long)nch_all * (cs + 1) / ncs) - cbeg;
+  const int nch = (Lx + 31) / 32;
+  const int T = rows * batch * ncs;
 
-  if (warp == 0) tmem_alloc(tslot, P::NCOL);
+  if (warp == 0) tmem_alloc(tslot, 2 * P::NCOL);
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&ready[s], 128);
+      mbar_init(&ready[s], WP_CONS);
       mbar_init(&hidone[s], 1);
-      mbar_init(&ready2[s], 128);
+      mbar_init(&ready2[s], WP_CONS);
       mbar_init(&empty[s], 1);
       last_issued[s] = -1;
       nzflag[s] = 0;
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], 128);
     }
     mbar_init(done, 1);
     *abort = 0;
@@ -160,173 +195,227 @@ __global__ void __launch_bounds__(TC_THREADS, 2) win_dft_tc_kernel(const __grid_
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
   auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
   auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B + P::B_B; };
+  // tile t -> (image, row block, column split) and its chunk range
+  auto decode = [&](int t, int& img, int& rb, int& cs, int& c0, int& c1) {
+    img = t / (rows * ncs);
+    const int r = t - img * rows * ncs;
+    rb = r / ncs;
+    cs = r - rb * ncs;
+    c0 = (int)((long long)nch * cs / ncs);
+    c1 = (int)((long long)nch * (cs + 1) / ncs);
+  };
 
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {  // TMA producer
-      for (int c = 0; c < nch; ++c) {
-        const int s = c % S;
-        if (c >= S && !mbar_wait_ab(&empty[s], (uint32_t)((c - S) / S) & 1u, abort)) {
-          *abort = 1;
-          break;
+      int q = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+        int img, rb, cs, c0, c1;
+        decode(t, img, rb, cs, c0, c1);
+        for (int c = c0; c < c1; ++c, ++q) {
+          const int s = q % S;
+          if (q >= S && !mbar_wait_ab(&empty[s], (uint32_t)((q - S) / S) & 1u, abort)) {
+            *abort = 1;
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
+          tma_load_3d(sA(s), &tmM, &full[s], 32 * c, 128 * rb, img);
+          tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
+          tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
+          last_issued[s] = q;
         }
-        mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
-        tma_load_3d(sA(s), &tmM, &full[s], 32 * (cbeg + c), y0, img);
-        tma_load_2d(sBh(s), &tmBh, &full[s], 32 * (cbeg + c), 0);
-        tma_load_2d(sBl(s), &tmBl, &full[s], 32 * (cbeg + c), 0);
-        last_issued[s] = c;
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     if (lane == 0) {  // MMA issuer
       constexpr uint32_t IDESC = idesc_tf32(128, NB);
       uint32_t ph2 = 0;  // per-stage parity of hidone / ready2
-      for (int c = 0; c < nch; ++c) {
-        const int s = c % S;
-        if (!mbar_wait_ab(&ready[s], (uint32_t)(c / S) & 1u, abort)) {
+      int q = 0, tl = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < T && ok; t += gridDim.x, ++tl) {
+        int img, rb, cs, c0, c1;
+        decode(t, img, rb, cs, c0, c1);
+        const int buf = tl & 1;
+        if (tl >= 2 && !mbar_wait_ab(&accempty[buf], (uint32_t)((tl - 2) >> 1) & 1u, abort)) {
           *abort = 1;
           break;
         }
         tc_fence_after();
-        const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
-        nzflag[s] = 0;  // every consumer read it before arriving on ready[s]
-        const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint32_t off = kk * 32;
-          mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
-          mma_tf32(tmem, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
-        }
-        if (two) {
-          mma_commit(&hidone[s]);
-          if (!mbar_wait_ab(&ready2[s], (ph2 >> s) & 1u, abort)) {
+        const uint32_t acc = tmem + (uint32_t)buf * P::NCOL;
+        for (int c = c0; c < c1; ++c, ++q) {
+          const int s = q % S;
+          if (!mbar_wait_ab(&ready[s], (uint32_t)(q / S) & 1u, abort)) {
             *abort = 1;
+            ok = false;
             break;
           }
-          ph2 ^= 1u << s;
           tc_fence_after();
+          const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
+          nzflag[s] = 0;  // every consumer read it before arriving on ready[s]
+          const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint32_t off = kk * 32;
-            mma_tf32(tmem, desc_add(da, off), desc_add(dbh, off), IDESC, 1u);
+            mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC, (c != c0 || kk != 0) ? 1u : 0u);
+            mma_tf32(acc, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
           }
+          if (two) {
+            mma_commit(&hidone[s]);
+            if (!mbar_wait_ab(&ready2[s], (ph2 >> s) & 1u, abort)) {
+              *abort = 1;
+              ok = false;
+              break;
+            }
+            ph2 ^= 1u << s;
+            tc_fence_after();
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t off = kk * 32;
+              mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC, 1u);
+            }
+          }
+          mma_commit(&empty[s]);
         }
-        mma_commit(&empty[s]);
+        if (ok) mma_commit(&accfull[buf]);  // arrives when this tile's MMAs have completed
       }
       mma_commit(done);  // arrives once everything issued above has completed
     }
-  } else {  // warps 0-3: split the landed tile in place
+  } else if (warp < 8) {  // warps 0-7: check / split the landed tiles in place
     uint32_t ph2 = 0;
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % S;
-      if (!mbar_wait_ab(&full[s], (uint32_t)(c / S) & 1u, abort)) {
+    int q = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+      int img, rb, cs, c0, c1;
+      decode(t, img, rb, cs, c0, c1);
+      for (int c = c0; c < c1; ++c, ++q) {
+        const int s = q % S;
+        if (!mbar_wait_ab(&full[s], (uint32_t)(q / S) & 1u, abort)) {
+          *abort = 1;
+          ok = false;
+          break;
+        }
+        float4* a = reinterpret_cast<float4*>(sA(s));
+        float4 v[4];
+        bool nz = false;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          v[i] = a[tid + WP_CONS * i];
+          nz |= (v[i].x != tf32_round(v[i].x)) | (v[i].y != tf32_round(v[i].y)) | (v[i].z != tf32_round(v[i].z)) |
+                (v[i].w != tf32_round(v[i].w));
+        }
+        if (__any_sync(0xffffffffu, nz) && lane == 0) atomicOr(&nzflag[s], 1);
+        named_bar(1, WP_CONS);
+        const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
+        if (two) {  // write Ah = round_tf32(A) in place; exact tiles are used as landed
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            a[tid + WP_CONS * i] =
+                make_float4(tf32_round(v[i].x), tf32_round(v[i].y), tf32_round(v[i].z), tf32_round(v[i].w));
+          fence_proxy_async();
+        }
+        mbar_arrive(&ready[s]);  // release: Ah visible to the MMA lane
+        if (two) {
+          if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) {
+            *abort = 1;
+            ok = false;
+            break;
+          }
+          ph2 ^= 1u << s;
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            a[tid + WP_CONS * i] = make_float4(v[i].x - tf32_round(v[i].x), v[i].y - tf32_round(v[i].y),
+                                               v[i].z - tf32_round(v[i].z), v[i].w - tf32_round(v[i].w));
+          fence_proxy_async();
+          mbar_arrive(&ready2[s]);
+        }
+      }
+    }
+  } else {  // warps 10-13: epilogue
+    const int etid = tid - 320, quarter = warp & 3;
+    const int row = 32 * quarter + lane;
+    const int KY = 2 * Ny + 1, NU = Nx + 1;
+    const float inv_ff = 1.0f / ((float)Fx * (float)Fy);
+    int tl = 0;
+    for (int t = blockIdx.x; t < T; t += gridDim.x, ++tl) {
+      int img, rb, cs, c0, c1;
+      decode(t, img, rb, cs, c0, c1);
+      const int buf = tl & 1;
+      if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) {
         *abort = 1;
         break;
       }
-      float4* a = reinterpret_cast<float4*>(sA(s));
-      float4 v[8];
-      bool nz = false;
+      tc_fence_after();
+      const uint32_t trow = tmem + (uint32_t)buf * P::NCOL + ((uint32_t)(32 * quarter) << 16);
+      if (NB >= 32) {
+        float v[32];
+        tmem_ld32(trow, v);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        v[i] = a[tid + 128 * i];
-        const float4 h = make_float4(tf32_round(v[i].x), tf32_round(v[i].y), tf32_round(v[i].z), tf32_round(v[i].w));
-        a[tid + 128 * i] = h;
-        nz |= (v[i].x != h.x) | (v[i].y != h.y) | (v[i].z != h.z) | (v[i].w != h.w);
+        for (int j = 0; j < 32; ++j) sR[j * RS + row] = v[j];
       }
-      if (__any_sync(0xffffffffu, nz) && lane == 0) atomicOr(&nzflag[s], 1);
-      fence_proxy_async();
-      named_bar(1, 128);
-      const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
-      mbar_arrive(&ready[s]);  // release: Ah visible to the MMA lane
-      if (two) {
-        if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) {
-          *abort = 1;
-          break;
+      if (NB == 16 || NB == 48) {
+        float v[16];
+        tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * RS + row] = v[j];
+      }
+      tc_fence_before();
+      mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
+      const int y0 = 128 * rb;
+      for (int i = etid; i < (Ny + 1) * 128; i += 128) {
+        const int v = i >> 7, r = i & 127, y = y0 + r;
+        sRT[v * RS + r] = y < Ly ? ytab[(size_t)v * Ly + y] : make_float2(0.f, 0.f);
+      }
+      named_bar(2, 128);
+      const int nps = part_stride > 0 ? part_stride : rows * ncs;
+      float2* out = win_part + ((size_t)img * nps + (rb * ncs + cs)) * KY * NU;
+      // one thread per (|v|, u): four row sums give both outputs +v and -v
+      //   S1 = sum c tx, S2 = sum s ty, S3 = sum c ty, S4 = sum s tx
+      //   (+v): (S1 - S2, S3 + S4)    (-v): (S1 + S2, S4 - S3)
+      // with c, s the cos / -sin accumulator columns of u (s = 0 for u = 0)
+      for (int pq = etid; pq < (Ny + 1) * NU; pq += 128) {
+        const int av = pq / NU, u = pq - av * NU;
+        const float* rc = sR + u * RS;
+        const float* rs = sR + (Nx + u) * RS;
+        const float2* rt = sRT + av * RS;
+        float s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
+        if (u == 0) {
+#pragma unroll 8
+          for (int r = 0; r < 128; ++r) {
+            const float2 tw = rt[r];
+            const float c = rc[r];
+            s1 = fmaf(c, tw.x, s1);
+            s3 = fmaf(c, tw.y, s3);
+          }
+        } else {
+#pragma unroll 8
+          for (int r = 0; r < 128; ++r) {
+            const float2 tw = rt[r];
+            const float c = rc[r], sn = rs[r];
+            s1 = fmaf(c, tw.x, s1);
+            s2 = fmaf(sn, tw.y, s2);
+            s3 = fmaf(c, tw.y, s3);
+            s4 = fmaf(sn, tw.x, s4);
+          }
         }
-        ph2 ^= 1u << s;
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-          a[tid + 128 * i] = make_float4(v[i].x - tf32_round(v[i].x), v[i].y - tf32_round(v[i].y),
-                                         v[i].z - tf32_round(v[i].z), v[i].w - tf32_round(v[i].w));
-        fence_proxy_async();
-        mbar_arrive(&ready2[s]);
+        out[(Ny + av) * NU + u] = make_float2((s1 - s2) * inv_ff, (s3 + s4) * inv_ff);
+        if (av > 0) out[(Ny - av) * NU + u] = make_float2((s1 + s2) * inv_ff, (s4 - s3) * inv_ff);
       }
+      named_bar(2, 128);  // sR / sRT are free for the next tile
     }
   }
   // the MMA lane always commits `done`; everyone waits for the tensor cores to drain
   if (!mbar_wait(done, 0)) *abort = 1;
   __syncthreads();
   if (*abort) {
-    if (tid == 160) mbar_wait(done, 0, 200u);  // the MMA lane's final commit covers all it issued
-    if (tid == 128)                            // warp 4 lane 0: wait for the last load of every stage
+    if (tid == 256)  // warp 8 lane 0: wait for the last load of every stage
       for (int s = 0; s < S; ++s)
         if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / S) & 1u, 200u);
     if (tid == 0) atomicExch(err, 1);
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, P::NCOL);
-    return;
-  }
-  tc_fence_after();
-  float* sR = reinterpret_cast<float*>(sm);  // [NB][128]
-  if (warp < 4) {
-    const int row = 32 * warp + lane;
-    const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
-    if (NB >= 32) {
-      float v[32];
-      tmem_ld32(trow, v);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) sR[j * 128 + row] = v[j];
-    }
-    if (NB == 16 || NB == 48) {
-      float v[16];
-      tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * 128 + row] = v[j];
-    }
-  }
-  float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NB * 128 * sizeof(float));
-  const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
-  for (int idx = tid; idx < (Ny + 1) * 128; idx += TC_THREADS) {
-    const int v = idx / 128, r = idx - v * 128;
-    long long m = ((long long)v * (y0 + r + oyc)) % Fy;
-    if (m < 0) m += Fy;
-    float sn, cs;
-    sincospif(2.0f * (float)m / (float)Fy, &sn, &cs);
-    sRT[idx] = make_float2(cs, -sn);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, P::NCOL);
-
-  const int KY = 2 * Ny + 1, NU = Nx + 1;
-  const float scale = 1.0f / ((float)Fx * (float)Fy);
-  const int nps = part_stride > 0 ? part_stride : (int)(gridDim.x * gridDim.z);
-  float2* out = win_part + ((size_t)img * nps + rb * ncs + cs) * KY * NU;
-  for (int o = tid; o < KY * NU; o += TC_THREADS) {
-    const int vi = o / NU, u = o - vi * NU;
-    const int v = vi - Ny;
-    const int av = v < 0 ? -v : v;
-    const float ts = v < 0 ? -1.f : 1.f;
-    const float* rc = sR + u * 128;
-    const float* rs = sR + (Nx + u) * 128;
-    const float2* rt = sRT + av * 128;
-    float re = 0.f, im = 0.f;
-    if (u == 0) {
-      for (int r = 0; r < 128; ++r) {
-        const float2 t = rt[r];
-        re = fmaf(rc[r], t.x, re);
-        im = fmaf(rc[r], ts * t.y, im);
-      }
-    } else {
-      for (int r = 0; r < 128; ++r) {
-        const float2 t = rt[r];
-        const float ty = ts * t.y;
-        re = fmaf(rc[r], t.x, fmaf(-rs[r], ty, re));
-        im = fmaf(rc[r], ty, fmaf(rs[r], t.x, im));
-      }
-    }
-    out[o] = make_float2(re * scale, im * scale);
-  }
+  if (warp == 0) tmem_dealloc(tmem, 2 * P::NCOL);
 }
 
 // ---------------------------------------------------------------------------
@@ -658,6 +747,16 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
     twT_init_kernel<<<dim3((g.Lx + 127) / 128, NB), 128, 0, ctx->stream>>>(twh, twl, g.Lx, g.Fx, g.Nx, NB);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
+  // row twiddles of the epilogue, cached per (Ly, Fy, Ny)
+  float* yt = nullptr;
+  LITHO_RET(cached_table(ctx, std::make_tuple(g.Ly, g.Fy, g.Ny, -3000), (size_t)(g.Ny + 1) * g.Ly * sizeof(float2),
+                         &fresh, &yt));
+  if (fresh) {
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    ytab_init_kernel<<<dim3((g.Ly + 127) / 128, g.Ny + 1), 128, 0, ctx->stream>>>(
+        reinterpret_cast<float2*>(yt), g.Ly, g.Fy);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
   CUtensorMap mM, mBh, mBl;
   LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
   LITHO_RET(make_map(ctx, &mBh, twh, 2, g.Lx, NB, 1, NB));
@@ -665,10 +764,14 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   const size_t smem = WinTC<NB>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  dim3 grid((g.Ly + 127) / 128, p.batch, std::max(1, p.colSplits));
+  const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
+  const int tiles = rows * p.batch * ncs;
+  const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
-  win_dft_tc_kernel<NB><<<grid, TC_THREADS, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
-                                                                  win_part, p.part_stride, err);
+  win_dft_tc_kernel<NB><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
+                                                                 rows, p.batch, ncs,
+                                                                 reinterpret_cast<const float2*>(yt), win_part,
+                                                                 p.part_stride, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }

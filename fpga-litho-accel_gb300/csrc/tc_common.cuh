@@ -54,21 +54,42 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity, uint32_
       : "memory");
   return ok != 0;
 }
-// bounded: at most `limit` suspensions of <= 1 ms each
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1000) {
-  for (uint32_t i = 0; i < limit; ++i)
-    if (mbar_try(bar, parity, 1000000u)) return true;
-  return false;
+// try_wait without a suspend-time hint: returns as soon as the phase completes,
+// or after a short system-dependent time if it does not
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
 }
-// As mbar_wait, but also gives up as soon as *abort (shared, set by another role)
-// is non-zero; suspensions are 20 us so the flag is looked at regularly.
-__device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, uint32_t parity, volatile int* abort,
-                                             uint32_t limit = 50000) {
-  for (uint32_t i = 0; i < limit; ++i) {
-    if (mbar_try(bar, parity, 20000u)) return true;
-    if (*abort) return false;
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded: gives up after `limit` milliseconds
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1000) {
+  if (mbar_poll(bar, parity)) return true;
+  const uint64_t t0 = global_ns(), lim = (uint64_t)limit * 1000000ull;
+  while (true) {
+    if (mbar_poll(bar, parity)) return true;
+    if (global_ns() - t0 > lim) return false;
   }
-  return false;
+}
+// As mbar_wait (limit ~1 s), but also gives up as soon as *abort (shared, set by
+// another role) is non-zero.
+__device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                             uint32_t limit_ms = 1000) {
+  if (mbar_poll(bar, parity)) return true;
+  const uint64_t t0 = global_ns(), lim = (uint64_t)limit_ms * 1000000ull;
+  while (true) {
+    if (mbar_poll(bar, parity)) return true;
+    if (*abort) return false;
+    if (global_ns() - t0 > lim) return false;
+  }
 }
 // named barrier over `count` threads (multiple of 32)
 __device__ __forceinline__ void named_bar(int id, int count) {
