@@ -42,7 +42,7 @@ METRIC = "aerial images/s at 1024^2 K=24: mixed/batched/surrogate vs plain GPU a
 L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
 # DRAM bytes (read + write) per mask of the dominant kernel, from an ncu capture of one
 # win_dft_tc launch on 48 masks of this workload (the traffic scales with the masks).
-TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.772288e6 + 3.230464e6) / 48}
+TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.713408e6 + 3.601408e6) / 48}
 WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
             "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
 
@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])
     p.add_argument("--no-surrogate", action="store_true")
+    p.add_argument("--no-large-tcc", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="warm-up + timed steps of both forms only (no clock sampling, e2e, CPU or surrogate legs)")
     p.add_argument("--surrogate-epochs", type=int, default=10)
@@ -211,6 +213,122 @@ def run_reference(args, ws, rank):
                                        f"(128^2 conv grid, embed 94) + FI in FP64, scipy.fft workers={cores}"},
             "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batched_leg(ctx, setup, reps=20):
+    """The batched workload: 256 seeded masks with sides drawn from {256, 512, 768, 1024, 2048}
+    and 20-60 % density (rectangles with sides L/64..L/8, count set by the drawn density),
+    imaged per size class in one CUDA graph (litho_batch_plan_*, autotuned).  Masks up to 1024
+    are centred in a 1024 period and use the K=24 kernels above; 2048 masks use a 2048-period
+    kernel set of the same optics (Nx = 16, tcc 1089, K = 24)."""
+    import math
+    import numpy as np
+    import torch
+    import litho_gb300 as LG
+    from litho_gb300 import surrogate as S
+    ctx.set_stream(None)
+    rng = np.random.default_rng(31)
+    sizes = rng.choice([256, 512, 768, 1024, 2048], size=256)
+    dens = rng.uniform(0.2, 0.6, size=256)
+    sig, src = setup["sigma"], setup["src"]
+    nx2 = LG.optics_n(NA, 2048, sig, WAVELENGTH)
+    t2 = ctx.calc_tcc(src, sig, WAVELENGTH, NA, DEFOCUS, 2048, 2048, nx2, nx2)
+    k2, s2, _ = ctx.calc_kernels(t2, K_KERNELS)
+    res = {"config": {"masks": 256, "sizes": {int(v): int((sizes == v).sum()) for v in (256, 512, 768, 1024, 2048)},
+                      "periods": [1024, 2048], "Nx": [setup["nx"], nx2], "K": K_KERNELS}}
+    items = [(0 if m <= 1024 else 1, int(m), int(m)) for m in sizes]
+    masks = []
+    for i, (m, d) in enumerate(zip(sizes, dens)):
+        lo, hi = max(1, int(m) // 64), max(2, int(m) // 8)
+        area = ((lo + hi) / 2.0) ** 2
+        n = int(min(256, max(1, round(-math.log(1.0 - d) * m * m / area))))
+        masks.append(S.rect_masks(ctx, 31, i, 1, int(m), nmin=n, nmax=n, wmin=lo, wmax=hi)[0])
+    torch.cuda.synchronize()
+    res["config"]["density_mean"] = float(np.mean([float(x.mean()) for x in masks]))
+    pix = float(sum(int(m) ** 2 for m in sizes))
+    for form, prec in (("plain", LG.PREC_FP32), ("mixed", LG.PREC_MIXED)):
+        f = setup[form]
+        sets = [ctx.kernel_set(f["krn"], f["s32"], setup["nx"], setup["nx"]), ctx.kernel_set(k2, s2, nx2, nx2)]
+        t0 = time.perf_counter()
+        plan = LG.BatchPlan(ctx, sets, [1024, 2048], items, precision=prec)
+        t_plan = time.perf_counter() - t0
+        for i, m in enumerate(masks):
+            plan.mask(i).copy_(m)
+        torch.cuda.synchronize()
+        plan.run()
+        ctx.synchronize()
+        st = torch.cuda.Stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ctx.set_stream(st.cuda_stream)
+        try:
+            e0.record(st)
+            for _ in range(reps):
+                plan.run()
+            e1.record(st)
+            torch.cuda.synchronize()
+        finally:
+            ctx.set_stream(None)
+        ms = e0.elapsed_time(e1) / reps
+        res[form] = {"images_per_s": 256 / (ms * 1e-3), "ms_per_batch": ms, "mask_mpix_per_s": pix / (ms * 1e-3) / 1e6,
+                     "plan_create_s": t_plan, "tuned": plan.describe().get("classes")}
+        plan.close()
+        for k in sets:
+            k.close()
+    return res
+
+
+def large_tcc_leg(ctx):
+    """The large-TCC workload: 2048^2 period at 1 nm/px, NA 1.35 (immersion, n = 1.44),
+    193 nm, annular source sigma 0.7-0.95 on a 113^2 grid (4,044 points): Nx = 27 by the
+    reference's formula, a 3025^2 TCC, top K = 48 eigenpairs.  Split-BF16 tensor-core TCC and
+    FP64 TCC, FP64 eigensolve of both; device times from the library's stage events;
+    errors of the split-BF16 form against the FP64 form."""
+    import numpy as np
+    import litho_gb300 as LG
+    from litho_gb300 import synth
+    ctx.set_stream(None)
+    NA_, LAM, L_, NMED, K = 1.35, 193.0, 2048, 1.44, 48
+    src = synth.annular_source(113, 0.7, 0.95)
+    sig = LG.outer_sigma(src)
+    nx = LG.optics_n(NA_, L_, sig, LAM)
+    npts = int((src > 0).sum())
+    res = {"config": {"L": L_, "NA": NA_, "wavelength": LAM, "n_medium": NMED, "source": "annular 0.7-0.95",
+                      "source_points": npts, "Nx": nx, "tcc": (2 * nx + 1) ** 2, "K": K}}
+    out = {}
+    for form, prec in (("fp64", LG.TCC_FP64), ("split_bf16", LG.TCC_SPLIT_BF16)):
+        ctx.calc_tcc(src, sig, LAM, NA_, 0.0, L_, L_, nx, nx, precision=prec, n_medium=NMED)  # warm
+        ctx.stage_times(reset=True)
+        ctx.enable_timing(True)
+        t0 = time.perf_counter()
+        tcc = ctx.calc_tcc(src, sig, LAM, NA_, 0.0, L_, L_, nx, nx, precision=prec, n_medium=NMED)
+        t1 = time.perf_counter()
+        k64, s32, s64 = ctx.calc_kernels(tcc, K)
+        t2 = time.perf_counter()
+        st = ctx.stage_times(reset=True)
+        ctx.enable_timing(False)
+        n = tcc.shape[0]
+        flops = 8.0 * npts * n * n
+        res[form] = {"tcc_device_ms": st["tcc"][0], "tcc_call_s": t1 - t0, "eig_device_ms": st["eig"][0],
+                     "eig_call_s": t2 - t1,
+                     "tcc_tflops_effective": flops / (st["tcc"][0] * 1e-3) / 1e12 if st["tcc"][0] else None}
+        out[form] = (tcc, k64, s64)
+    t64, k64, w64 = out["fp64"]
+    tbf, kbf, wbf = out["split_bf16"]
+    err = {"tcc": float(np.linalg.norm(tbf - t64) / np.linalg.norm(t64)),
+           "eigenvalues": float(np.max(np.abs(wbf - w64) / np.abs(w64)))}
+    V, W = k64[:, ::-1].T, kbf[:, ::-1].T
+    proj, i = 0.0, 0
+    while i < K:
+        j = i + 1
+        while j < K and abs(w64[j - 1] - w64[j]) <= 1e-6 * w64[0]:
+            j += 1
+        if j < K:
+            a, b = W[:, i:j], V[:, i:j]
+            proj = max(proj, float(np.linalg.norm(a @ a.conj().T - b @ b.conj().T)))
+        i = j
+    err["kernel_projector"] = proj
+    res["split_bf16_vs_fp64"] = err
+    return res
 
 
 def surrogate_leg(ctx, epochs):
@@ -439,6 +557,10 @@ def main():
         line["rel_l2_vs_fp64"] = err
     if rank == 0 and not args.no_surrogate:
         line["forms"]["surrogate"] = surrogate_leg(ctx, args.surrogate_epochs)
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_leg(ctx, setup)
+    if rank == 0 and not args.no_large_tcc:
+        line["large_tcc"] = large_tcc_leg(ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     for k in ks.values():

@@ -166,7 +166,7 @@ int default_conv_n(int Nx, int Ny);
 
 int calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength, float NA,
                   float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision, int mem, int sh_in,
-                  int oSgm_in);
+                  int oSgm_in, float n_medium = 1.0f);
 
 // Host input -> device staging buffer (device input passes through).
 int stage_in(litho_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem, const void** dev);

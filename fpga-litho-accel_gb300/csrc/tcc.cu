@@ -21,6 +21,7 @@ struct PupilParams {
   int Nx, Ny, tccSize, ns;
   int sh;
   float Lx_norm, Ly_norm, dzk, NA;
+  double nm2;  // immersion index squared: 1 reproduces litho.cpp:463
 };
 
 // The reference's per-source support bounds (litho.cpp:449-454): C truncation.
@@ -50,7 +51,7 @@ __global__ void pupil_kernel(const int2* __restrict__ pq, PupilParams pp, float2
       const float rho2 = __fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy));
       if ((double)rho2 <= 1.0) {
         const float r = __fmul_rn(__fmul_rn(rho2, pp.NA), pp.NA);
-        const double val = (double)pp.dzk * sqrt(1.0 - (double)r);
+        const double val = (double)pp.dzk * sqrt(pp.nm2 - (double)r);
         const float ph = (float)val;
         float sn, cs;
         sincosf(ph, &sn, &cs);
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(256) tcc_fp64_kernel(const float2* __restrict_
 // check that every pupil point the reference would store lies on the grid.
 int tcc_sources(litho_ctx* ctx, const float* src_h, int S, float outerSigma, float wavelength, float NA,
                 float defocus, int Lx, int Ly, int Nx, int Ny, std::vector<SrcPt>& pts, PupilParams& pp,
-                int sh_in = -1, int oSgm_in = -1) {
+                int sh_in = -1, int oSgm_in = -1, float n_medium = 1.0f) {
   // litho.cpp:429-430; the FPGA top (calc_tcc.cpp:34-42) receives sh and oSgm from its caller instead
   const int sh = sh_in >= 0 ? sh_in : (int)((S - 1) / 2.0);
   volatile float osf = (float)sh * outerSigma;
@@ -148,7 +149,8 @@ int tcc_sources(litho_ctx* ctx, const float* src_h, int S, float outerSigma, flo
   volatile float lyn = (float)Ly * NA;
   const float Lx_norm = lxn / wavelength, Ly_norm = lyn / wavelength;
   volatile float dzk = dz * k;
-  pp = PupilParams{Nx, Ny, (2 * Nx + 1) * (2 * Ny + 1), 0, sh, Lx_norm, Ly_norm, (float)dzk, NA};
+  pp = PupilParams{Nx, Ny, (2 * Nx + 1) * (2 * Ny + 1), 0, sh, Lx_norm, Ly_norm, (float)dzk, NA,
+                   (double)n_medium * (double)n_medium};
   pts.clear();
   for (int q = -oSgm; q <= oSgm; ++q)
     for (int p = -oSgm; p <= oSgm; ++p) {
@@ -219,7 +221,7 @@ using namespace litho;
 // top receives them from its caller); -1 derives them as litho.cpp:429-430.
 int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float outerSigma, float wavelength,
                          float NA, float defocus, int Lx, int Ly, int Nx, int Ny, double* tcc, int tccPrecision,
-                         int mem, int sh_in, int oSgm_in) {
+                         int mem, int sh_in, int oSgm_in, float n_medium) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_ARG_CHECK(ctx, src && tcc, "null pointer");
   LITHO_ARG_CHECK(ctx, srcSize >= 1 && srcSize <= 4097, "srcSize %d outside [1, 4097]", srcSize);
@@ -228,6 +230,7 @@ int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float ou
   LITHO_ARG_CHECK(ctx, outerSigma >= 0.f && outerSigma <= 1.f, "outerSigma %g outside [0, 1] (litho.cpp:1298 clamps)",
                   outerSigma);
   LITHO_ARG_CHECK(ctx, tccPrecision == LITHO_TCC_FP64 || tccPrecision == LITHO_TCC_SPLIT_BF16, "bad tccPrecision");
+  LITHO_ARG_CHECK(ctx, n_medium > 0.f && std::isfinite(n_medium), "n_medium %g must be positive", n_medium);
   LITHO_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   std::vector<float> src_h;
   const float* sh = src;
@@ -241,7 +244,7 @@ int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float ou
   std::vector<SrcPt> pts;
   PupilParams pp;
   LITHO_RET(tcc_sources(ctx, sh, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, pts, pp, sh_in,
-                        oSgm_in));
+                        oSgm_in, n_medium));
   const int n = pp.tccSize, ns = pp.ns;
   const int ldp = ((ns + 63) / 64) * 64 + 64;  // padded, multiple of 64 (tensor-core K tiles)
   LITHO_RET(ctx->tcc_a.ensure(ctx, (size_t)n * ldp * sizeof(float2)));
@@ -274,7 +277,9 @@ int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float ou
     LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     for (size_t i = 0; i < (size_t)2 * n * n; ++i)
       if (!std::isfinite(tcc[i])) {
-        set_error(ctx, LITHO_ERR_NAN, "non-finite TCC entry (NA > 1 makes the pupil phase NaN, litho.cpp:463)");
+        set_error(ctx, LITHO_ERR_NAN,
+                  "non-finite TCC entry (NA > n_medium makes the pupil phase NaN, litho.cpp:463; "
+                  "litho_calc_tcc_medium takes an immersion index)");
         return LITHO_ERR_NAN;
       }
   }
@@ -286,4 +291,13 @@ extern "C" int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, flo
                               int mem) {
   return litho::calc_tcc_impl(ctx, src, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, tcc,
                               tccPrecision, mem, -1, -1);
+}
+
+// Immersion extension: the pupil phase dz k sqrt(n^2 - rho^2 NA^2) (n = 1 is litho.cpp:463,
+// which is NaN wherever rho NA > 1, even at zero defocus)
+extern "C" int litho_calc_tcc_medium(litho_ctx* ctx, const float* src, int srcSize, float outerSigma,
+                                     float wavelength, float NA, float defocus, float n_medium, int Lx, int Ly,
+                                     int Nx, int Ny, double* tcc, int tccPrecision, int mem) {
+  return litho::calc_tcc_impl(ctx, src, srcSize, outerSigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, tcc,
+                              tccPrecision, mem, -1, -1, n_medium);
 }

@@ -68,6 +68,7 @@ _SIGS = {
     "litho_image_batch": (_i, [_p, _p, _p, _i, _i, _i, _p, _i, _i]),
     "litho_calc_tcc": (_i, [_p, _p, _i, _f, _f, _f, _f, _i, _i, _i, _i, _p, _i, _i]),
     "litho_calc_kernels": (_i, [_p, _p, _i, _i, _p, _p, _p, _p, _p, _i]),
+    "litho_calc_tcc_medium": (_i, [_p, _p, _i, _f, _f, _f, _f, _f, _i, _i, _i, _i, _p, _i, _i]),
     "litho_calc_image": (_i, [_p, _p, _p, _i, _i, _p, _i, _i, _i, _i, _i, _p, _i]),
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
@@ -389,13 +390,18 @@ class Context:
 
     # -- calcTCC ---------------------------------------------------------------
     def calc_tcc(self, src, outer_sigma_: float, wavelength: float, NA: float, defocus: float,
-                 Lx: int, Ly: int, Nx: int, Ny: int, precision: int = TCC_FP64) -> np.ndarray:
-        """calcTCC (litho.cpp:428-516). Returns complex128 (tcc, tcc)."""
+                 Lx: int, Ly: int, Nx: int, Ny: int, precision: int = TCC_FP64, n_medium: float = 1.0) -> np.ndarray:
+        """calcTCC (litho.cpp:428-516). Returns complex128 (tcc, tcc).  n_medium != 1 uses the
+        immersion form of the pupil phase (litho_calc_tcc_medium)."""
         s = _host_f32(src)
         n = (2 * Nx + 1) * (2 * Ny + 1)
         out = np.empty((n, n), np.complex128)
-        self._check(_lib.litho_calc_tcc(self.h, _ptr(s), int(s.shape[0]), outer_sigma_, wavelength, NA, defocus,
-                                        Lx, Ly, Nx, Ny, _ptr(out), precision, MEM_HOST))
+        if n_medium == 1.0:
+            self._check(_lib.litho_calc_tcc(self.h, _ptr(s), int(s.shape[0]), outer_sigma_, wavelength, NA, defocus,
+                                            Lx, Ly, Nx, Ny, _ptr(out), precision, MEM_HOST))
+        else:
+            self._check(_lib.litho_calc_tcc_medium(self.h, _ptr(s), int(s.shape[0]), outer_sigma_, wavelength, NA,
+                                                   defocus, n_medium, Lx, Ly, Nx, Ny, _ptr(out), precision, MEM_HOST))
         return out
 
     # -- calcKernels -----------------------------------------------------------

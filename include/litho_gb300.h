@@ -295,6 +295,14 @@ int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSig
                    float wavelength, float NA, float defocus, int Lx, int Ly, int Nx, int Ny,
                    double* tcc, int tccPrecision, int mem);
 
+/* Immersion extension (no reference counterpart): the pupil phase is
+ * dz k sqrt(n_medium^2 - rho^2 NA^2) instead of litho.cpp:463's sqrt(1 - rho^2 NA^2),
+ * so NA > 1 (immersion optics) gives a finite TCC when n_medium >= NA.
+ * n_medium = 1 is litho_calc_tcc. */
+int litho_calc_tcc_medium(litho_ctx* ctx, const float* src, int srcSize, float outerSigma,
+                          float wavelength, float NA, float defocus, float n_medium, int Lx, int Ly,
+                          int Nx, int Ny, double* tcc, int tccPrecision, int mem);
+
 /* ---- SOCS kernels (litho.cpp:579-645 calcKernels) --------------------------
  * Top-nk eigenpairs of the Hermitian tcc (interleaved float64, upper triangle
  * used as zheevr 'U').  scales descending (float32, and optionally float64);

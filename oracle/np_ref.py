@@ -222,12 +222,14 @@ def ft_c2r_padded(spec: np.ndarray, out_x: int, out_y: int) -> np.ndarray:
 # ---------------------------------------------------------------------------
 
 def pupil_matrix(src: np.ndarray, outer_sigma: float, wavelength: float, NA: float,
-                 defocus: float, Lx: int, Ly: int, Nx: int, Ny: int):
+                 defocus: float, Lx: int, Ly: int, Nx: int, Ny: int, n_medium: float = 1.0):
     """The pupil table of litho.cpp:437-471 restricted to lit source points.
 
     Returns (P, J, ids): P is complex128 (tccSize, n_lit) with the float32
     cos/sin of the float32 phase, J the float32 source weights, ids the source
-    pixel indices in the reference's (q, p) loop order.
+    pixel indices in the reference's (q, p) loop order.  n_medium != 1 is the
+    immersion extension of the phase, sqrt(n^2 - rho^2 NA^2) (the reference's
+    sqrt(1 - rho^2 NA^2) is NaN wherever rho NA > 1).
     """
     S = src.shape[0]
     srcf = src.astype(np.float32).ravel()
@@ -262,7 +264,8 @@ def pupil_matrix(src: np.ndarray, outer_sigma: float, wavelength: float, NA: flo
             ok = ((FY * FY) <= 1) & (rho2.astype(np.float64) <= 1.0)
             r = (rho2 * NAf).astype(np.float32) * NAf
             with np.errstate(invalid="ignore"):
-                val = np.float64(f32(dz * k)) * np.sqrt(1.0 - r.astype(np.float32).astype(np.float64))
+                nm2 = float(n_medium) * float(n_medium)
+                val = np.float64(f32(dz * k)) * np.sqrt(nm2 - r.astype(np.float32).astype(np.float64))
             phase = val.astype(np.float32)
             idx = (NY + Ny) * (2 * Nx + 1) + NX + Nx
             if ok.any():
@@ -280,9 +283,9 @@ def pupil_matrix(src: np.ndarray, outer_sigma: float, wavelength: float, NA: flo
 
 
 def calc_tcc(src: np.ndarray, outer_sigma: float, wavelength: float, NA: float, defocus: float,
-             Lx: int, Ly: int, Nx: int, Ny: int) -> np.ndarray:
+             Lx: int, Ly: int, Nx: int, Ny: int, n_medium: float = 1.0) -> np.ndarray:
     """litho.cpp:428-516 ``calcTCC``: TCC = sum_s J_s p_s p_s^H, upper triangle then conj mirror."""
-    P, J, _ = pupil_matrix(src, outer_sigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny)
+    P, J, _ = pupil_matrix(src, outer_sigma, wavelength, NA, defocus, Lx, Ly, Nx, Ny, n_medium)
     T = (P * J.astype(np.float64)[None, :]) @ P.conj().T
     up = np.triu(T)
     return up + np.conj(np.triu(T, 1)).T

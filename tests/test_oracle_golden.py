@@ -77,3 +77,20 @@ def test_ft_r2c_padded_is_centred_fft():
     out = R.ft_r2c_padded(m, 32, 32)
     ref = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(R.pad_centered(m, 32, 32).astype(np.float64)))) / 1024
     np.testing.assert_allclose(out, ref, atol=1e-14)
+
+
+def test_immersion_extension_of_the_pupil():
+    """n_medium = 1 is the reference formula; NA > 1 is NaN there and finite with n = 1.44."""
+    from oracle import np_ref as R
+    src = R.normalize_source(R.create_annular(21, 0.6, 0.9))
+    sig = R.get_outer_sigma(src)
+    a = R.calc_tcc(src, sig, 193.0, 0.8, 0.2, 256, 256, 2, 2)
+    b = R.calc_tcc(src, sig, 193.0, 0.8, 0.2, 256, 256, 2, 2, n_medium=1.0)
+    assert np.array_equal(a, b)
+    nx = R.optics_nx(1.35, 128, sig, 193.0)
+    with np.errstate(invalid="ignore"):
+        c = R.calc_tcc(src, sig, 193.0, 1.35, 0.0, 128, 128, nx, nx)
+    assert not np.isfinite(c).all()
+    d = R.calc_tcc(src, sig, 193.0, 1.35, 0.0, 128, 128, nx, nx, n_medium=1.44)
+    assert np.isfinite(d).all()
+    assert np.allclose(d, d.conj().T)
