@@ -133,6 +133,15 @@ int litho_ctx_destroy(litho_ctx* ctx) {
     cudaEventDestroy(p.b);
   }
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  for (cudaStream_t st : {ctx->copy_in, ctx->copy_out})
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  for (int i = 0; i < 3; ++i)
+    for (cudaEvent_t e : {ctx->ev_in[i], ctx->ev_comp[i], ctx->ev_out[i]})
+      if (e) cudaEventDestroy(e);
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return LITHO_OK;
@@ -277,6 +286,59 @@ int default_conv_n(int Nx, int Ny) {
 
 }  // namespace litho
 
+// Host buffers: the batch moves in chunks of up to 8 masks through three device
+// staging slots each way.  Host->device copies run on one copy stream and
+// device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
+// while chunk k is imaged on the context's stream; events order the reuse of
+// every slot, and both copy streams join the context's stream at the end.
+static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
+                      float* images, int precision, size_t img) {
+  constexpr int NS = 3;
+  const int CH = batch < 16 ? batch : 8;
+  if (ctx->copy_in == nullptr) {
+    LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+    for (int i = 0; i < NS; ++i) {
+      LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_in[i], cudaEventDisableTiming));
+      LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_comp[i], cudaEventDisableTiming));
+      LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_out[i], cudaEventDisableTiming));
+    }
+    LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
+  }
+  const int nslot = (batch + CH - 1) / CH < NS ? (batch + CH - 1) / CH : NS;
+  LITHO_RET(ctx->stage_in.ensure(ctx, (size_t)nslot * CH * img));
+  LITHO_RET(ctx->stage_out.ensure(ctx, (size_t)nslot * CH * img));
+  char* din = ctx->stage_in.as<char>();
+  char* dout = ctx->stage_out.as<char>();
+  // both copy streams start after the caller's earlier work
+  LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_start, 0));
+  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_start, 0));
+  const int nchunk = (batch + CH - 1) / CH;
+  for (int k = 0; k < nchunk; ++k) {
+    const int sl = k % NS, nb = (k + 1) * CH <= batch ? CH : batch - k * CH;
+    const size_t off = (size_t)k * CH * img, bytes = (size_t)nb * img;
+    char* in = din + (size_t)sl * CH * img;
+    char* out = dout + (size_t)sl * CH * img;
+    if (k >= NS) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_comp[sl], 0));  // slot read
+    LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(in, reinterpret_cast<const char*>(masks) + off, bytes,
+                                        cudaMemcpyHostToDevice, ctx->copy_in));
+    LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_in[sl], ctx->copy_in));
+    LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[sl], 0));
+    if (k >= NS) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_out[sl], 0));  // slot drained
+    LITHO_RET(image_pipeline(ctx, g, nb, reinterpret_cast<const float*>(in), ks->krn, ks->scales,
+                             reinterpret_cast<float*>(out), precision));
+    LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_comp[sl], ctx->stream));
+    LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_comp[sl], 0));
+    LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(reinterpret_cast<char*>(images) + off, out, bytes, cudaMemcpyDeviceToHost,
+                                        ctx->copy_out));
+    LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_out[sl], ctx->copy_out));
+  }
+  // join: the context's stream continues after the last copy out
+  for (int i = 0; i < nslot; ++i) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_out[i], 0));
+  return LITHO_OK;
+}
+
 extern "C" {
 
 int litho_calc_socs(litho_ctx* ctx, const float* mskf_r, const float* mskf_i, int fftLx, int fftLy,
@@ -387,20 +449,13 @@ int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* m
     set_error(ctx, LITHO_ERR_UNSUPPORTED, "mixed precision needs Lx %% 32 == 0 and Nx <= 16 (Lx=%d)", Lx);
     return LITHO_ERR_UNSUPPORTED;
   }
-  const size_t bytes = (size_t)batch * Lx * Ly * sizeof(float);
-  const void* dm = nullptr;
-  LITHO_RET(stage_in(ctx, ctx->stage_in, masks, bytes, mem, &dm));
-  float* dimg = images;
-  if (mem == LITHO_MEM_HOST) {
-    LITHO_RET(ctx->stage_out.ensure(ctx, bytes));
-    dimg = ctx->stage_out.as<float>();
+  const size_t img = (size_t)Lx * Ly * sizeof(float);
+  if (mem == LITHO_MEM_DEVICE) {
+    return image_pipeline(ctx, g, batch, masks, ks->krn, ks->scales, images, precision);
   }
-  LITHO_RET(image_pipeline(ctx, g, batch, static_cast<const float*>(dm), ks->krn, ks->scales, dimg, precision));
-  if (mem == LITHO_MEM_HOST) {
-    LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(images, dimg, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (precision == LITHO_PREC_MIXED) LITHO_RET(tc_check_flag(ctx));
-  }
+  LITHO_RET(host_batch(ctx, g, batch, masks, ks, images, precision, img));
+  LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (precision == LITHO_PREC_MIXED) LITHO_RET(tc_check_flag(ctx));
   return LITHO_OK;
 }
 

@@ -110,6 +110,9 @@ struct litho_ctx {
   litho::DevBuf tcc_a, tcc_b, tcc_c, tcc_pq, eig_w, eig_v, eig_work, eig_info;
   // mixed-precision (tensor-core) workspaces
   litho::DevBuf mx_b, mx_c, mx_d;
+  // host-buffer batches: copy streams and per-slot events of the staging pipeline
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in[3] = {}, ev_comp[3] = {}, ev_out[3] = {}, ev_start = nullptr;
   // per-stage timers
   bool timing = false;
   double stage_ms[LITHO_STAGE_COUNT] = {};
