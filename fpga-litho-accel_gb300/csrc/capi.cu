@@ -286,7 +286,7 @@ int default_conv_n(int Nx, int Ny) {
 
 }  // namespace litho
 
-// Host buffers: the batch moves in chunks of up to 8 masks through three device
+// Host buffers: the batch moves in chunks of about 16 MB through three device
 // staging slots each way.  Host->device copies run on one copy stream and
 // device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
 // while chunk k is imaged on the context's stream; events order the reuse of
@@ -294,7 +294,8 @@ int default_conv_n(int Nx, int Ny) {
 static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
                       float* images, int precision, size_t img) {
   constexpr int NS = 3;
-  const int CH = batch < 16 ? batch : 8;
+  // ~16 MB chunks: short pipeline fill and drain, enough masks per launch
+  const int CH = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, ((size_t)16 << 20) / img));
   if (ctx->copy_in == nullptr) {
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));

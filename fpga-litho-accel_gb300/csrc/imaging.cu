@@ -43,7 +43,7 @@ __device__ __forceinline__ int pmod(long long a, int m) {
 // exp(sign * 2 pi i * m / F) for an exact integer phase m (the argument of
 // sincospif is exact because F is a power of two).
 __device__ __forceinline__ float2 cis_exact(long long m, int F, float sign) {
-  const int r = pmod(m, F);
+  const int r = (int)(m & (long long)(F - 1));  // F (an FFT size) is a power of two
   float s, c;
   sincospif(2.0f * (float)r / (float)F, &s, &c);
   return make_float2(c, sign * s);

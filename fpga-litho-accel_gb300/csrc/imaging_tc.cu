@@ -421,43 +421,60 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
 // ---------------------------------------------------------------------------
 // FI prep for the tensor-core contraction: TmT[img][X][KP] split hi/lo
 // ---------------------------------------------------------------------------
-constexpr int FPT_THREADS = 128;
+// FI step 1 for the tensor cores.  band_reduce_kernel sums the SOCS band
+// partials of each image once; fi_prep_tc_kernel computes the T rows of
+// FPT_COLS image columns per CTA (four threads per column, each a quarter of the
+// fy rows) with column twiddles from a cached table, and writes hi/lo K-major
+// ([img][X][KP]) for the MMA.
+constexpr int FPT_THREADS = 256, FPT_COLS = 64;
+
+__global__ void band_reduce_kernel(const float2* __restrict__ band_part, int ngroups, int n, float2* __restrict__ S) {
+  const int img = blockIdx.y, idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < n) S[(size_t)img * n + idx] = sum_strided(band_part + (size_t)img * ngroups * n + idx, (size_t)n, ngroups);
+}
+
+// twF[d][X] = e^{+2 pi i d x'/Fx}, d = 0..2Nx
+__global__ void twF_init_kernel(float2* __restrict__ tw, int Lx, int Fx, int ND) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, d = blockIdx.y;
+  if (x >= Lx || d >= ND) return;
+  const int xp = x + (Fx - Lx) / 2 - Fx / 2;
+  const int m = (d * xp) & (Fx - 1);
+  float sn, cs;
+  sincospif(2.0f * (float)m / (float)Fx, &sn, &cs);
+  tw[(size_t)d * Lx + x] = make_float2(cs, sn);
+}
 
 template <int MAXD>
-__global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ band_part, int ngroups,
-                                                                 int Lx, int Fx, int Nx, int Ny, int KP,
+__global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ Sg, const float2* __restrict__ twF,
+                                                                 int Lx, int Nx, int Ny, int KP,
                                                                  float* __restrict__ tmh, float* __restrict__ tml) {
   extern __shared__ __align__(16) float2 fps[];
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
-  float2* sS = fps;                                     // [BH][BW]
-  float* sO = reinterpret_cast<float*>(fps + BH * BW);  // [128][KP+1]
+  float2* sS = fps;                                             // [BH][BW]
+  float2* sTw = sS + BH * BW;                                   // [MAXD][FPT_COLS]
+  float* sO = reinterpret_cast<float*>(sTw + MAXD * FPT_COLS);  // [FPT_COLS][KP+1]
   const int tid = threadIdx.x, img = blockIdx.y;
-  const int X0 = blockIdx.x * FPT_THREADS, X = X0 + tid;
-  const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) sS[idx] = sum_strided(B + idx, (size_t)BH * BW, ngroups);
-  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
-  float2 tw[MAXD];
-#pragma unroll
-  for (int d = 0; d < MAXD; ++d) {
-    long long m = ((long long)d * xp) % Fx;
-    if (m < 0) m += Fx;
-    float sn, cs;
-    sincospif(2.0f * (float)m / (float)Fx, &sn, &cs);
-    tw[d] = d < ND ? make_float2(cs, sn) : make_float2(0.f, 0.f);
+  const int X0 = blockIdx.x * FPT_COLS;
+  const float2* S0 = Sg + (size_t)img * BH * BW;
+  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) sS[idx] = S0[idx];
+  for (int idx = tid; idx < MAXD * FPT_COLS; idx += FPT_THREADS) {
+    const int d = idx / FPT_COLS, c = idx % FPT_COLS;
+    sTw[idx] = (d < ND && X0 + c < Lx) ? twF[(size_t)d * Lx + X0 + c] : make_float2(0.f, 0.f);
   }
+  for (int idx = tid; idx < FPT_COLS * (KP + 1); idx += FPT_THREADS) sO[idx] = 0.f;
   __syncthreads();
-  float* o = sO + tid * (KP + 1);
-  for (int r = 4 * Ny + 1; r < KP; ++r) o[r] = 0.f;
-  for (int fy = 0; fy < BH; ++fy) {
+  const int c = tid >> 2, q = tid & 3;
+  float* o = sO + c * (KP + 1);
+  for (int fy = q; fy < BH; fy += 4) {
     const float2* S = sS + fy * BW + 2 * Nx;
     float re = S[0].x, im = S[0].y;
 #pragma unroll
     for (int d = 1; d < MAXD; ++d) {
       if (d < ND) {
-        const float2 t = tw[d];
-        const float2 p = S[d], q = S[-d];
-        re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
-        im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+        const float2 t = sTw[d * FPT_COLS + c];
+        const float2 p = S[d], qv = S[-d];
+        re += (p.x + qv.x) * t.x - (p.y - qv.y) * t.y;
+        im += (p.y + qv.y) * t.x + (p.x - qv.x) * t.y;
       }
     }
     if (fy == 0) {
@@ -468,14 +485,16 @@ __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* _
     }
   }
   __syncthreads();
-  const size_t base = ((size_t)img * Lx + X0) * KP;
-  const int nrow = min(FPT_THREADS, Lx - X0);
-  for (int idx = tid; idx < nrow * KP; idx += FPT_THREADS) {
-    const int xr = idx / KP, r = idx - xr * KP;
-    const float v = sO[xr * (KP + 1) + r];
-    const float h = tf32_round(v);
-    tmh[base + idx] = h;
-    tml[base + idx] = v - h;
+  const int nrow = min(FPT_COLS, Lx - X0);
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int xr = warp; xr < nrow; xr += FPT_THREADS / 32) {  // one output row (KP floats) per warp pass
+    const size_t rowb = ((size_t)img * Lx + X0 + xr) * KP;
+    for (int r = lane; r < KP; r += 32) {
+      const float v = sO[xr * (KP + 1) + r];
+      const float h = tf32_round(v);
+      tmh[rowb + r] = h;
+      tml[rowb + r] = v - h;
+    }
   }
 }
 
@@ -815,8 +834,10 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   return LITHO_OK;
 }
 
+// hi/lo T rows [2][batch][Lx][KP] float, then the reduced band [batch][2Ny+1][4Nx+1] float2
 size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch) {
-  return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float);
+  return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float) +
+         (size_t)batch * (2 * g.Ny + 1) * (4 * g.Nx + 1) * sizeof(float2);
 }
 
 // tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
@@ -848,13 +869,28 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
   float* tml = tmh + (size_t)p.batch * g.Lx * KP;
   {
     const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
-    const size_t smem = (size_t)BH * BW * sizeof(float2) + (size_t)FPT_THREADS * (KP + 1) * sizeof(float);
+    // column twiddles, cached per (Lx, Fx, Nx)
+    float* twf = nullptr;
+    LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -4000), (size_t)ND * g.Lx * sizeof(float2), &fresh,
+                           &twf));
+    if (fresh) {
+      StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+      twF_init_kernel<<<dim3((g.Lx + 127) / 128, ND), 128, 0, ctx->stream>>>(reinterpret_cast<float2*>(twf), g.Lx,
+                                                                             g.Fx, ND);
+      LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    float2* S = reinterpret_cast<float2*>(tml + (size_t)p.batch * g.Lx * KP);  // tail of the workspace
+    const int MAXD = ND <= 5 ? 5 : ND <= 9 ? 9 : ND <= 17 ? 17 : 33;
+    const size_t smem = (size_t)BH * BW * sizeof(float2) + (size_t)MAXD * FPT_COLS * sizeof(float2) +
+                        (size_t)FPT_COLS * (KP + 1) * sizeof(float);
     auto k = ND <= 5 ? fi_prep_tc_kernel<5> : ND <= 9 ? fi_prep_tc_kernel<9> : ND <= 17 ? fi_prep_tc_kernel<17>
                                                                                         : fi_prep_tc_kernel<33>;
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    StageScope sc(ctx, LITHO_STAGE_FI_PREP);
-    k<<<dim3((g.Lx + FPT_THREADS - 1) / FPT_THREADS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
-        band_part, p.ngroups, g.Lx, g.Fx, g.Nx, g.Ny, KP, tmh, tml);
+    StageScope sc(ctx, LITHO_STAGE_FI_PREP, 2);
+    band_reduce_kernel<<<dim3((BH * BW + 127) / 128, p.batch), 128, 0, ctx->stream>>>(band_part, p.ngroups, BH * BW,
+                                                                                       S);
+    k<<<dim3((g.Lx + FPT_COLS - 1) / FPT_COLS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
+        S, reinterpret_cast<const float2*>(twf), g.Lx, g.Nx, g.Ny, KP, tmh, tml);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   switch (KBLK) {
