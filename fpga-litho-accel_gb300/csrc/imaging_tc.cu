@@ -4,29 +4,34 @@
 // FP32 on the CUDA cores.
 //
 // Split products.  Every operand X is written as X = Xh + Xl with
-// Xh = round_tf32(X) and Xl = X - Xh (exact in FP32); each contraction issues
-// Ah*Bh + Ah*Bl + Al*Bh, all accumulated into one TMEM accumulator.  The
+// Xh = round_tf32(X) and Xl = X - Xh (exact in FP32); each contraction computes
+// Ah*Bh + Ah*Bl + Al*Bh.  The hi and lo tiles of B sit back to back in shared
+// memory, so Ah*[Bh; Bl] is ONE MMA of twice the width (the mask or Cy tile is
+// read once for both products) and the epilogue adds the two column halves.  The
 // dropped Al*Bl term and the TF32 rounding of Xl leave a relative error of about
 // 2^-22 per product.
 //
-// Both kernels are warp-specialised and synchronised only by mbarriers, so TMA
-// traffic, tensor-core work and CUDA-core work overlap (warp 4: TMA producer,
-// warp 5: MMA issuer, warps 0-3: compute; they own TMEM lanes 0-127).
+// Both kernels are persistent (one CTA per SM), warp-specialised and synchronised
+// only by mbarriers, so TMA traffic, tensor-core work and CUDA-core work overlap.
 //
 // win_dft_tc_kernel   D[y][j] = sum_x mask[y][x] * T[x][j]  (M = 128 mask rows
-//                     per tile, N = 2Nx+1 column twiddles padded to NB, K = the
-//                     tile's columns).  Persistent (one CTA per SM, 320 threads):
-//                     TMA streams 128 x 32 mask tiles (SWIZZLE_128B) through a
-//                     6-8 stage ring; warps 0-3 split each landed tile in place;
-//                     the accumulator is double-buffered in TMEM and warps 6-9
-//                     run each tile's row-DFT epilogue while the next tile streams.
-// fi_tc_kernel        image[Y][X] = sum_r Cy[Y][r] * Tm[r][X]  (M = 128 image
-//                     rows, N = BN columns per tile, K = 4Ny+1 padded to 32*KBLK).
-//                     Persistent over the X tiles of one row band: A (the Cy
-//                     table) is loaded once, B (Tm^T) and the TMEM accumulator are
-//                     double-buffered, and the epilogue drains each accumulator
-//                     through two swizzled staging tiles with TMA bulk stores
-//                     (the image is written exactly once).
+//                     per tile, N = 2 NB (hi | lo) for the 2Nx+1 column twiddles
+//                     padded to NB, K = the tile's columns).  448 threads: TMA
+//                     streams 128 x 32 mask tiles (SWIZZLE_128B) through a 6-8
+//                     stage ring; warps 0-7 check each landed tile for TF32
+//                     exactness and split it in place only when it has a
+//                     residual; the accumulator is double-buffered in TMEM and
+//                     warps 10-13 run each tile's row-DFT epilogue while the next
+//                     tile streams.
+// fi_tc_kernel        image[Y][X] = T0[X] + sum_r Cy[Y][r] * Tm[r][X]  (M = 128
+//                     image rows, N = 2 BN per tile, K = 4Ny rows padded to
+//                     32*KBLK; the DC row T0 is added in FP32 by the epilogue).
+//                     320 threads over output tiles ordered (row band, image,
+//                     column tile): Cy is reloaded only when a CTA's range crosses
+//                     a row band, Tm tiles stream through a TMA ring, and two
+//                     epilogue groups drain the double-buffered accumulator
+//                     through swizzled staging tiles with TMA bulk stores (the
+//                     image is written exactly once).
 #include "litho_internal.cuh"
 #include "tc_common.cuh"
 
@@ -75,22 +80,23 @@ __global__ void ytab_init_kernel(float2* __restrict__ yt, int Ly, int Fy) {
   yt[(size_t)v * Ly + y] = make_float2(cs, -sn);
 }
 
-// CyT[Y][r] (KP columns): r = 0 -> 1; 1..2Ny -> 2cos(2 pi r y'/Fy); 2Ny+1..4Ny -> -2sin; else 0
+// CyT[Y][r] (KP columns): r < 2Ny -> 2cos(2 pi (r+1) y'/Fy); 2Ny <= r < 4Ny ->
+// -2sin(2 pi (r-2Ny+1) y'/Fy); else 0.  The fy = 0 (DC) row is not a column: the
+// FI epilogue adds T0[X] in FP32, so 4Ny rows fill the K blocks exactly when Ny is
+// a multiple of 8.
 __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, int Ly, int Fy, int Ny, int KP) {
   const int Y = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
   if (Y >= Ly || r >= KP) return;
   const long long yp = (long long)Y + (Fy - Ly) / 2 - Fy / 2;
   double v = 0.0;
-  if (r == 0) {
-    v = 1.0;
-  } else if (r <= 4 * Ny) {
-    const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
+  if (r < 4 * Ny) {
+    const int dy = r < 2 * Ny ? r + 1 : r - 2 * Ny + 1;
     long long m = ((long long)dy * yp) % Fy;
     if (m < 0) m += Fy;
     double s, c;
     sincospi(2.0 * (double)m / (double)Fy, &s, &c);
-    v = r <= 2 * Ny ? 2.0 * c : -2.0 * s;
+    v = r < 2 * Ny ? 2.0 * c : -2.0 * s;
   }
   const float h = tf32_round((float)v);
   hi[(size_t)Y * KP + r] = h;
@@ -100,7 +106,6 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // ---------------------------------------------------------------------------
 // window DFT on the tensor cores
 // ---------------------------------------------------------------------------
-constexpr int TC_THREADS = 192;
 
 // Persistent window DFT: one CTA per SM streams its tiles (image, 128-row block,
 // column range) through one TMA ring; the TMEM accumulator is double-buffered so
@@ -115,7 +120,8 @@ constexpr int TC_THREADS = 192;
 //   consumers : wait full[s]; vote residual (nzflag); if any: Ah = round_tf32(A) in
 //               place; arrive ready[s]; if residual: wait hidone[s], write Al,
 //               arrive ready2[s]
-//   MMA lane  : [tile start: wait accempty[buf]]; wait ready[s]; Ah*Bh + Ah*Bl;
+//   MMA lane  : [tile start: wait accempty[buf]]; wait ready[s]; Ah*[Bh; Bl] as one
+//               N = 2 NB MMA per K step (the epilogue adds the two column halves);
 //               if residual: commit hidone[s], wait ready2[s], Al*Bh; commit empty[s];
 //               [tile end: commit accfull[buf]]
 //   epilogue  : wait accfull[buf]; TMEM -> sR; arrive accempty[buf]; row DFT with
@@ -127,7 +133,10 @@ struct WinTC {
   static constexpr uint32_t A_B = 128 * 128;       // 128 rows x 32 fp32 (split in place: hi, then lo)
   static constexpr uint32_t B_B = NB * 128;        // NB rows x 32 fp32
   static constexpr uint32_t STAGE_B = A_B + 2 * B_B;
-  static constexpr uint32_t NCOL = NB <= 32 ? 32 : 64;  // columns of one accumulator
+  // one accumulator holds A*Bh in columns [0, NB) and A*Bl in [NB, 2 NB): the hi and
+  // lo twiddle tiles sit back to back in shared memory, so one N = 2 NB MMA reads
+  // the mask tile once for both products
+  static constexpr uint32_t NCOL = NB == 16 ? 32 : (NB == 32 ? 64 : 128);
   static constexpr uint32_t EPI_B = NB * 129 * 4 + 17 * 129 * 8;  // sR [NB][129] + sRT [Ny+1 <= 17][129]
   static constexpr int FIT = (int)((220u * 1024u - EPI_B - 2048u) / STAGE_B);
   static constexpr int STAGES = FIT > 8 ? 8 : FIT;
@@ -138,8 +147,7 @@ constexpr int WP_CONS = 256;     // consumer threads
 
 template <int NB>
 __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
-                                                                   const __grid_constant__ CUtensorMap tmBh,
-                                                                   const __grid_constant__ CUtensorMap tmBl,
+                                                                   const __grid_constant__ CUtensorMap tmB,
                                                                    int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
                                                                    int rows, int batch, int ncs,
                                                                    const float2* __restrict__ ytab,
@@ -193,8 +201,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   const uint32_t tmem = *tslot;
 
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
-  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };
-  auto sBl = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B + P::B_B; };
+  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };  // [Bh; Bl], 2 NB rows
   // tile t -> (image, row block, column split) and its chunk range
   auto decode = [&](int t, int& img, int& rb, int& cs, int& c0, int& c1) {
     img = t / (rows * ncs);
@@ -221,15 +228,15 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           }
           mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
           tma_load_3d(sA(s), &tmM, &full[s], 32 * c, 128 * rb, img);
-          tma_load_2d(sBh(s), &tmBh, &full[s], 32 * c, 0);
-          tma_load_2d(sBl(s), &tmBl, &full[s], 32 * c, 0);
+          tma_load_2d(sBh(s), &tmB, &full[s], 32 * c, 0);
           last_issued[s] = q;
         }
       }
     }
   } else if (warp == 9) {
     if (lane == 0) {  // MMA issuer
-      constexpr uint32_t IDESC = idesc_tf32(128, NB);
+      constexpr uint32_t IDESC2 = idesc_tf32(128, 2 * NB);  // A x [Bh; Bl]
+      constexpr uint32_t IDESC1 = idesc_tf32(128, NB);      // Al x Bh
       uint32_t ph2 = 0;  // per-stage parity of hidone / ready2
       int q = 0, tl = 0;
       bool ok = true;
@@ -253,12 +260,11 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           tc_fence_after();
           const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
           nzflag[s] = 0;  // every consumer read it before arriving on ready[s]
-          const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s)), dbl = desc_sw128(sBl(s));
+          const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s));
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint32_t off = kk * 32;
-            mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC, (c != c0 || kk != 0) ? 1u : 0u);
-            mma_tf32(acc, desc_add(da, off), desc_add(dbl, off), IDESC, 1u);
+            mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC2, (c != c0 || kk != 0) ? 1u : 0u);
           }
           if (two) {
             mma_commit(&hidone[s]);
@@ -272,7 +278,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
               const uint32_t off = kk * 32;
-              mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC, 1u);
+              mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC1, 1u);
             }
           }
           mma_commit(&empty[s]);
@@ -284,17 +290,15 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   } else if (warp < 8) {  // warps 0-7: check / split the landed tiles in place
     uint32_t ph2 = 0;
     int q = 0;
-    bool ok = true;
-    for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+    // a wait that gives up flags the error and the thread carries on through the
+    // named barriers with the others (later waits return at once): a thread that
+    // left alone would strand the rest at the next barrier
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
       int img, rb, cs, c0, c1;
       decode(t, img, rb, cs, c0, c1);
       for (int c = c0; c < c1; ++c, ++q) {
         const int s = q % S;
-        if (!mbar_wait_ab(&full[s], (uint32_t)(q / S) & 1u, abort)) {
-          *abort = 1;
-          ok = false;
-          break;
-        }
+        if (!mbar_wait_ab(&full[s], (uint32_t)(q / S) & 1u, abort)) *abort = 1;
         float4* a = reinterpret_cast<float4*>(sA(s));
         float4 v[4];
         bool nz = false;
@@ -316,11 +320,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         }
         mbar_arrive(&ready[s]);  // release: Ah visible to the MMA lane
         if (two) {
-          if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) {
-            *abort = 1;
-            ok = false;
-            break;
-          }
+          if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) *abort = 1;
           ph2 ^= 1u << s;
 #pragma unroll
           for (int i = 0; i < 4; ++i)
@@ -341,23 +341,31 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       int img, rb, cs, c0, c1;
       decode(t, img, rb, cs, c0, c1);
       const int buf = tl & 1;
-      if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) {
-        *abort = 1;
-        break;
-      }
+      // on a wait that gives up: flag it and carry on with the group (see above)
+      if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) *abort = 1;
       tc_fence_after();
       const uint32_t trow = tmem + (uint32_t)buf * P::NCOL + ((uint32_t)(32 * quarter) << 16);
-      if (NB >= 32) {
+      // sR[j] = (A Bh)[j] + (A Bl)[j]
+      if (NB == 16) {
         float v[32];
         tmem_ld32(trow, v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sR[j * RS + row] = v[j];
-      }
-      if (NB == 16 || NB == 48) {
-        float v[16];
-        tmem_ld16(trow + (NB == 48 ? 32u : 0u), v);
+        for (int j = 0; j < 16; ++j) sR[j * RS + row] = v[j] + v[16 + j];
+      } else if (NB == 32) {
+        float h[32], l[32];
+        tmem_ld32(trow, h);
+        tmem_ld32(trow + 32u, l);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) sR[(j + (NB == 48 ? 32 : 0)) * RS + row] = v[j];
+        for (int j = 0; j < 32; ++j) sR[j * RS + row] = h[j] + l[j];
+      } else {  // NB = 48: three 16-column groups of each half
+#pragma unroll
+        for (int g = 0; g < 3; ++g) {
+          float h[16], l[16];
+          tmem_ld16(trow + 16u * g, h);
+          tmem_ld16(trow + 48u + 16u * g, l);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) sR[(16 * g + j) * RS + row] = h[j] + l[j];
+        }
       }
       tc_fence_before();
       mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
@@ -447,7 +455,8 @@ __global__ void twF_init_kernel(float2* __restrict__ tw, int Lx, int Fx, int ND)
 template <int MAXD>
 __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ Sg, const float2* __restrict__ twF,
                                                                  int Lx, int Nx, int Ny, int KP,
-                                                                 float* __restrict__ tmh, float* __restrict__ tml) {
+                                                                 float* __restrict__ tmh, float* __restrict__ tml,
+                                                                 float* __restrict__ t0) {
   extern __shared__ __align__(16) float2 fps[];
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
   float2* sS = fps;                                             // [BH][BW]
@@ -478,10 +487,10 @@ __global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* _
       }
     }
     if (fy == 0) {
-      o[0] = re;
+      if (X0 + c < Lx) t0[(size_t)img * Lx + X0 + c] = re;  // the DC row, added by the FI epilogue
     } else {
-      o[fy] = re;
-      o[2 * Ny + fy] = im;
+      o[fy - 1] = re;
+      o[2 * Ny + fy - 1] = im;
     }
   }
   __syncthreads();
@@ -507,49 +516,81 @@ struct FiTC {
   static constexpr uint32_t B_KB = BN * 128;      // BN rows x 32 fp32
   static constexpr uint32_t A_BYTES = 2 * KBLK * A_KB;
   static constexpr uint32_t B_BYTES = 2 * KBLK * B_KB;
+  static constexpr int NS = KBLK == 1 ? 3 : 2;    // B stages
+  static constexpr int NOUT = KBLK == 1 ? 2 : 1;  // staging tiles per epilogue group
   static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
-  static constexpr size_t SMEM = 1024 + A_BYTES + 2 * (size_t)B_BYTES + 2 * OUT_B + 256;
+  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
+constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
 
+// Persistent FI contraction: one CTA per SM takes a contiguous range of output
+// tiles ordered (row band, image, column tile), so the Cy operand (A, the row
+// band's twiddles) is reloaded only when the range crosses a row band.  Tm tiles
+// (B) stream through an NS-stage TMA ring; the two TMEM accumulators alternate
+// between tiles.  Roles (320 threads):
+//   warp 8   : TMA producer  [band change: wait emptyA] A -> fullA;
+//              [wait emptyB[s]] B -> fullB[s]
+//   warp 9   : MMA issuer    [band change: wait fullA]; wait fullB[s], accEmpty[b];
+//              Ah x [Bh; Bl] (N = 2 BN) + Al x Bh; commit emptyB[s], accFull[b];
+//              [last tile of a band: commit emptyA]
+//   warps 0-7: epilogue in two groups of four warps (one warp per TMEM lane
+//              quarter each); group g drains the 32-column slabs g, g + 2, ...:
+//              hi + lo halves + T0[X] -> swizzled staging -> TMA store, then both
+//              groups arrive on accEmpty[b].
+// The epilogue is latency-bound per slab (TMEM load, barriers, staging), so two
+// groups with their own staging tiles and barriers keep twice the slabs in flight.
 template <int KBLK, int BN>
-__global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
+__global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
                                                               const __grid_constant__ CUtensorMap tmCl,
                                                               const __grid_constant__ CUtensorMap tmTh,
                                                               const __grid_constant__ CUtensorMap tmTl,
                                                               const __grid_constant__ CUtensorMap tmOut, int Lx,
-                                                              int* __restrict__ err) {
+                                                              int batch, int ntile, int ntiles,
+                                                              const float* __restrict__ t0g, int* __restrict__ err) {
   using P = FiTC<KBLK, BN>;
+  constexpr int NS = P::NS, NOUT = P::NOUT;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   unsigned char* sAh = sm;
   unsigned char* sAl = sm + KBLK * P::A_KB;
-  unsigned char* sB = sm + P::A_BYTES;               // [2][hi kb..., lo kb...]
-  unsigned char* sOut = sB + 2 * P::B_BYTES;         // [2][OUT_B]
-  uint64_t* fullA = reinterpret_cast<uint64_t*>(sOut + 2 * P::OUT_B);
-  uint64_t* fullB = fullA + 1;     // [2]
-  uint64_t* emptyB = fullA + 3;    // [2]
-  uint64_t* accFull = fullA + 5;   // [2]
-  uint64_t* accEmpty = fullA + 7;  // [2]
-  uint64_t* drain = fullA + 9;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(fullA + 10);
+  unsigned char* sB = sm + P::A_BYTES;               // [NS][kb][hi, lo]
+  unsigned char* sOut = sB + NS * P::B_BYTES;        // [2 groups][NOUT][OUT_B]
+  float* sT0 = reinterpret_cast<float*>(sOut + 2 * NOUT * P::OUT_B);  // [2 groups][BN]: the tile's DC row
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(sT0 + 2 * BN);
+  uint64_t* emptyA = fullA + 1;
+  uint64_t* fullB = fullA + 2;           // [NS]
+  uint64_t* emptyB = fullB + NS;         // [NS]
+  uint64_t* accFull = emptyB + NS;       // [2]
+  uint64_t* accEmpty = accFull + 2;      // [2]
+  uint64_t* drain = accEmpty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
-  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [2]
+  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [NS], then the last A generation
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int yb = blockIdx.x, img = blockIdx.y, y0 = yb * 128;
-  // X split: CTA blockIdx.z writes tiles [t0, t0 + ntile) of the row band
-  const int ntile_all = (Lx + BN - 1) / BN;
-  const int t0 = (int)((long long)ntile_all * blockIdx.z / gridDim.z);
-  const int ntile = (int)((long long)ntile_all * (blockIdx.z + 1) / gridDim.z) - t0;
+  const int i0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int i1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  // tile i -> (row band, image, column tile)
+  auto band_of = [&](int i) { return i / (batch * ntile); };
+  auto decode = [&](int i, int& yb, int& img, int& xt) {
+    yb = i / (batch * ntile);
+    const int r = i - yb * batch * ntile;
+    img = r / ntile;
+    xt = r - img * ntile;
+  };
 
-  if (warp == 0) tmem_alloc(tslot, 2 * BN);
+  if (warp == 0) tmem_alloc(tslot, 4 * BN);  // two accumulators of [A Bh | A Bl]
   if (tid == 0) {
     mbar_init(fullA, 1);
+    mbar_init(emptyA, 1);
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&fullB[s], 1);
+      mbar_init(&emptyB[s], 1);
+      last_issued[s] = -1;
+    }
+    last_issued[NS] = -1;
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&fullB[b], 1);
-      mbar_init(&emptyB[b], 1);
       mbar_init(&accFull[b], 1);
-      mbar_init(&accEmpty[b], 128);
-      last_issued[b] = -1;
+      mbar_init(&accEmpty[b], 256);
     }
     mbar_init(drain, 1);
     *abort = 0;
@@ -559,110 +600,165 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fi_tc_kernel(const __grid_const
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  auto Bh = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)kb * P::B_KB; };
-  auto Bl = [&](int b, int kb) { return sB + (size_t)b * P::B_BYTES + (size_t)(KBLK + kb) * P::B_KB; };
+  // the hi and lo tiles of one K block sit back to back, so Ah x [Bh; Bl] is one N = 2 BN MMA
+  auto Bh = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb) * P::B_KB; };
+  auto Bl = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb + 1) * P::B_KB; };
 
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {  // TMA producer
-      mbar_arrive_expect_tx(fullA, P::A_BYTES);
-      for (int kb = 0; kb < KBLK; ++kb) {
-        tma_load_2d(sAh + (size_t)kb * P::A_KB, &tmCh, fullA, 32 * kb, y0);
-        tma_load_2d(sAl + (size_t)kb * P::A_KB, &tmCl, fullA, 32 * kb, y0);
-      }
-      for (int t = 0; t < ntile; ++t) {
-        const int b = t & 1;
-        if (t >= 2 && !mbar_wait_ab(&emptyB[b], (uint32_t)((t - 2) >> 1) & 1u, abort)) {
+      int cur = -1, gen = 0;
+      for (int i = i0; i < i1; ++i) {
+        int yb, img, xt;
+        decode(i, yb, img, xt);
+        if (yb != cur) {  // (re)load the row band's Cy tiles once the MMAs on the previous ones are done
+          if (gen > 0 && !mbar_wait_ab(emptyA, (uint32_t)(gen - 1) & 1u, abort)) {
+            *abort = 1;
+            break;
+          }
+          mbar_arrive_expect_tx(fullA, P::A_BYTES);
+          for (int kb = 0; kb < KBLK; ++kb) {
+            tma_load_2d(sAh + (size_t)kb * P::A_KB, &tmCh, fullA, 32 * kb, 128 * yb);
+            tma_load_2d(sAl + (size_t)kb * P::A_KB, &tmCl, fullA, 32 * kb, 128 * yb);
+          }
+          last_issued[NS] = gen;
+          ++gen;
+          cur = yb;
+        }
+        const int q = i - i0, s = q % NS;
+        if (q >= NS && !mbar_wait_ab(&emptyB[s], (uint32_t)((q - NS) / NS) & 1u, abort)) {
           *abort = 1;
           break;
         }
-        mbar_arrive_expect_tx(&fullB[b], P::B_BYTES);
+        mbar_arrive_expect_tx(&fullB[s], P::B_BYTES);
         for (int kb = 0; kb < KBLK; ++kb) {
-          tma_load_3d(Bh(b, kb), &tmTh, &fullB[b], 32 * kb, (t0 + t) * BN, img);
-          tma_load_3d(Bl(b, kb), &tmTl, &fullB[b], 32 * kb, (t0 + t) * BN, img);
+          tma_load_3d(Bh(s, kb), &tmTh, &fullB[s], 32 * kb, xt * BN, img);
+          tma_load_3d(Bl(s, kb), &tmTl, &fullB[s], 32 * kb, xt * BN, img);
         }
-        last_issued[b] = t;
+        last_issued[s] = q;
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == 9) {
     if (lane == 0) {  // MMA issuer
-      constexpr uint32_t IDESC = idesc_tf32(128, BN);
-      bool ok = mbar_wait_ab(fullA, 0, abort);
-      for (int t = 0; ok && t < ntile; ++t) {
-        const int b = t & 1;
-        if (!mbar_wait_ab(&fullB[b], (uint32_t)(t >> 1) & 1u, abort) ||
-            (t >= 2 && !mbar_wait_ab(&accEmpty[b], (uint32_t)((t - 2) >> 1) & 1u, abort))) {
+      constexpr uint32_t IDESC2 = idesc_tf32(128, 2 * BN);  // Ah x [Bh; Bl]
+      constexpr uint32_t IDESC1 = idesc_tf32(128, BN);      // Al x Bh
+      int cur = -1, gen = 0;
+      bool ok = true;
+      for (int i = i0; ok && i < i1; ++i) {
+        const int q = i - i0, s = q % NS, b = q & 1;
+        const int yb = band_of(i);
+        if (yb != cur) {
+          if (!mbar_wait_ab(fullA, (uint32_t)gen & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          ++gen;
+          cur = yb;
+        }
+        if (!mbar_wait_ab(&fullB[s], (uint32_t)(q / NS) & 1u, abort) ||
+            (q >= 2 && !mbar_wait_ab(&accEmpty[b], (uint32_t)((q - 2) >> 1) & 1u, abort))) {
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t acc = tmem + (uint32_t)(b * BN);
+        const uint32_t acc = tmem + (uint32_t)(b * 2 * BN);
 #pragma unroll
         for (int kb = 0; kb < KBLK; ++kb) {
           const uint64_t dah = desc_sw128(sAh + (size_t)kb * P::A_KB), dal = desc_sw128(sAl + (size_t)kb * P::A_KB);
-          const uint64_t dbh = desc_sw128(Bh(b, kb)), dbl = desc_sw128(Bl(b, kb));
+          const uint64_t dbh = desc_sw128(Bh(s, kb));
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint32_t off = kk * 32;
-            mma_tf32(acc, desc_add(dah, off), desc_add(dbh, off), IDESC, (kb | kk) != 0 ? 1u : 0u);
-            mma_tf32(acc, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
-            mma_tf32(acc, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+            mma_tf32(acc, desc_add(dah, off), desc_add(dbh, off), IDESC2, (kb | kk) != 0 ? 1u : 0u);
+            mma_tf32(acc, desc_add(dal, off), desc_add(dbh, off), IDESC1, 1u);
           }
         }
-        mma_commit(&emptyB[b]);
+        mma_commit(&emptyB[s]);
         mma_commit(&accFull[b]);
+        if (i + 1 == i1 || band_of(i + 1) != yb) mma_commit(emptyA);  // the A tiles may be replaced
       }
       if (!ok) *abort = 1;
     }
-  } else {  // warps 0-3: epilogue
-    const int row = 32 * warp + lane;
+  } else {  // warps 0-7: epilogue, group grp = warp / 4
+    const int grp = warp >> 2, gtid = tid & 127, quarter = warp & 3;
+    const int row = 32 * quarter + lane;
+    const bool leader = gtid == 0;
+    float* t0s = sT0 + grp * BN;
+    unsigned char* stg = sOut + (size_t)grp * NOUT * P::OUT_B;
     int slab_count = 0;
-    for (int t = 0; t < ntile; ++t) {
-      const int b = t & 1;
-      if (!mbar_wait_ab(&accFull[b], (uint32_t)(t >> 1) & 1u, abort)) {
-        *abort = 1;
-        break;
-      }
+    // the DC row of the next tile is fetched one tile ahead (its latency hides behind a tile)
+    auto t0_of = [&](int i) {
+      int yb, img, xt;
+      decode(i, yb, img, xt);
+      const int X = xt * BN + gtid;
+      return X < Lx ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
+    };
+    float t0n = i0 < i1 ? t0_of(i0) : 0.f;
+    for (int i = i0; i < i1; ++i) {
+      const int q = i - i0, b = q & 1;
+      int yb, img, xt;
+      decode(i, yb, img, xt);
+      // every reader of the previous tile's DC row has passed its last slab's second barrier
+      t0s[gtid] = t0n;
+      if (i + 1 < i1) t0n = t0_of(i + 1);
+      // a wait that gives up flags the error and carries on with the rest of the
+      // group (later waits return at once): a thread that left the loop alone
+      // would strand the others at the next named barrier
+      if (!mbar_wait_ab(&accFull[b], (uint32_t)(q >> 1) & 1u, abort)) *abort = 1;
       tc_fence_after();
-      const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * BN);
+      const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * 2 * BN);
 #pragma unroll 1
-      for (int slab = 0; slab < BN / 32; ++slab, ++slab_count) {
-        float v[32];
-        tmem_ld32(trow + (uint32_t)(slab * 32), v);
-        unsigned char* st = sOut + (size_t)(slab_count & 1) * P::OUT_B;
-        if (tid == 0) bulk_wait_read1();  // the store that used this staging tile has read it
-        named_bar(1, 128);
+      for (int slab = grp; slab < BN / 32; slab += 2, ++slab_count) {
+        uint32_t v[32], w[32];
+        tmem_ld32_async(trow + (uint32_t)(slab * 32), v);
+        tmem_ld32_async(trow + (uint32_t)(BN + slab * 32), w);
+        tmem_ld_wait();
+        unsigned char* st = stg + (size_t)(slab_count % NOUT) * P::OUT_B;
+        if (leader) {  // the store that used this staging tile has read it
+          if (NOUT == 2) bulk_wait_read1();
+          else bulk_wait_read0();
+        }
+        named_bar(1 + grp, 128);  // ... and t0s holds this tile's DC row
+        const float4* t04 = reinterpret_cast<const float4*>(t0s + slab * 32);
+        float4 d[8];
+#pragma unroll
+        for (int q4 = 0; q4 < 8; ++q4) d[q4] = t04[q4];
         float4* rowp = reinterpret_cast<float4*>(st + (size_t)row * 128);
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          rowp[q ^ (row & 7)] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        for (int q4 = 0; q4 < 8; ++q4) {
+          const int j = 4 * q4;
+          rowp[q4 ^ (row & 7)] = make_float4(__uint_as_float(v[j]) + (__uint_as_float(w[j]) + d[q4].x),
+                                             __uint_as_float(v[j + 1]) + (__uint_as_float(w[j + 1]) + d[q4].y),
+                                             __uint_as_float(v[j + 2]) + (__uint_as_float(w[j + 2]) + d[q4].z),
+                                             __uint_as_float(v[j + 3]) + (__uint_as_float(w[j + 3]) + d[q4].w));
+        }
         fence_proxy_async();
-        named_bar(1, 128);
-        if (tid == 0) {
-          tma_store_3d(&tmOut, st, (t0 + t) * BN + slab * 32, y0, img);
+        named_bar(1 + grp, 128);
+        if (leader) {
+          tma_store_3d(&tmOut, st, xt * BN + slab * 32, 128 * yb, img);
           bulk_commit();
         }
       }
       tc_fence_before();
       mbar_arrive(&accEmpty[b]);
     }
-    if (tid == 0) bulk_wait0();
+    if (leader) bulk_wait0();
   }
   __syncthreads();
   if (*abort) {
-    if (tid == 160) {
+    if (tid == 288) {  // the MMA lane: drain what it issued
       mma_commit(drain);
       mbar_wait(drain, 0, 200u);
     }
-    if (tid == 128) {
-      mbar_wait(fullA, 0, 200u);
-      for (int b = 0; b < 2; ++b)
-        if (last_issued[b] >= 0) mbar_wait(&fullB[b], (uint32_t)(last_issued[b] >> 1) & 1u, 200u);
+    if (tid == 256) {  // the producer: wait for its last loads
+      if (last_issued[NS] >= 0) mbar_wait(fullA, (uint32_t)last_issued[NS] & 1u, 200u);
+      for (int s = 0; s < NS; ++s)
+        if (last_issued[s] >= 0) mbar_wait(&fullB[s], (uint32_t)(last_issued[s] / NS) & 1u, 200u);
     }
     if (tid == 0) atomicExch(err, 1);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 2 * BN);
+  if (warp == 0) tmem_dealloc(tmem, 4 * BN);
 }
 
 // ---------------------------------------------------------------------------
@@ -707,10 +803,10 @@ static int nb_for(int Nx) {
   const int nj = 2 * Nx + 1;
   return nj <= 16 ? 16 : (nj <= 32 ? 32 : (nj <= 48 ? 48 : -1));
 }
-static int kblk_for(int Ny) { return (4 * Ny + 1 + 31) / 32; }
+static int kblk_for(int Ny) { return std::max(1, (4 * Ny + 31) / 32); }  // 4Ny K rows (the DC row is separate)
 
 bool tc_supported(const ImgGeom& g) {
-  return (g.Lx % 4) == 0 && g.Nx <= 16 && g.Ny <= 16 && nb_for(g.Nx) > 0 && kblk_for(g.Ny) <= 3;
+  return (g.Lx % 4) == 0 && g.Nx <= 16 && g.Ny <= 16 && nb_for(g.Nx) > 0 && kblk_for(g.Ny) <= 2;
 }
 
 static int tc_err_flag(litho_ctx* ctx, int** flag) {
@@ -776,10 +872,9 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
         reinterpret_cast<float2*>(yt), g.Ly, g.Fy);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  CUtensorMap mM, mBh, mBl;
+  CUtensorMap mM, mB;
   LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
-  LITHO_RET(make_map(ctx, &mBh, twh, 2, g.Lx, NB, 1, NB));
-  LITHO_RET(make_map(ctx, &mBl, twl, 2, g.Lx, NB, 1, NB));
+  LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NB, 1, 2 * NB));  // hi rows, then lo rows
   const size_t smem = WinTC<NB>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
@@ -787,7 +882,7 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   const int tiles = rows * p.batch * ncs;
   const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
-  win_dft_tc_kernel<NB><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mBh, mBl, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
+  win_dft_tc_kernel<NB><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
                                                                  rows, p.batch, ncs,
                                                                  reinterpret_cast<const float2*>(yt), win_part,
                                                                  p.part_stride, err);
@@ -810,7 +905,7 @@ int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2*
 
 template <int KBLK, int BN>
 static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, const float* cyl, const float* tmh,
-                        const float* tml, float* images, int* err) {
+                        const float* tml, const float* t0, float* images, int* err) {
   const ImgGeom& g = p.g;
   const int KP = 32 * KBLK;
   CUtensorMap mCh, mCl, mTh, mTl, mO;
@@ -822,22 +917,22 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   const size_t smem = FiTC<KBLK, BN>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  // split the X tiles of a row block only when the row blocks alone leave SMs idle
+  // persistent: one CTA per SM over all (row band, image, column tile) tiles
   const int ntile = (g.Lx + BN - 1) / BN, rows = (g.Ly + 127) / 128;
-  const int units = rows * p.batch;
-  int xs = units < ctx->sm_count ? (2 * ctx->sm_count + units - 1) / units : 1;
-  xs = std::max(1, std::min(xs, ntile / 2));
-  dim3 grid(rows, p.batch, xs);
+  const int ntiles = rows * p.batch * ntile;
+  const int grid = std::min(ntiles, ctx->sm_count);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);
-  fi_tc_kernel<KBLK, BN><<<grid, TC_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, err);
+  fi_tc_kernel<KBLK, BN><<<grid, FI_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, p.batch, ntile,
+                                                                  ntiles, t0, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
 
-// hi/lo T rows [2][batch][Lx][KP] float, then the reduced band [batch][2Ny+1][4Nx+1] float2
+// hi/lo T rows [2][batch][Lx][KP] float, the reduced band [batch][2Ny+1][4Nx+1]
+// float2, then the DC row T0 [batch][Lx] float
 size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch) {
   return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float) +
-         (size_t)batch * (2 * g.Ny + 1) * (4 * g.Nx + 1) * sizeof(float2);
+         (size_t)batch * (2 * g.Ny + 1) * (4 * g.Nx + 1) * sizeof(float2) + (size_t)batch * g.Lx * sizeof(float);
 }
 
 // tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
@@ -867,6 +962,7 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     tmh = ctx->mx_b.as<float>();
   }
   float* tml = tmh + (size_t)p.batch * g.Lx * KP;
+  float* t0 = nullptr;
   {
     const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
     // column twiddles, cached per (Lx, Fx, Nx)
@@ -879,7 +975,8 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
                                                                              g.Fx, ND);
       LITHO_CUDA_TRY(ctx, cudaGetLastError());
     }
-    float2* S = reinterpret_cast<float2*>(tml + (size_t)p.batch * g.Lx * KP);  // tail of the workspace
+    float2* S = reinterpret_cast<float2*>(tml + (size_t)p.batch * g.Lx * KP);  // after the T rows
+    t0 = reinterpret_cast<float*>(S + (size_t)p.batch * BH * BW);
     const int MAXD = ND <= 5 ? 5 : ND <= 9 ? 9 : ND <= 17 ? 17 : 33;
     const size_t smem = (size_t)BH * BW * sizeof(float2) + (size_t)MAXD * FPT_COLS * sizeof(float2) +
                         (size_t)FPT_COLS * (KP + 1) * sizeof(float);
@@ -890,14 +987,11 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     band_reduce_kernel<<<dim3((BH * BW + 127) / 128, p.batch), 128, 0, ctx->stream>>>(band_part, p.ngroups, BH * BW,
                                                                                        S);
     k<<<dim3((g.Lx + FPT_COLS - 1) / FPT_COLS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
-        S, reinterpret_cast<const float2*>(twf), g.Lx, g.Nx, g.Ny, KP, tmh, tml);
+        S, reinterpret_cast<const float2*>(twf), g.Lx, g.Nx, g.Ny, KP, tmh, tml, t0);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  switch (KBLK) {
-    case 1: return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);
-    case 2: return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, images, err);
-    default: return launch_fi_tc<3, 64>(ctx, p, cyh, cyl, tmh, tml, images, err);
-  }
+  if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
+  return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
 }
 
 }  // namespace litho
