@@ -18,7 +18,7 @@
 //                    (warp-shuffle radix-2, fft_warp.cuh), accumulate s_k|E|^2 in
 //                    registers; then a forward FFT of the intensity and the
 //                    |f| <= 2N band S[fy][fx] / N^2 is written out.
-//   fi_prep_kernel : T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx}   (fy >= 0)
+//   fi_rows_kernel : T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx}   (fy >= 0)
 //   fi_out_kernel  : image[Y][X] = T0 + 2 sum_{fy>0} Re(e^{2 pi i fy y'/Fy} T[fy][X]),
 //                    a rank-(4Ny+1) FP32 contraction written once with 16-byte
 //                    streaming stores.  HBM: one write of the image.
@@ -27,6 +27,7 @@
 // crop2DCentered (litho.cpp:164-177, 997-1001).
 #include "litho_internal.cuh"
 #include "fft_warp.cuh"
+#include "tc_common.cuh"
 
 #include <algorithm>
 
@@ -381,45 +382,157 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// FI, step 1: T[fy][X] for fy = 0..2Ny (T[-fy] = conj(T[fy]) because the
-// intensity is real).  tm layout per image: row 0 = Re T0, rows 1..2Ny = Re T,
-// rows 2Ny+1..4Ny = Im T; Lx columns.
+// FI, step 1: T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx} for fy = 0..2Ny
+// (T[-fy] = conj(T[fy]) because the intensity is real).  One thread per image
+// column X and half of the fy rows; the column twiddles live in registers and
+// the band, summed over its kernel-group partials in a fixed order, sits in
+// shared memory pre-combined as C[fy][d] = (Re(p+q), Im(p-q), Im(p+q), Re(p-q))
+// for p = S[fy][d], q = S[fy][-d], so that
+//   T = S0 + sum_{d>0} (p t + q conj(t)),  t = e^{+2 pi i d x'/Fx},
+// costs one broadcast shared load and four FMAs per (fy, d).
+// Two output layouts:
+//   plain  tm[img][r][X]: r = 0 Re T0, 1..2Ny Re T, 2Ny+1..4Ny Im T (fi_out_kernel)
+//   K-major (tensor-core FI) t0[img][X] = Re T0 and hi/lo TF32 splits of
+//          tm[img][X][KP]: r = fy-1 Re T, 2Ny+fy-1 Im T, zero to KP
 // ---------------------------------------------------------------------------
-constexpr int FIP_THREADS = 256;
+constexpr int FR_THREADS = 256, FR_COLS = 128;
 
-__global__ void __launch_bounds__(FIP_THREADS) fi_prep_kernel(const float2* __restrict__ band_part, int ngroups,
-                                                              int Lx, int Fx, int Nx, int Ny,
-                                                              float* __restrict__ tm) {
-  extern __shared__ __align__(16) float2 fs[];
+template <int MAXD, bool KMAJ>
+__global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __restrict__ band_part, int ngroups,
+                                                             const float2* __restrict__ twF, int Lx, int Fx,
+                                                             int Nx, int Ny, int KP, float* __restrict__ tm,
+                                                             float* __restrict__ tmh, float* __restrict__ tml,
+                                                             float* __restrict__ t0) {
+  extern __shared__ __align__(16) float4 frs[];
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
-  float2* sS = fs;                 // [BH][BW]
-  float2* sT = fs + BH * BW;       // [ND][FIP_THREADS]
-  const int tid = threadIdx.x, img = blockIdx.y;
+  float4* sC = frs;                                       // [BH][MAXD]
+  float* sO = reinterpret_cast<float*>(sC + BH * MAXD);  // K-major: [FR_COLS][KP + 1]
+  const int tid = threadIdx.x, img = blockIdx.y, X0 = blockIdx.x * FR_COLS;
+  const int xl = tid & (FR_COLS - 1), grp = tid / FR_COLS;
   const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-  for (int idx = tid; idx < BH * BW; idx += FIP_THREADS) sS[idx] = sum_strided(B + idx, (size_t)BH * BW, ngroups);
-  const int X = blockIdx.x * FIP_THREADS + tid;
-  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
-  for (int d = 0; d < ND; ++d) sT[d * FIP_THREADS + tid] = cis_exact((long long)d * xp, Fx, 1.f);
-  __syncthreads();
-  if (X >= Lx) return;
-  float* out = tm + (size_t)img * (4 * Ny + 1) * Lx;
-  for (int fy = 0; fy < BH; ++fy) {
-    const float2* S = sS + fy * BW + 2 * Nx;
-    float re = S[0].x, im = S[0].y;
-    for (int d = 1; d < ND; ++d) {
-      const float2 t = sT[d * FIP_THREADS + tid];
-      const float2 p = S[d], q = S[-d];
-      // p * t + q * conj(t)
-      re += (p.x + q.x) * t.x - (p.y - q.y) * t.y;
-      im += (p.y + q.y) * t.x + (p.x - q.x) * t.y;
+  const size_t pst = (size_t)BH * BW;
+  for (int idx = tid; idx < BH * ND; idx += FR_THREADS) {
+    const int fy = idx / ND, d = idx - fy * ND;
+    const float2* S = B + fy * BW + 2 * Nx;
+    const float2 pv = sum_strided(S + d, pst, ngroups);
+    if (d == 0) {
+      sC[fy * MAXD] = make_float4(pv.x, pv.y, 0.f, 0.f);
+    } else {
+      const float2 qv = sum_strided(S - d, pst, ngroups);
+      sC[fy * MAXD + d] = make_float4(pv.x + qv.x, pv.y - qv.y, pv.y + qv.y, pv.x - qv.x);
     }
-    if (fy == 0) {
+  }
+  if (KMAJ)
+    for (int idx = tid; idx < FR_COLS * (KP - 4 * Ny); idx += FR_THREADS) {
+      const int c = idx / (KP - 4 * Ny), r = 4 * Ny + idx % (KP - 4 * Ny);
+      sO[c * (KP + 1) + r] = 0.f;
+    }
+  const int X = X0 + xl;
+  const bool live = X < Lx;
+  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
+  float2 tw[MAXD];
+#pragma unroll
+  for (int d = 1; d < MAXD; ++d)
+    tw[d] = (d < ND && live) ? (twF != nullptr ? twF[(size_t)d * Lx + X] : cis_exact((long long)d * xp, Fx, 1.f))
+                             : make_float2(0.f, 0.f);
+  __syncthreads();
+  const int fy0 = grp == 0 ? 0 : Ny + 1, fy1 = grp == 0 ? Ny + 1 : BH;
+  float* out = KMAJ ? nullptr : tm + (size_t)img * (4 * Ny + 1) * Lx;
+  for (int fy = fy0; fy < fy1; ++fy) {
+    const float4* C = sC + fy * MAXD;
+    float re = C[0].x, im = C[0].y;
+#pragma unroll
+    for (int d = 1; d < MAXD; ++d) {
+      if (d < ND) {
+        const float4 a = C[d];
+        re = fmaf(a.x, tw[d].x, re);
+        re = fmaf(-a.y, tw[d].y, re);
+        im = fmaf(a.z, tw[d].x, im);
+        im = fmaf(a.w, tw[d].y, im);
+      }
+    }
+    if (!live) continue;
+    if (KMAJ) {
+      if (fy == 0) {
+        t0[(size_t)img * Lx + X] = re;
+      } else {
+        sO[xl * (KP + 1) + fy - 1] = re;
+        sO[xl * (KP + 1) + 2 * Ny + fy - 1] = im;
+      }
+    } else if (fy == 0) {
       out[X] = re;
     } else {
       out[(size_t)fy * Lx + X] = re;
       out[(size_t)(2 * Ny + fy) * Lx + X] = im;
     }
   }
+  if (KMAJ) {
+    __syncthreads();
+    // rows X0 .. X0 + ncol - 1 of [X][KP] are one contiguous run: float4 stores
+    const int ncol = min(FR_COLS, Lx - X0);
+    const size_t base = ((size_t)img * Lx + X0) * KP;
+    for (int e = tid; e < ncol * KP / 4; e += FR_THREADS) {
+      const int xr = (4 * e) / KP, r = 4 * e - xr * KP;
+      const float* v = sO + xr * (KP + 1) + r;
+      const float h0 = tc::tf32_round(v[0]), h1 = tc::tf32_round(v[1]), h2 = tc::tf32_round(v[2]),
+                  h3 = tc::tf32_round(v[3]);
+      reinterpret_cast<float4*>(tmh + base)[e] = make_float4(h0, h1, h2, h3);
+      reinterpret_cast<float4*>(tml + base)[e] = make_float4(v[0] - h0, v[1] - h1, v[2] - h2, v[3] - h3);
+    }
+  }
+}
+
+template <int MAXD, bool KMAJ>
+static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const float2* band_part, const float2* twF,
+                                    int KP, float* tm, float* tmh, float* tml, float* t0) {
+  const ImgGeom& g = p.g;
+  const size_t smem = (size_t)(2 * g.Ny + 1) * MAXD * sizeof(float4) +
+                      (KMAJ ? (size_t)FR_COLS * (KP + 1) * sizeof(float) : 0);
+  auto k = fi_rows_kernel<MAXD, KMAJ>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<dim3((g.Lx + FR_COLS - 1) / FR_COLS, p.batch), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx,
+                                                                          g.Nx, g.Ny, KP, tm, tmh, tml, t0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fi_rows(cudaStream_t s, const ImgPlan& p, const float2* band_part, const float2* twF, int KP,
+                           float* tm, float* tmh, float* tml, float* t0) {
+  const int ND = 2 * p.g.Nx + 1;
+  const bool km = tmh != nullptr;
+  if (ND <= 5) return km ? launch_fi_rows_t<5, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
+                         : launch_fi_rows_t<5, false>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+  if (ND <= 9) return km ? launch_fi_rows_t<9, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
+                         : launch_fi_rows_t<9, false>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+  if (ND <= 17) return km ? launch_fi_rows_t<17, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
+                          : launch_fi_rows_t<17, false>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+  return km ? launch_fi_rows_t<33, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
+            : launch_fi_rows_t<33, false>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+}
+
+// twF[d][X] = e^{+2 pi i d x'/Fx}, d = 0..2Nx: the FI column twiddles
+__global__ void twF_init_kernel(float2* __restrict__ tw, int Lx, int Fx, int ND) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, d = blockIdx.y;
+  if (x >= Lx || d >= ND) return;
+  const long long xp = (long long)x + (Fx - Lx) / 2 - Fx / 2;
+  tw[(size_t)d * Lx + x] = cis_exact((long long)d * xp, Fx, 1.f);
+}
+
+// cached per (Lx, Fx, Nx) on the context
+int fi_twiddles(litho_ctx* ctx, const ImgGeom& g, const float2** out) {
+  auto key = std::make_tuple(g.Lx, g.Fx, g.Nx, -4000);
+  auto it = ctx->twx_tables.find(key);
+  if (it == ctx->twx_tables.end()) {
+    const int ND = 2 * g.Nx + 1;
+    DevBuf b;
+    LITHO_RET(b.ensure(ctx, (size_t)ND * g.Lx * sizeof(float2)));
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    twF_init_kernel<<<dim3((g.Lx + 127) / 128, ND), 128, 0, ctx->stream>>>(b.as<float2>(), g.Lx, g.Fx, ND);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    it = ctx->twx_tables.emplace(key, b).first;
+  }
+  *out = it->second.as<float2>();
+  return LITHO_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -687,13 +800,10 @@ int run_socs(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2*
 int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images) {
   const ImgGeom& g = p.g;
   {
-    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
-    const size_t smem = ((size_t)BH * BW + (size_t)ND * FIP_THREADS) * sizeof(float2);
-    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((g.Lx + FIP_THREADS - 1) / FIP_THREADS, p.batch);
+    const float2* twF = nullptr;
+    LITHO_RET(fi_twiddles(ctx, g, &twF));
     StageScope sc(ctx, LITHO_STAGE_FI_PREP);
-    fi_prep_kernel<<<grid, FIP_THREADS, smem, ctx->stream>>>(band_part, p.ngroups, g.Lx, g.Fx, g.Nx, g.Ny, tm);
-    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    LITHO_CUDA_TRY(ctx, launch_fi_rows(ctx->stream, p, band_part, twF, 0, tm, nullptr, nullptr, nullptr));
   }
   {
     const int KB = 4 * g.Ny + 1;
@@ -830,17 +940,8 @@ cudaError_t image_pipeline_noctx(cudaStream_t s, const ImgPlan& p, const float* 
     default: e = noctx_socs_t<128>(s, p, win_part, krn, sc, band_part); break;
   }
   if (e != cudaSuccess) return e;
-  {
-    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
-    const size_t smem = ((size_t)BH * BW + (size_t)ND * FIP_THREADS) * sizeof(float2);
-    if ((e = cudaFuncSetAttribute(fi_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-      return e;
-    fi_prep_kernel<<<dim3((g.Lx + FIP_THREADS - 1) / FIP_THREADS, 1), FIP_THREADS, smem, s>>>(band_part, p.ngroups,
-                                                                                              g.Lx, g.Fx, g.Nx,
-                                                                                              g.Ny, tm);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
+  // no twiddle table here (nothing may be allocated): the kernel evaluates them
+  if ((e = launch_fi_rows(s, p, band_part, nullptr, 0, tm, nullptr, nullptr, nullptr)) != cudaSuccess) return e;
   {
     const int KB = 4 * g.Ny + 1;
     const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);

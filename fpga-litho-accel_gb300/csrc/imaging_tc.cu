@@ -427,87 +427,6 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
 }
 
 // ---------------------------------------------------------------------------
-// FI prep for the tensor-core contraction: TmT[img][X][KP] split hi/lo
-// ---------------------------------------------------------------------------
-// FI step 1 for the tensor cores.  band_reduce_kernel sums the SOCS band
-// partials of each image once; fi_prep_tc_kernel computes the T rows of
-// FPT_COLS image columns per CTA (four threads per column, each a quarter of the
-// fy rows) with column twiddles from a cached table, and writes hi/lo K-major
-// ([img][X][KP]) for the MMA.
-constexpr int FPT_THREADS = 256, FPT_COLS = 64;
-
-__global__ void band_reduce_kernel(const float2* __restrict__ band_part, int ngroups, int n, float2* __restrict__ S) {
-  const int img = blockIdx.y, idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx < n) S[(size_t)img * n + idx] = sum_strided(band_part + (size_t)img * ngroups * n + idx, (size_t)n, ngroups);
-}
-
-// twF[d][X] = e^{+2 pi i d x'/Fx}, d = 0..2Nx
-__global__ void twF_init_kernel(float2* __restrict__ tw, int Lx, int Fx, int ND) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, d = blockIdx.y;
-  if (x >= Lx || d >= ND) return;
-  const int xp = x + (Fx - Lx) / 2 - Fx / 2;
-  const int m = (d * xp) & (Fx - 1);
-  float sn, cs;
-  sincospif(2.0f * (float)m / (float)Fx, &sn, &cs);
-  tw[(size_t)d * Lx + x] = make_float2(cs, sn);
-}
-
-template <int MAXD>
-__global__ void __launch_bounds__(FPT_THREADS) fi_prep_tc_kernel(const float2* __restrict__ Sg, const float2* __restrict__ twF,
-                                                                 int Lx, int Nx, int Ny, int KP,
-                                                                 float* __restrict__ tmh, float* __restrict__ tml,
-                                                                 float* __restrict__ t0) {
-  extern __shared__ __align__(16) float2 fps[];
-  const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
-  float2* sS = fps;                                             // [BH][BW]
-  float2* sTw = sS + BH * BW;                                   // [MAXD][FPT_COLS]
-  float* sO = reinterpret_cast<float*>(sTw + MAXD * FPT_COLS);  // [FPT_COLS][KP+1]
-  const int tid = threadIdx.x, img = blockIdx.y;
-  const int X0 = blockIdx.x * FPT_COLS;
-  const float2* S0 = Sg + (size_t)img * BH * BW;
-  for (int idx = tid; idx < BH * BW; idx += FPT_THREADS) sS[idx] = S0[idx];
-  for (int idx = tid; idx < MAXD * FPT_COLS; idx += FPT_THREADS) {
-    const int d = idx / FPT_COLS, c = idx % FPT_COLS;
-    sTw[idx] = (d < ND && X0 + c < Lx) ? twF[(size_t)d * Lx + X0 + c] : make_float2(0.f, 0.f);
-  }
-  for (int idx = tid; idx < FPT_COLS * (KP + 1); idx += FPT_THREADS) sO[idx] = 0.f;
-  __syncthreads();
-  const int c = tid >> 2, q = tid & 3;
-  float* o = sO + c * (KP + 1);
-  for (int fy = q; fy < BH; fy += 4) {
-    const float2* S = sS + fy * BW + 2 * Nx;
-    float re = S[0].x, im = S[0].y;
-#pragma unroll
-    for (int d = 1; d < MAXD; ++d) {
-      if (d < ND) {
-        const float2 t = sTw[d * FPT_COLS + c];
-        const float2 p = S[d], qv = S[-d];
-        re += (p.x + qv.x) * t.x - (p.y - qv.y) * t.y;
-        im += (p.y + qv.y) * t.x + (p.x - qv.x) * t.y;
-      }
-    }
-    if (fy == 0) {
-      if (X0 + c < Lx) t0[(size_t)img * Lx + X0 + c] = re;  // the DC row, added by the FI epilogue
-    } else {
-      o[fy - 1] = re;
-      o[2 * Ny + fy - 1] = im;
-    }
-  }
-  __syncthreads();
-  const int nrow = min(FPT_COLS, Lx - X0);
-  const int warp = tid >> 5, lane = tid & 31;
-  for (int xr = warp; xr < nrow; xr += FPT_THREADS / 32) {  // one output row (KP floats) per warp pass
-    const size_t rowb = ((size_t)img * Lx + X0 + xr) * KP;
-    for (int r = lane; r < KP; r += 32) {
-      const float v = sO[xr * (KP + 1) + r];
-      const float h = tf32_round(v);
-      tmh[rowb + r] = h;
-      tml[rowb + r] = v - h;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // FI contraction on the tensor cores
 // ---------------------------------------------------------------------------
 template <int KBLK, int BN>
@@ -928,11 +847,9 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   return LITHO_OK;
 }
 
-// hi/lo T rows [2][batch][Lx][KP] float, the reduced band [batch][2Ny+1][4Nx+1]
-// float2, then the DC row T0 [batch][Lx] float
+// hi/lo T rows [2][batch][Lx][KP] float, then the DC row T0 [batch][Lx] float
 size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch) {
-  return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float) +
-         (size_t)batch * (2 * g.Ny + 1) * (4 * g.Nx + 1) * sizeof(float2) + (size_t)batch * g.Lx * sizeof(float);
+  return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float) + (size_t)batch * g.Lx * sizeof(float);
 }
 
 // tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
@@ -955,40 +872,19 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     cyT_init_kernel<<<dim3((g.Ly + 127) / 128, KP), 128, 0, ctx->stream>>>(cyh, cyl, g.Ly, g.Fy, g.Ny, KP);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  // TmT hi/lo: [batch][Lx][KP]
+  // TmT hi/lo: [batch][Lx][KP], then T0
   float* tmh = tmT;
   if (tmh == nullptr) {
     LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(g, p.batch)));
     tmh = ctx->mx_b.as<float>();
   }
   float* tml = tmh + (size_t)p.batch * g.Lx * KP;
-  float* t0 = nullptr;
+  float* t0 = tml + (size_t)p.batch * g.Lx * KP;
   {
-    const int BH = 2 * g.Ny + 1, BW = 4 * g.Nx + 1, ND = 2 * g.Nx + 1;
-    // column twiddles, cached per (Lx, Fx, Nx)
-    float* twf = nullptr;
-    LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -4000), (size_t)ND * g.Lx * sizeof(float2), &fresh,
-                           &twf));
-    if (fresh) {
-      StageScope sc(ctx, LITHO_STAGE_UPLOAD);
-      twF_init_kernel<<<dim3((g.Lx + 127) / 128, ND), 128, 0, ctx->stream>>>(reinterpret_cast<float2*>(twf), g.Lx,
-                                                                             g.Fx, ND);
-      LITHO_CUDA_TRY(ctx, cudaGetLastError());
-    }
-    float2* S = reinterpret_cast<float2*>(tml + (size_t)p.batch * g.Lx * KP);  // after the T rows
-    t0 = reinterpret_cast<float*>(S + (size_t)p.batch * BH * BW);
-    const int MAXD = ND <= 5 ? 5 : ND <= 9 ? 9 : ND <= 17 ? 17 : 33;
-    const size_t smem = (size_t)BH * BW * sizeof(float2) + (size_t)MAXD * FPT_COLS * sizeof(float2) +
-                        (size_t)FPT_COLS * (KP + 1) * sizeof(float);
-    auto k = ND <= 5 ? fi_prep_tc_kernel<5> : ND <= 9 ? fi_prep_tc_kernel<9> : ND <= 17 ? fi_prep_tc_kernel<17>
-                                                                                        : fi_prep_tc_kernel<33>;
-    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    StageScope sc(ctx, LITHO_STAGE_FI_PREP, 2);
-    band_reduce_kernel<<<dim3((BH * BW + 127) / 128, p.batch), 128, 0, ctx->stream>>>(band_part, p.ngroups, BH * BW,
-                                                                                       S);
-    k<<<dim3((g.Lx + FPT_COLS - 1) / FPT_COLS, p.batch), FPT_THREADS, smem, ctx->stream>>>(
-        S, reinterpret_cast<const float2*>(twf), g.Lx, g.Nx, g.Ny, KP, tmh, tml, t0);
-    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    const float2* twF = nullptr;
+    LITHO_RET(fi_twiddles(ctx, g, &twF));
+    StageScope sc(ctx, LITHO_STAGE_FI_PREP);
+    LITHO_CUDA_TRY(ctx, launch_fi_rows(ctx->stream, p, band_part, twF, KP, nullptr, tmh, tml, t0));
   }
   if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
   return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);

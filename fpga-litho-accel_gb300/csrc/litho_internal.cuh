@@ -186,6 +186,11 @@ int run_win_dft(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* wi
 int run_socs(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2* krn,
              const float* scales, float2* band_part, float* tmpImgp);
 int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
+// FI step 1 for both layouts (tmh == nullptr: plain tm; else K-major hi/lo + t0);
+// twF == nullptr evaluates the column twiddles in the kernel
+cudaError_t launch_fi_rows(cudaStream_t s, const ImgPlan& p, const float2* band_part, const float2* twF, int KP,
+                           float* tm, float* tmh, float* tml, float* t0);
+int fi_twiddles(litho_ctx* ctx, const ImgGeom& g, const float2** out);
 int run_fft_mask(litho_ctx* ctx, const float* mask, int Lx, int Ly, float* mskf_r, float* mskf_i);
 int upload_kernels(litho_ctx* ctx, const float* krn_r, const float* krn_i, const float* scales,
                    int nk, int kdim, int mem, float2* krn_dev, float* scales_dev);
