@@ -115,52 +115,65 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 //               a tile with a residual is split in place (hi, then lo)
 //   warp 8      TMA producer (one lane), warp 9 MMA issuer (one lane)
 //   warps 10-13 epilogue: TMEM -> registers -> shared -> row DFT -> partials
-// Per stage s and running chunk q (parity (q / S) & 1):
-//   producer  : [wait empty[s]] -> TMA mask tile + twiddle hi/lo tiles -> full[s]
+// Per stage s and running chunk q (parity (q / S) & 1; every role keeps s and the
+// parity as running counters, since a division by the launch-time S on the
+// per-chunk path measurably slows the ring):
+//   producer  : [wait empty[s]] -> TMA mask tile + twiddle [hi; lo] tile -> full[s]
 //   consumers : wait full[s]; vote residual (nzflag); if any: Ah = round_tf32(A) in
 //               place; arrive ready[s]; if residual: wait hidone[s], write Al,
 //               arrive ready2[s]
 //   MMA lane  : [tile start: wait accempty[buf]]; wait ready[s]; Ah*[Bh; Bl] as one
-//               N = 2 NB MMA per K step (the epilogue adds the two column halves);
+//               N = 2 NBH MMA per K step (the epilogue adds the two column halves);
 //               if residual: commit hidone[s], wait ready2[s], Al*Bh; commit empty[s];
 //               [tile end: commit accfull[buf]]
-//   epilogue  : wait accfull[buf]; TMEM -> sR; arrive accempty[buf]; row DFT with
-//               one warp per output (lanes over rows, shuffle reduction)
+//   epilogue  : wait accfull[buf]; TMEM -> sR (hi + lo halves); arrive accempty[buf];
+//               row DFT with one thread per output pair (+v, -v)
 // hidone/ready2 complete only on chunks with a residual, so their parities are
 // tracked per stage in bit masks that both sides flip identically.
-template <int NB>
+//
+// The ring is as deep as shared memory allows: under full load a mask tile takes
+// ~3 us from TMA issue to landing, so the bytes in flight per SM, not the work per
+// tile, set the throughput.  Hence the twiddle tile carries only the 2Nx+1 used
+// rows of each half (NBH = 2Nx+1 rounded up to 8) and the epilogue buffers are
+// sized for the actual Ny; the stage count S is chosen at launch.
+template <int NBH>
 struct WinTC {
-  static constexpr uint32_t A_B = 128 * 128;       // 128 rows x 32 fp32 (split in place: hi, then lo)
-  static constexpr uint32_t B_B = NB * 128;        // NB rows x 32 fp32
-  static constexpr uint32_t STAGE_B = A_B + 2 * B_B;
-  // one accumulator holds A*Bh in columns [0, NB) and A*Bl in [NB, 2 NB): the hi and
-  // lo twiddle tiles sit back to back in shared memory, so one N = 2 NB MMA reads
-  // the mask tile once for both products
-  static constexpr uint32_t NCOL = NB == 16 ? 32 : (NB == 32 ? 64 : 128);
-  static constexpr uint32_t EPI_B = NB * 129 * 4 + 17 * 129 * 8;  // sR [NB][129] + sRT [Ny+1 <= 17][129]
-  static constexpr int FIT = (int)((220u * 1024u - EPI_B - 2048u) / STAGE_B);
-  static constexpr int STAGES = FIT > 8 ? 8 : FIT;
-  static constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_B + EPI_B + 1024;
+  static constexpr uint32_t A_B = 128 * 128;        // 128 rows x 32 fp32 (split in place: hi, then lo)
+  static constexpr uint32_t B_B = 2 * NBH * 128;    // [hi NBH rows; lo NBH rows] x 32 fp32
+  static constexpr uint32_t STAGE_B = A_B + B_B;    // a multiple of 2048: every stage is 1024-aligned
+  // one accumulator holds A*Bh in columns [0, NBH) and A*Bl in [NBH, 2 NBH): one
+  // N = 2 NBH MMA reads the mask tile once for both products
+  static constexpr uint32_t NCOL = 2 * NBH <= 32 ? 32 : (2 * NBH <= 64 ? 64 : 128);
+  static constexpr int NLO = (NBH + 15) / 16 * 16;  // N of the residual pass Al*Bh (>= NBH, multiple of 16)
 };
 constexpr int WP_THREADS = 448;  // warps 0-7 split, 8 TMA, 9 MMA, 10-13 epilogue
 constexpr int WP_CONS = 256;     // consumer threads
+constexpr int WP_RS = 129;       // padded row stride of the epilogue buffers
+constexpr int WP_MAX_STAGES = 12;
+constexpr size_t WP_SMEM_CAP = 227 * 1024;
 
-template <int NB>
+// epilogue buffers: sR [NBH][RS] fp32 + sRT [Ny+1][RS] float2
+static inline size_t win_epi_bytes(int NBH, int Ny) {
+  return (size_t)NBH * WP_RS * 4 + (size_t)(Ny + 1) * WP_RS * 8;
+}
+// mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES)
+static inline size_t win_bar_bytes(int S) { return (size_t)(5 * S + 5) * 8 + 16 + 8 * (size_t)S; }
+
+template <int NBH>
 __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
                                                                    const __grid_constant__ CUtensorMap tmB,
                                                                    int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
-                                                                   int rows, int batch, int ncs,
+                                                                   int rows, int batch, int ncs, int S,
                                                                    const float2* __restrict__ ytab,
                                                                    float2* __restrict__ win_part, int part_stride,
                                                                    int* __restrict__ err) {
-  using P = WinTC<NB>;
-  constexpr int S = P::STAGES;
+  using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  constexpr int RS = 129;  // padded row stride: per-thread row walks hit distinct banks
-  float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [NB][RS]
-  float2* sRT = reinterpret_cast<float2*>(sR + NB * RS);              // [Ny+1][RS]
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)S * P::STAGE_B + P::EPI_B);
+  constexpr int RS = WP_RS;  // padded row stride: per-thread row walks hit distinct banks
+  float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [NBH][RS]
+  float2* sRT = reinterpret_cast<float2*>(sR + NBH * RS);             // [Ny+1][RS]
+  uint64_t* full = reinterpret_cast<uint64_t*>(sRT + (Ny + 1) * RS);
   uint64_t* ready = full + S;
   uint64_t* hidone = ready + S;
   uint64_t* ready2 = hidone + S;
@@ -201,7 +214,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   const uint32_t tmem = *tslot;
 
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
-  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };  // [Bh; Bl], 2 NB rows
+  auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };  // [Bh; Bl], 2 NBH rows
   // tile t -> (image, row block, column split) and its chunk range
   auto decode = [&](int t, int& img, int& rb, int& cs, int& c0, int& c1) {
     img = t / (rows * ncs);
@@ -214,31 +227,38 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
 
   if (warp == 8) {
     if (lane == 0) {  // TMA producer
-      int q = 0;
+      int q = 0, s = 0;
+      uint32_t ph = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
         int img, rb, cs, c0, c1;
         decode(t, img, rb, cs, c0, c1);
         for (int c = c0; c < c1; ++c, ++q) {
-          const int s = q % S;
-          if (q >= S && !mbar_wait_ab(&empty[s], (uint32_t)((q - S) / S) & 1u, abort)) {
+          if (q >= S && !mbar_wait_ab(&empty[s], ph ^ 1u, abort)) {
             *abort = 1;
             ok = false;
             break;
           }
-          mbar_arrive_expect_tx(&full[s], P::A_B + 2 * P::B_B);
+          mbar_arrive_expect_tx(&full[s], P::STAGE_B);
           tma_load_3d(sA(s), &tmM, &full[s], 32 * c, 128 * rb, img);
           tma_load_2d(sBh(s), &tmB, &full[s], 32 * c, 0);
           last_issued[s] = q;
+          if (++s == S) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
       }
     }
   } else if (warp == 9) {
     if (lane == 0) {  // MMA issuer
-      constexpr uint32_t IDESC2 = idesc_tf32(128, 2 * NB);  // A x [Bh; Bl]
-      constexpr uint32_t IDESC1 = idesc_tf32(128, NB);      // Al x Bh
+      constexpr uint32_t IDESC2 = idesc_tf32(128, 2 * NBH);  // A x [Bh; Bl]
+      // Al x Bh over the first NLO twiddle rows: the hi rows, plus (when NBH is not
+      // a multiple of 16) a few lo rows whose Al*Bl terms only add accuracy
+      constexpr uint32_t IDESC1 = idesc_tf32(128, P::NLO);
       uint32_t ph2 = 0;  // per-stage parity of hidone / ready2
-      int q = 0, tl = 0;
+      int tl = 0, s = 0;
+      uint32_t ph = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < T && ok; t += gridDim.x, ++tl) {
         int img, rb, cs, c0, c1;
@@ -250,9 +270,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         }
         tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)buf * P::NCOL;
-        for (int c = c0; c < c1; ++c, ++q) {
-          const int s = q % S;
-          if (!mbar_wait_ab(&ready[s], (uint32_t)(q / S) & 1u, abort)) {
+        for (int c = c0; c < c1; ++c) {
+          if (!mbar_wait_ab(&ready[s], ph, abort)) {
             *abort = 1;
             ok = false;
             break;
@@ -282,23 +301,26 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
             }
           }
           mma_commit(&empty[s]);
+          if (++s == S) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
         if (ok) mma_commit(&accfull[buf]);  // arrives when this tile's MMAs have completed
       }
       mma_commit(done);  // arrives once everything issued above has completed
     }
   } else if (warp < 8) {  // warps 0-7: check / split the landed tiles in place
-    uint32_t ph2 = 0;
-    int q = 0;
+    uint32_t ph2 = 0, ph = 0;
+    int s = 0;
     // a wait that gives up flags the error and the thread carries on through the
     // named barriers with the others (later waits return at once): a thread that
     // left alone would strand the rest at the next barrier
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
       int img, rb, cs, c0, c1;
       decode(t, img, rb, cs, c0, c1);
-      for (int c = c0; c < c1; ++c, ++q) {
-        const int s = q % S;
-        if (!mbar_wait_ab(&full[s], (uint32_t)(q / S) & 1u, abort)) *abort = 1;
+      for (int c = c0; c < c1; ++c) {
+        if (!mbar_wait_ab(&full[s], ph, abort)) *abort = 1;
         float4* a = reinterpret_cast<float4*>(sA(s));
         float4 v[4];
         bool nz = false;
@@ -329,6 +351,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           fence_proxy_async();
           mbar_arrive(&ready2[s]);
         }
+        if (++s == S) {
+          s = 0;
+          ph ^= 1u;
+        }
       }
     }
   } else {  // warps 10-13: epilogue
@@ -345,27 +371,14 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) *abort = 1;
       tc_fence_after();
       const uint32_t trow = tmem + (uint32_t)buf * P::NCOL + ((uint32_t)(32 * quarter) << 16);
-      // sR[j] = (A Bh)[j] + (A Bl)[j]
-      if (NB == 16) {
-        float v[32];
-        tmem_ld32(trow, v);
+      // sR[j] = (A Bh)[j] + (A Bl)[j]: 2 NBH columns in 8-column loads, one wait
+      {
+        uint32_t v[2 * NBH];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) sR[j * RS + row] = v[j] + v[16 + j];
-      } else if (NB == 32) {
-        float h[32], l[32];
-        tmem_ld32(trow, h);
-        tmem_ld32(trow + 32u, l);
+        for (int g = 0; g < 2 * NBH / 8; ++g) tmem_ld8_async(trow + 8u * g, &v[8 * g]);
+        tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) sR[j * RS + row] = h[j] + l[j];
-      } else {  // NB = 48: three 16-column groups of each half
-#pragma unroll
-        for (int g = 0; g < 3; ++g) {
-          float h[16], l[16];
-          tmem_ld16(trow + 16u * g, h);
-          tmem_ld16(trow + 48u + 16u * g, l);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) sR[(16 * g + j) * RS + row] = h[j] + l[j];
-        }
+        for (int j = 0; j < NBH; ++j) sR[j * RS + row] = __uint_as_float(v[j]) + __uint_as_float(v[NBH + j]);
       }
       tc_fence_before();
       mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
@@ -718,9 +731,10 @@ static int make_map(litho_ctx* ctx, CUtensorMap* m, const void* base, int rank, 
   return LITHO_OK;
 }
 
+// twiddle rows of each half of the window DFT's B tile: 2Nx+1 rounded up to 8
 static int nb_for(int Nx) {
   const int nj = 2 * Nx + 1;
-  return nj <= 16 ? 16 : (nj <= 32 ? 32 : (nj <= 48 ? 48 : -1));
+  return nj <= 40 ? (nj + 7) / 8 * 8 : -1;
 }
 static int kblk_for(int Ny) { return std::max(1, (4 * Ny + 31) / 32); }  // 4Ny K rows (the DC row is separate)
 
@@ -767,18 +781,18 @@ static int cached_table(litho_ctx* ctx, std::tuple<int, int, int, int> key, size
   return LITHO_OK;
 }
 
-template <int NB>
+template <int NBH>
 static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
   const ImgGeom& g = p.g;
   bool fresh = false;
   float* tw = nullptr;
-  LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -NB), (size_t)2 * NB * g.Lx * sizeof(float), &fresh,
-                         &tw));
+  LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -NBH), (size_t)2 * NBH * g.Lx * sizeof(float),
+                         &fresh, &tw));
   float* twh = tw;
-  float* twl = tw + (size_t)NB * g.Lx;
+  float* twl = tw + (size_t)NBH * g.Lx;
   if (fresh) {
     StageScope sc(ctx, LITHO_STAGE_UPLOAD);
-    twT_init_kernel<<<dim3((g.Lx + 127) / 128, NB), 128, 0, ctx->stream>>>(twh, twl, g.Lx, g.Fx, g.Nx, NB);
+    twT_init_kernel<<<dim3((g.Lx + 127) / 128, NBH), 128, 0, ctx->stream>>>(twh, twl, g.Lx, g.Fx, g.Nx, NBH);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   // row twiddles of the epilogue, cached per (Ly, Fy, Ny)
@@ -793,18 +807,22 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   }
   CUtensorMap mM, mB;
   LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
-  LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NB, 1, 2 * NB));  // hi rows, then lo rows
-  const size_t smem = WinTC<NB>::SMEM;
-  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
+  // as many ring stages as shared memory holds
+  using P = WinTC<NBH>;
+  const size_t fixed = 1024 + win_epi_bytes(NBH, g.Ny) + win_bar_bytes(WP_MAX_STAGES);
+  const int S = (int)std::min<size_t>(WP_MAX_STAGES, (WP_SMEM_CAP - fixed) / P::STAGE_B);
+  const size_t smem = 1024 + (size_t)S * P::STAGE_B + win_epi_bytes(NBH, g.Ny) + win_bar_bytes(S);
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NBH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
   const int tiles = rows * p.batch * ncs;
   const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
-  win_dft_tc_kernel<NB><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny,
-                                                                 rows, p.batch, ncs,
-                                                                 reinterpret_cast<const float2*>(yt), win_part,
-                                                                 p.part_stride, err);
+  win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, rows,
+                                                                  p.batch, ncs, S,
+                                                                  reinterpret_cast<const float2*>(yt), win_part,
+                                                                  p.part_stride, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
@@ -813,9 +831,11 @@ int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2*
   int* err = nullptr;
   LITHO_RET(tc_err_flag(ctx, &err));
   switch (nb_for(p.g.Nx)) {
+    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err);
     case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err);
+    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err);
     case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err);
-    case 48: return launch_win_tc<48>(ctx, p, masks, win_part, err);
+    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err);
     default:
       set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT supports Nx <= 16");
       return LITHO_ERR_UNSUPPORTED;
