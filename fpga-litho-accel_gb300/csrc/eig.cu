@@ -4,21 +4,34 @@
 //
 //   1. hermitize_kernel     A = upper triangle of TCC mirrored (zheevr reads 'U' only)
 //   2. Householder tridiagonalisation, one reflector per column k (the zhetd2
-//      recurrence): hh_kernel forms v, tau, beta; symv_kernel x = tau*B*v;
-//      her2_kernel B -= v w^H + w v^H with w = x - tau/2 (x^H v) v.  The
-//      off-diagonal comes out real; v_k is kept in column k below the diagonal.
-//   3. bisect_kernel        the nk largest eigenvalues of the real tridiagonal T
-//                           by Sturm-count bisection (one thread each);
-//   4. inviter_kernel       eigenvectors of T by inverse iteration on a pivoted
-//                           tridiagonal LU, re-orthogonalised inside clusters of
-//                           close eigenvalues (degenerate pairs are common: a
-//                           symmetric source gives exact pairs);
+//      recurrence), two launches per column: symv_hh_kernel forms v, tau, beta
+//      and x = tau*B*v; her2_kernel B -= v w^H + w v^H with w = x - tau/2 (x^H v) v
+//      on the lower-triangle tiles, mirrored.  The off-diagonal comes out real.
+//      Column k below the diagonal is read as the conjugate of row k (A stays
+//      Hermitian in full), and v_k is packed contiguously for the back-transform.
+//      Both kernels are bound by the FP64 pipe (GB300: 2 DFMA/clk/SM), so the
+//      arithmetic is written as FMA chains and the update touches each element
+//      pair once.
+//   3. multisect_kernel     the nk largest eigenvalues of the real tridiagonal T
+//                           by Sturm counts, one warp per eigenvalue and one CTA
+//                           per SM: each round evaluates 32 points of the
+//                           bracketing interval at once (33-way multisection);
+//   4. invvec_kernel        eigenvector j of T by inverse iteration on the
+//                           pivoted tridiagonal LU of T - shift_j I (the dgttrf
+//                           recurrence), one CTA per eigenvector with the LU in
+//                           shared memory;
+//      cluster_rr_kernel    inside each cluster of close eigenvalues (a symmetric
+//                           source gives exact degenerate pairs) the vectors are
+//                           orthonormalised (Gram-Schmidt, twice) and rotated by
+//                           a Rayleigh-Ritz step on the cluster's subspace
+//                           (Jacobi eigendecomposition of Z^T T Z);
 //   5. backtransform_kernel y = H_0 H_1 ... H_{n-2} z;
 //   6. output_kernel        scales[i] = lambda_i (descending) and
 //                           krn[i][j] = y_i[n-1-j] (litho.cpp:626-634 reversal).
 // No kernel waits on another; every step is a separate launch on the stream.
 #include "litho_internal.cuh"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <vector>
@@ -61,105 +74,194 @@ __global__ void hermitize_kernel(const double2* __restrict__ in, double2* __rest
   A[(size_t)i * n + j] = v;
 }
 
-// Reflector for column k: x = A[k+1:n][k], m = n-k-1.
-__global__ void __launch_bounds__(256) hh_kernel(double2* __restrict__ A, int n, int k, double2* __restrict__ vbuf,
-                                                 double2* __restrict__ tau, double* __restrict__ d,
-                                                 double* __restrict__ e) {
+// Step k of the reduction, fused: the reflector of column k and x = tau B v with
+// B = A[k+1:, k+1:].  Column k below the diagonal is conj(row k right of it), read
+// contiguously.  Every CTA derives the reflector's scalars (norm, beta, tau, scale)
+// from row k by the same fixed-order reduction, so they agree bitwise, and CTA 0
+// publishes v, tau, d[k], e[k] and the packed copy of v kept for the back-transform.
+// With v = (1, scl conj(row_k[1:])), B v = B[:,0] + scl B[:,1:] conj(row_k[1:]), so a
+// row needs only row k itself; one warp per row, FMA chains (4 per complex element).
+// Each CTA also leaves the partial sum of conj(x_i) v_i over its rows: the rank-2
+// update adds them up in a fixed order for its correction term.
+__device__ __forceinline__ size_t vpack_off(int n, int k) { return (size_t)k * (n - 1) - (size_t)k * (k - 1) / 2; }
+
+__global__ void __launch_bounds__(256) symv_hh_kernel(const double2* __restrict__ A, int n, int k,
+                                                      double2* __restrict__ vbuf, double2* __restrict__ vpack,
+                                                      double2* __restrict__ tau, double* __restrict__ d,
+                                                      double* __restrict__ e, double2* __restrict__ xbuf,
+                                                      double2* __restrict__ part) {
   __shared__ double red[32];
+  __shared__ double2 sp[8];
   const int m = n - k - 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double2* rowk = A + (size_t)k * n + (k + 1);
   double s = 0.0;
   for (int i = 1 + threadIdx.x; i < m; i += 256) {
-    const double2 x = A[(size_t)(k + 1 + i) * n + k];
-    s += x.x * x.x + x.y * x.y;
+    const double2 x = rowk[i];
+    s = fma(x.x, x.x, s);
+    s = fma(x.y, x.y, s);
   }
   const double xnorm2 = block_sum<256>(s, red);
-  const double2 alpha = A[(size_t)(k + 1) * n + k];
-  double2 t = make_double2(0.0, 0.0);
-  double beta = alpha.x;
-  double2 scl = make_double2(0.0, 0.0);
-  if (!(xnorm2 == 0.0 && alpha.y == 0.0)) {
-    const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2);
-    beta = alpha.x >= 0.0 ? -nrm : nrm;
-    t = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-    // scl = 1 / (alpha - beta)
-    const double2 den = make_double2(alpha.x - beta, alpha.y);
-    const double dd = den.x * den.x + den.y * den.y;
-    scl = make_double2(den.x / dd, -den.y / dd);
+  __shared__ double2 s_t, s_scl;
+  __shared__ double s_beta;
+  if (threadIdx.x == 0) {  // the reflector's scalars (FP64 is scarce: one thread)
+    const double2 alpha = zconj(rowk[0]);
+    double2 tt = make_double2(0.0, 0.0);
+    double beta = alpha.x;
+    double2 sc = make_double2(0.0, 0.0);
+    if (!(xnorm2 == 0.0 && alpha.y == 0.0)) {
+      const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2);
+      beta = alpha.x >= 0.0 ? -nrm : nrm;
+      tt = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+      // scl = 1 / (alpha - beta)
+      const double2 den = make_double2(alpha.x - beta, alpha.y);
+      const double dd = den.x * den.x + den.y * den.y;
+      sc = make_double2(den.x / dd, -den.y / dd);
+    }
+    s_t = tt;
+    s_scl = sc;
+    s_beta = beta;
   }
-  for (int i = threadIdx.x; i < m; i += 256) {
-    double2 v;
-    if (i == 0) v = make_double2(1.0, 0.0);
-    else v = zmul(A[(size_t)(k + 1 + i) * n + k], scl);
-    vbuf[i] = v;
-    A[(size_t)(k + 1 + i) * n + k] = v;  // keep v_k for the back-transform
+  __syncthreads();
+  const double2 t = s_t, scl = s_scl;
+  const double beta = s_beta;
+  if (blockIdx.x == 0) {
+    double2* vp = vpack + vpack_off(n, k);
+    for (int i = threadIdx.x; i < m; i += 256) {
+      const double2 v = i == 0 ? make_double2(1.0, 0.0) : zmul(zconj(rowk[i]), scl);
+      vbuf[i] = v;
+      vp[i] = v;
+    }
+    if (threadIdx.x == 0) {
+      tau[k] = t;
+      e[k] = beta;
+      d[k] = A[(size_t)k * n + k].x;
+    }
   }
-  if (threadIdx.x == 0) {
-    tau[k] = t;
-    e[k] = beta;
-    d[k] = A[(size_t)k * n + k].x;
-  }
-}
-
-// x_i = tau * sum_j B[i][j] v_j, B = A[k+1:, k+1:]; one warp per row.
-__global__ void __launch_bounds__(256) symv_kernel(const double2* __restrict__ A, int n, int k,
-                                                   const double2* __restrict__ vbuf, const double2* __restrict__ tau,
-                                                   double2* __restrict__ xbuf) {
-  const int m = n - k - 1;
-  const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (row >= m) return;
-  const double2* Ar = A + (size_t)(k + 1 + row) * n + (k + 1);
-  double re = 0.0, im = 0.0;
-  for (int j = lane; j < m; j += 32) {
-    const double2 a = Ar[j], v = vbuf[j];
-    re += a.x * v.x - a.y * v.y;
-    im += a.x * v.y + a.y * v.x;
-  }
+  const int row = blockIdx.x * 8 + warp;
+  double2 contrib = make_double2(0.0, 0.0);
+  if (row < m) {
+    const double2* Ar = A + (size_t)(k + 1 + row) * n + (k + 1);
+    double re = 0.0, im = 0.0;
+    for (int j = 1 + lane; j < m; j += 32) {
+      const double2 a = Ar[j], r = rowk[j];  // a * conj(r)
+      re = fma(a.x, r.x, re);
+      re = fma(a.y, r.y, re);
+      im = fma(a.y, r.x, im);
+      im = fma(-a.x, r.y, im);
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    re += __shfl_xor_sync(0xffffffffu, re, o);
-    im += __shfl_xor_sync(0xffffffffu, im, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    const double2 a0 = Ar[0];
+    const double2 bv = make_double2(a0.x + (scl.x * re - scl.y * im), a0.y + (scl.x * im + scl.y * re));
+    const double2 xr = zmul(t, bv);
+    const double2 vr = row == 0 ? make_double2(1.0, 0.0) : zmul(zconj(rowk[row]), scl);
+    contrib = zmul(zconj(xr), vr);
+    if (lane == 0) xbuf[row] = xr;
   }
-  if (lane == 0) xbuf[row] = zmul(tau[k], make_double2(re, im));
-}
-
-// w = x - tau/2 (x^H v) v (one CTA), written over xbuf.
-__global__ void __launch_bounds__(256) wdot_kernel(int n, int k, const double2* __restrict__ vbuf,
-                                                   double2* __restrict__ xbuf, const double2* __restrict__ tau) {
-  __shared__ double red[32];
-  const int m = n - k - 1;
-  double sr = 0.0, si = 0.0;
-  for (int i = threadIdx.x; i < m; i += 256) {
-    const double2 x = xbuf[i], v = vbuf[i];
-    sr += x.x * v.x + x.y * v.y;  // conj(x) * v
-    si += x.x * v.y - x.y * v.x;
-  }
-  sr = block_sum<256>(sr, red);
-  si = block_sum<256>(si, red);
-  const double2 t = tau[k];
-  const double2 c = zmul(make_double2(-0.5 * t.x, -0.5 * t.y), make_double2(sr, si));
-  for (int i = threadIdx.x; i < m; i += 256) {
-    const double2 v = vbuf[i];
-    const double2 x = xbuf[i];
-    xbuf[i] = make_double2(x.x + c.x * v.x - c.y * v.y, x.y + c.x * v.y + c.y * v.x);
+  if (lane == 0) sp[warp] = contrib;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double2 acc = sp[0];
+    for (int w = 1; w < 8; ++w) acc = make_double2(acc.x + sp[w].x, acc.y + sp[w].y);
+    part[blockIdx.x] = acc;
   }
 }
 
-// B -= v w^H + w v^H (w in wbuf); 32 x 32 tiles, 8 rows per pass.
+// B -= v w^H + w v^H with w = x - tau/2 (x^H v) v, on the lower-triangle 32 x 32
+// tiles (I >= J) only; x^H v is the fixed-order sum of the nparts partials of the
+// product kernel, formed by every CTA.  An off-diagonal tile is computed once and
+// written twice, as itself and as its conjugate transpose (staged in shared memory
+// so both writes are coalesced); a diagonal tile writes its lower half and mirrors
+// it into the upper.  That halves the FP64 work, and B stays exactly Hermitian,
+// which the product kernel (full rows) relies on.  Each element is 8 FMAs.
+// blockIdx.x enumerates the tiles row by row: t = I (I + 1) / 2 + J.
 __global__ void __launch_bounds__(256) her2_kernel(double2* __restrict__ A, int n, int k,
-                                                   const double2* __restrict__ vbuf, const double2* __restrict__ wbuf) {
+                                                   const double2* __restrict__ vbuf, const double2* __restrict__ xbuf,
+                                                   const double2* __restrict__ tau, const double2* __restrict__ part,
+                                                   int nparts) {
+  __shared__ double2 tile[32][33];
+  __shared__ double2 s_c;
+  __shared__ double2 s_v[2][32], s_w[2][32];  // [0]: the tile's columns, [1]: its rows
   const int m = n - k - 1;
-  const int j = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int i0 = blockIdx.y * 32 + (threadIdx.x >> 5);
-  if (j >= m) return;
-  const double2 vj = vbuf[j];
-  const double2 wj = wbuf[j];
-  for (int i = i0; i < min(m, blockIdx.y * 32 + 32); i += 8) {
-    const double2 vi = vbuf[i];
-    const double2 wi = wbuf[i];
-    double2* a = A + (size_t)(k + 1 + i) * n + (k + 1 + j);
-    const double2 p = zmul(vi, zconj(wj)), q = zmul(wi, zconj(vj));
-    a->x -= p.x + q.x;
-    a->y -= p.y + q.y;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  if (ty == 0) {
+    double sr = 0.0, si = 0.0;
+    for (int p = tx; p < nparts; p += 32) {
+      sr += part[p].x;
+      si += part[p].y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (tx == 0) {
+      const double2 tk = tau[k];
+      s_c = zmul(make_double2(-0.5 * tk.x, -0.5 * tk.y), make_double2(sr, si));
+    }
+  }
+  __syncthreads();
+  const int t = blockIdx.x;
+  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  const int J = t - I * (I + 1) / 2;
+  if (threadIdx.x < 64) {  // w = x + c v for the tile's 32 columns and 32 rows, once
+    const int side = threadIdx.x >> 5, q = (side ? I : J) * 32 + tx;
+    double2 vq = make_double2(0.0, 0.0), wq = vq;
+    if (q < m) {
+      const double2 c = s_c;
+      vq = vbuf[q];
+      const double2 xq = xbuf[q];
+      wq = make_double2(xq.x + (c.x * vq.x - c.y * vq.y), xq.y + (c.x * vq.y + c.y * vq.x));
+    }
+    s_v[side][tx] = vq;
+    s_w[side][tx] = wq;
+  }
+  __syncthreads();
+  const int j = J * 32 + tx;
+  const double2 vj = s_v[0][tx], wj = s_w[0][tx];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = I * 32 + ty + 8 * r;
+    if (i < m && j < m) {
+      const double2 vi = s_v[1][ty + 8 * r], wi = s_w[1][ty + 8 * r];
+      double2* a = A + (size_t)(k + 1 + i) * n + (k + 1 + j);
+      const double2 av = *a;
+      // a - vi conj(wj) - wi conj(vj)
+      double re = fma(-vi.x, wj.x, av.x);
+      re = fma(-vi.y, wj.y, re);
+      re = fma(-wi.x, vj.x, re);
+      re = fma(-wi.y, vj.y, re);
+      double im = fma(-vi.y, wj.x, av.y);
+      im = fma(vi.x, wj.y, im);
+      im = fma(-wi.y, vj.x, im);
+      im = fma(wi.x, vj.y, im);
+      const double2 nv = make_double2(re, im);
+      if (I != J) *a = nv;
+      tile[ty + 8 * r][tx] = nv;
+    }
+  }
+  __syncthreads();
+  if (I == J) {  // diagonal tile: lower half as computed, upper half mirrored
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int ii = ty + 8 * r, i = I * 32 + ii;
+      if (i < m && j < m)
+        A[(size_t)(k + 1 + i) * n + (k + 1 + j)] = ii >= tx ? tile[ii][tx] : zconj(tile[tx][ii]);
+    }
+    return;
+  }
+  // mirror: A[J-tile row jj][I-tile col ii] = conj(tile[ii][jj])
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int jj = ty + 8 * r, ii = tx;
+    const int row = J * 32 + jj, col = I * 32 + ii;
+    if (row < m && col < m) A[(size_t)(k + 1 + row) * n + (k + 1 + col)] = zconj(tile[ii][jj]);
   }
 }
 
@@ -180,148 +282,405 @@ __device__ int sturm_count_lt(const double* d, const double* e, int n, double x,
   return c;
 }
 
-// eigenvalue j (0 = largest) of T by bisection; T has diagonal d, off-diagonal e.
-__global__ void bisect_kernel(const double* __restrict__ d, const double* __restrict__ e, int n, int nk,
-                              double* __restrict__ evals) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+// eigenvalue j (0 = largest) of T (diagonal d, off-diagonal e) by multisection:
+// one CTA of MS_THREADS per eigenvalue (blockIdx.x); every round evaluates the Sturm
+// count at MS_THREADS interior points of the bracket [lo, hi], count(lo) <= m <
+// count(hi) with m the ascending index, and keeps the sub-interval holding the
+// crossing.  A Sturm count is a sequential FP64 recurrence with a division per row,
+// so one count is latency-bound; the points of a round run side by side, and a
+// 129-way split needs ~8 rounds where bisection needs ~52.  The rounds stop when the
+// bracket no longer shrinks in floating point.
+constexpr int MS_THREADS = 128;
+
+__global__ void __launch_bounds__(MS_THREADS) multisect_kernel(const double* __restrict__ d,
+                                                               const double* __restrict__ e, int n, int nk,
+                                                               double* __restrict__ evals) {
+  __shared__ double sh[3][MS_THREADS / 32];
+  __shared__ unsigned masks[MS_THREADS / 32];
+  const int j = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (j >= nk) return;
-  double lo = d[0], hi = d[0], emax = 0.0;
-  for (int i = 0; i < n; ++i) {
+  double lo = 1e300, hi = -1e300, emax = 0.0;
+  for (int i = t; i < n; i += MS_THREADS) {
     const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
     lo = fmin(lo, d[i] - r);
     hi = fmax(hi, d[i] + r);
     if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
+  if (lane == 0) {
+    sh[0][warp] = lo;
+    sh[1][warp] = hi;
+    sh[2][warp] = emax;
+  }
+  __syncthreads();
+  for (int w = 0; w < MS_THREADS / 32; ++w) {
+    lo = fmin(lo, sh[0][w]);
+    hi = fmax(hi, sh[1][w]);
+    emax = fmax(emax, sh[2][w]);
   }
   const double span = fmax(fabs(lo), fabs(hi));
   lo -= 2.0 * DBL_EPSILON * span + 1e-300;
   hi += 2.0 * DBL_EPSILON * span + 1e-300;
   const double pivmin = 1e-290 * fmax(1.0, emax);
   const int m = n - 1 - j;  // ascending index
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count_lt(d, e, n, mid, pivmin) > m) hi = mid;
-    else lo = mid;
+  for (int it = 0; it < 64; ++it) {
+    // every thread evaluates the same expressions, so lo, hi stay identical in all
+    const double w = (hi - lo) / (double)(MS_THREADS + 1);
+    const double x = lo + w * (double)(t + 1);
+    const bool above = x > lo && x < hi && sturm_count_lt(d, e, n, x, pivmin) > m;
+    const unsigned up = __ballot_sync(0xffffffffu, above);
+    __syncthreads();  // the previous round's masks have been read
+    if (lane == 0) masks[warp] = up;
+    __syncthreads();
+    // counts grow with the point index: the first point above m
+    int f = MS_THREADS;
+    for (int ww = MS_THREADS / 32 - 1; ww >= 0; --ww)
+      if (masks[ww]) f = 32 * ww + __ffs(masks[ww]) - 1;
+    const double nlo = f == 0 ? lo : lo + w * (double)f;
+    const double nhi = f == MS_THREADS ? hi : lo + w * (double)(f + 1);
+    if (!(nhi - nlo < hi - lo)) break;  // no progress: the bracket is a few ulps wide
+    lo = nlo;
+    hi = nhi;
   }
-  evals[j] = 0.5 * (lo + hi);
+  if (t == 0) evals[j] = 0.5 * (lo + hi);
 }
 
-// Inverse iteration for all nk eigenvectors of T, in descending order, one CTA.
-// Thread 0 runs the pivoted tridiagonal LU and the solves (sequential by
-// nature); the CTA re-orthogonalises against earlier members of the cluster.
-constexpr int IV_THREADS = 256;
+// Eigenvector j of T by inverse iteration, one CTA per eigenvector.  Inside a
+// cluster of close eigenvalues the shifts are separated as dstein does, so each
+// member starts from a distinct shift; the cluster's vectors are made orthonormal
+// and rotated afterwards (cluster_rr_kernel).  Thread 0 runs the pivoted
+// tridiagonal LU of T - shift I (the dgttrf recurrence) and the triangular solves,
+// which are sequential by nature, on arrays in shared memory (or in this CTA's
+// slice of global scratch when n is large); the CTA normalises between iterations.
+constexpr int IV_THREADS = 128;
+constexpr int IV_ITERS = 4;
 
-__global__ void __launch_bounds__(IV_THREADS) inviter_kernel(const double* __restrict__ d, const double* __restrict__ e,
-                                                             int n, int nk, const double* __restrict__ evals,
-                                                             double* __restrict__ Z, double* __restrict__ work) {
+__device__ __forceinline__ double iv_ortol(const double* d, const double* e, int n, double* red) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < n; i += IV_THREADS)
+    t = fmax(t, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < IV_THREADS / 32; ++w) r = fmax(r, red[w]);
+  __syncthreads();
+  return r;
+}
+
+// Shared-memory path: [dl, dd, du, du2, z] (5n doubles) + n pivot bytes.  Global
+// path (large n): this CTA's slice of `scratch`, [dl, dd, du, du2, z, pivot] as 6n
+// doubles; vectors j0 .. j0 + gridDim.x - 1.
+template <bool SMEM>
+__global__ void __launch_bounds__(IV_THREADS) invvec_kernel(const double* __restrict__ d,
+                                                            const double* __restrict__ e, int n, int j0,
+                                                            const double* __restrict__ evals, double* __restrict__ Z,
+                                                            double* __restrict__ scratch) {
+  extern __shared__ __align__(16) double ivs[];
   __shared__ double red[32];
-  __shared__ double s_shift;
-  double* dl = work;          // L multipliers
-  double* dd = work + n;      // U diagonal
-  double* du = work + 2 * n;  // U first super-diagonal
-  double* du2 = work + 3 * n; // U second super-diagonal
-  int* piv = reinterpret_cast<int*>(work + 4 * n);
-  double tnorm = 0.0;
-  for (int i = 0; i < n; ++i)
-    tnorm = fmax(tnorm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0));
+  const int j = j0 + blockIdx.x;
+  double* base = SMEM ? ivs : scratch + (size_t)blockIdx.x * 6 * n;
+  double* dl = base;           // L multipliers
+  double* dd = base + n;       // U diagonal
+  double* du = base + 2 * n;   // U first super-diagonal
+  double* du2 = base + 3 * n;  // U second super-diagonal
+  double* z = base + 4 * n;
+  unsigned char* pivb = reinterpret_cast<unsigned char*>(base + 5 * n);  // SMEM: bytes
+  double* pivd = base + 5 * n;                                           // global: doubles
+  const double tnorm = iv_ortol(d, e, n, red);
   const double ortol = 1e-3 * tnorm;
   const double eps = DBL_EPSILON;
   const double tiny = eps * fmax(tnorm, 1e-300);
-  int cluster_start = 0;
-  double prev_shift = 0.0;
-  for (int j = 0; j < nk; ++j) {
-    double lam = evals[j];
-    if (j > 0 && fabs(evals[j - 1] - lam) > ortol) cluster_start = j;
-    if (j > cluster_start) {
-      // separate identical shifts inside a cluster (dstein's perturbation)
-      const double pert = 10.0 * eps * fmax(fabs(lam), tnorm * 1e-3);
-      if (prev_shift - lam < pert) lam = prev_shift - pert;
+  // the shift of member j: dstein's perturbation applied along its cluster
+  double lam = evals[j];
+  {
+    int c0 = j;
+    while (c0 > 0 && fabs(evals[c0 - 1] - evals[c0]) <= ortol) --c0;
+    double prev = evals[c0];
+    for (int i = c0 + 1; i <= j; ++i) {
+      double li = evals[i];
+      const double pert = 10.0 * eps * fmax(fabs(li), tnorm * 1e-3);
+      if (prev - li < pert) li = prev - pert;
+      prev = li;
     }
-    prev_shift = lam;
-    double* z = Z + (size_t)j * n;
-    // deterministic start vector
-    for (int i = threadIdx.x; i < n; i += IV_THREADS) {
-      unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)((j + 1) * 40503u);
-      h ^= h >> 13;
-      h *= 0x5bd1e995u;
-      h ^= h >> 15;
-      z[i] = ((double)(h & 0xffffff) / 16777216.0) - 0.5;
+    lam = prev;
+  }
+  // deterministic start vector
+  for (int i = threadIdx.x; i < n; i += IV_THREADS) {
+    unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)((j + 1) * 40503u);
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    z[i] = ((double)(h & 0xffffff) / 16777216.0) - 0.5;
+  }
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) {
+      dd[i] = d[i] - lam;
+      du[i] = i < n - 1 ? e[i] : 0.0;
+      dl[i] = i < n - 1 ? e[i] : 0.0;
+      du2[i] = 0.0;
     }
-    if (threadIdx.x == 0) {
-      // LU of T - lam I with partial pivoting (the dgttrf recurrence)
-      for (int i = 0; i < n; ++i) {
-        dd[i] = d[i] - lam;
-        du[i] = i < n - 1 ? e[i] : 0.0;
-        dl[i] = i < n - 1 ? e[i] : 0.0;
+    for (int i = 0; i < n - 1; ++i) {
+      bool sw = false;
+      if (fabs(dd[i]) >= fabs(dl[i])) {
+        if (dd[i] == 0.0) dd[i] = tiny;
+        const double f = dl[i] / dd[i];
+        dl[i] = f;
+        dd[i + 1] -= f * du[i];
         du2[i] = 0.0;
+      } else {
+        const double f = dd[i] / dl[i];
+        dd[i] = dl[i];
+        dl[i] = f;
+        const double t = du[i];
+        du[i] = dd[i + 1];
+        dd[i + 1] = t - f * dd[i + 1];
+        if (i < n - 2) {
+          du2[i] = du[i + 1];
+          du[i + 1] = -f * du[i + 1];
+        }
+        sw = true;
       }
+      if (SMEM) pivb[i] = sw ? 1 : 0;
+      else pivd[i] = sw ? 1.0 : 0.0;
+    }
+    if (dd[n - 1] == 0.0) dd[n - 1] = tiny;
+    for (int i = 0; i < n; ++i)
+      if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
+  }
+  __syncthreads();
+  for (int it = 0; it < IV_ITERS; ++it) {
+    if (threadIdx.x == 0) {
       for (int i = 0; i < n - 1; ++i) {
-        if (fabs(dd[i]) >= fabs(dl[i])) {
-          if (dd[i] == 0.0) dd[i] = tiny;
-          const double f = dl[i] / dd[i];
-          dl[i] = f;
-          dd[i + 1] -= f * du[i];
-          du2[i] = 0.0;
-          piv[i] = i;
+        const bool sw = SMEM ? pivb[i] != 0 : pivd[i] != 0.0;
+        if (!sw) {
+          z[i + 1] -= dl[i] * z[i];
         } else {
-          const double f = dd[i] / dl[i];
-          dd[i] = dl[i];
-          dl[i] = f;
-          const double t = du[i];
-          du[i] = dd[i + 1];
-          dd[i + 1] = t - f * dd[i + 1];
-          if (i < n - 2) {
-            du2[i] = du[i + 1];
-            du[i + 1] = -f * du[i + 1];
-          }
-          piv[i] = i + 1;
+          const double t = z[i];
+          z[i] = z[i + 1];
+          z[i + 1] = t - dl[i] * z[i];
         }
       }
-      if (dd[n - 1] == 0.0) dd[n - 1] = tiny;
-      for (int i = 0; i < n; ++i)
-        if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
+      z[n - 1] /= dd[n - 1];
+      if (n > 1) z[n - 2] = (z[n - 2] - du[n - 2] * z[n - 1]) / dd[n - 2];
+      for (int i = n - 3; i >= 0; --i) z[i] = (z[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) / dd[i];
     }
     __syncthreads();
-    for (int it = 0; it < 4; ++it) {
-      if (threadIdx.x == 0) {
-        for (int i = 0; i < n - 1; ++i) {
-          if (piv[i] == i) {
-            z[i + 1] -= dl[i] * z[i];
-          } else {
-            const double t = z[i];
-            z[i] = z[i + 1];
-            z[i + 1] = t - dl[i] * z[i];
-          }
+    double sq = 0.0;
+    for (int i = threadIdx.x; i < n; i += IV_THREADS) sq += z[i] * z[i];
+    sq = block_sum<IV_THREADS>(sq, red);
+    const double inv = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
+    for (int i = threadIdx.x; i < n; i += IV_THREADS) z[i] *= inv;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += IV_THREADS) Z[(size_t)j * n + i] = z[i];
+}
+
+// Clusters of close eigenvalues (|lambda_{i-1} - lambda_i| <= 1e-3 ||T||, the
+// inverse-iteration cluster rule; on a flat spectrum it chains many members): the
+// members' vectors Z_c are orthonormalised by Cholesky QR applied twice (Gram matrix
+// G = Z_c^T Z_c = L L^T, Z_c <- Z_c L^-T), then rotated by the eigenvectors of the
+// Rayleigh quotient H = Z_c^T T Z_c (cyclic Jacobi), ordered by descending Ritz
+// value, so each member is the eigenvector of its own eigenvalue, not a mixture.
+// The Gram and Rayleigh matrices are formed with one warp per entry pair and every
+// row update is one thread per vector component, so the work is parallel.  A cluster
+// larger than RR_MAXC (the near-zero tail of a rank-deficient TCC), or one whose
+// Gram matrix is not numerically positive definite, is orthonormalised by modified
+// Gram-Schmidt (two passes) instead, without the rotation in the first case.
+// One CTA per cluster: CTA j works only if a cluster starts at j.
+constexpr int RR_THREADS = 256, RR_MAXC = 48;
+
+// y_i = (T z)_i for the symmetric tridiagonal T
+__device__ __forceinline__ double tri_mul(const double* d, const double* e, const double* z, int n, int i) {
+  double y = d[i] * z[i];
+  if (i > 0) y += e[i - 1] * z[i - 1];
+  if (i < n - 1) y += e[i] * z[i + 1];
+  return y;
+}
+
+// S[a][b] = z_a . (T z_b) (withT) or z_a . z_b over the c x c lower triangle, mirrored;
+// one warp per pair
+__device__ void rr_pairs(const double* d, const double* e, const double* Zc, int n, int c, bool withT,
+                         double (*S)[RR_MAXC + 1]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int np = c * (c + 1) / 2;
+  for (int p = warp; p < np; p += RR_THREADS / 32) {
+    int a = (int)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    while (a * (a + 1) / 2 > p) --a;
+    while ((a + 1) * (a + 2) / 2 <= p) ++a;
+    const int b = p - a * (a + 1) / 2;
+    const double* za = Zc + (size_t)a * n;
+    const double* zb = Zc + (size_t)b * n;
+    double sd = 0.0;
+    for (int i = lane; i < n; i += 32) sd += za[i] * (withT ? tri_mul(d, e, zb, n, i) : zb[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    if (lane == 0) {
+      S[a][b] = sd;
+      S[b][a] = sd;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RR_THREADS) cluster_rr_kernel(const double* __restrict__ d,
+                                                                const double* __restrict__ e, int n, int nk,
+                                                                const double* __restrict__ evals,
+                                                                double* __restrict__ Z) {
+  __shared__ double red[32];
+  __shared__ double H[RR_MAXC][RR_MAXC + 1];
+  __shared__ double V[RR_MAXC][RR_MAXC + 1];
+  __shared__ int s_order[RR_MAXC];
+  __shared__ int s_ok;
+  double tn = 0.0;
+  for (int i = threadIdx.x; i < n; i += RR_THREADS)
+    tn = fmax(tn, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tn = fmax(tn, __shfl_xor_sync(0xffffffffu, tn, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tn;
+  __syncthreads();
+  double tnorm = 0.0;
+  for (int w = 0; w < RR_THREADS / 32; ++w) tnorm = fmax(tnorm, red[w]);
+  __syncthreads();
+  const double ortol = 1e-3 * tnorm;
+  const int c0 = blockIdx.x;
+  if (c0 > 0 && fabs(evals[c0 - 1] - evals[c0]) <= ortol) return;  // not a cluster start
+  int c1 = c0 + 1;
+  while (c1 < nk && fabs(evals[c1 - 1] - evals[c1]) <= ortol) ++c1;
+  const int c = c1 - c0;
+  if (c < 2) return;
+  double* Zc = Z + (size_t)c0 * n;
+  bool ok = c <= RR_MAXC;
+  // Cholesky QR, twice
+  for (int pass = 0; ok && pass < 2; ++pass) {
+    rr_pairs(d, e, Zc, n, c, false, H);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_ok = 1;
+      for (int a = 0; a < c && s_ok; ++a) {  // H <- L (lower), in place
+        double diag = H[a][a];
+        for (int b = 0; b < a; ++b) diag -= H[a][b] * H[a][b];
+        if (!(diag > 1e-24)) {
+          s_ok = 0;
+          break;
         }
-        z[n - 1] /= dd[n - 1];
-        if (n > 1) z[n - 2] = (z[n - 2] - du[n - 2] * z[n - 1]) / dd[n - 2];
-        for (int i = n - 3; i >= 0; --i) z[i] = (z[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) / dd[i];
+        H[a][a] = sqrt(diag);
+        for (int r = a + 1; r < c; ++r) {
+          double v = H[r][a];
+          for (int b = 0; b < a; ++b) v -= H[r][b] * H[a][b];
+          H[r][a] = v / H[a][a];
+        }
       }
-      __syncthreads();
-      // re-orthogonalise against the earlier members of the cluster (twice)
-      for (int pass = 0; pass < 2; ++pass)
-        for (int c = cluster_start; c < j; ++c) {
-          const double* zc = Z + (size_t)c * n;
-          double s = 0.0;
-          for (int i = threadIdx.x; i < n; i += IV_THREADS) s += zc[i] * z[i];
-          s = block_sum<IV_THREADS>(s, red);
-          for (int i = threadIdx.x; i < n; i += IV_THREADS) z[i] -= s * zc[i];
+    }
+    __syncthreads();
+    ok = s_ok != 0;
+    if (!ok) break;
+    // z_i <- L^-1 z_i for every component i (forward substitution)
+    for (int i = threadIdx.x; i < n; i += RR_THREADS) {
+      double y[RR_MAXC];
+      for (int a = 0; a < c; ++a) {
+        double v = Zc[(size_t)a * n + i];
+        for (int b = 0; b < a; ++b) v -= H[a][b] * y[b];
+        y[a] = v / H[a][a];
+      }
+      for (int a = 0; a < c; ++a) Zc[(size_t)a * n + i] = y[a];
+    }
+    __syncthreads();
+  }
+  if (!ok) {  // modified Gram-Schmidt, two passes
+    for (int pass = 0; pass < 2; ++pass)
+      for (int a = 0; a < c; ++a) {
+        double* za = Zc + (size_t)a * n;
+        for (int b = 0; b < a; ++b) {
+          const double* zb = Zc + (size_t)b * n;
+          double sd = 0.0;
+          for (int i = threadIdx.x; i < n; i += RR_THREADS) sd += zb[i] * za[i];
+          sd = block_sum<RR_THREADS>(sd, red);
+          for (int i = threadIdx.x; i < n; i += RR_THREADS) za[i] -= sd * zb[i];
           __syncthreads();
         }
-      double s = 0.0;
-      for (int i = threadIdx.x; i < n; i += IV_THREADS) s += z[i] * z[i];
-      s = block_sum<IV_THREADS>(s, red);
-      const double inv = s > 0.0 ? 1.0 / sqrt(s) : 0.0;
-      for (int i = threadIdx.x; i < n; i += IV_THREADS) z[i] *= inv;
-      __syncthreads();
+        double sq = 0.0;
+        for (int i = threadIdx.x; i < n; i += RR_THREADS) sq += za[i] * za[i];
+        sq = block_sum<RR_THREADS>(sq, red);
+        const double inv = sq > 0.0 ? 1.0 / sqrt(sq) : 0.0;
+        for (int i = threadIdx.x; i < n; i += RR_THREADS) za[i] *= inv;
+        __syncthreads();
+      }
+    if (c > RR_MAXC) return;
+  }
+  // Rayleigh-Ritz: H = Z_c^T T Z_c
+  rr_pairs(d, e, Zc, n, c, true, H);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // cyclic Jacobi on the c x c symmetric H; V accumulates the rotations
+    for (int a = 0; a < c; ++a)
+      for (int b = 0; b < c; ++b) V[a][b] = a == b ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+      double off = 0.0, dia = 0.0;
+      for (int a = 0; a < c; ++a) {
+        dia += H[a][a] * H[a][a];
+        for (int b = a + 1; b < c; ++b) off += H[a][b] * H[a][b];
+      }
+      if (off <= 1e-32 * dia) break;
+      for (int p = 0; p < c - 1; ++p)
+        for (int q = p + 1; q < c; ++q) {
+          const double apq = H[p][q];
+          if (apq == 0.0) continue;
+          const double theta = (H[q][q] - H[p][p]) / (2.0 * apq);
+          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          for (int k = 0; k < c; ++k) {  // H <- J^T H J
+            const double hkp = H[k][p], hkq = H[k][q];
+            H[k][p] = cs * hkp - sn * hkq;
+            H[k][q] = sn * hkp + cs * hkq;
+          }
+          for (int k = 0; k < c; ++k) {
+            const double hpk = H[p][k], hqk = H[q][k];
+            H[p][k] = cs * hpk - sn * hqk;
+            H[q][k] = sn * hpk + cs * hqk;
+          }
+          for (int k = 0; k < c; ++k) {
+            const double vkp = V[k][p], vkq = V[k][q];
+            V[k][p] = cs * vkp - sn * vkq;
+            V[k][q] = sn * vkp + cs * vkq;
+          }
+        }
     }
-    (void)s_shift;
+    // descending Ritz values
+    for (int a = 0; a < c; ++a) s_order[a] = a;
+    for (int a = 1; a < c; ++a) {
+      const int key = s_order[a];
+      int b = a - 1;
+      while (b >= 0 && H[s_order[b]][s_order[b]] < H[key][key]) {
+        s_order[b + 1] = s_order[b];
+        --b;
+      }
+      s_order[b + 1] = key;
+    }
+  }
+  __syncthreads();
+  // Z_c <- Z_c V (columns in descending Ritz order), one thread per component
+  for (int i = threadIdx.x; i < n; i += RR_THREADS) {
+    double x[RR_MAXC];
+    for (int b = 0; b < c; ++b) x[b] = Zc[(size_t)b * n + i];
+    for (int a = 0; a < c; ++a) {
+      const int col = s_order[a];
+      double acc = 0.0;
+      for (int b = 0; b < c; ++b) acc += x[b] * V[b][col];
+      Zc[(size_t)a * n + i] = acc;
+    }
   }
 }
 
 // y = H_0 H_1 ... H_{n-2} z for eigenvector j = blockIdx.x; H_k = I - tau_k v_k v_k^H
-// acting on rows k+1..n-1, v_k stored in A column k.
-__global__ void __launch_bounds__(256) backtransform_kernel(const double2* __restrict__ A, int n,
+// acting on rows k+1..n-1, v_k packed contiguously in vpack.
+__global__ void __launch_bounds__(256) backtransform_kernel(const double2* __restrict__ vpack, int n,
                                                             const double2* __restrict__ tau,
                                                             const double* __restrict__ Z, double2* __restrict__ Y) {
   __shared__ double red[32];
@@ -331,19 +690,19 @@ __global__ void __launch_bounds__(256) backtransform_kernel(const double2* __res
   __syncthreads();
   for (int k = n - 2; k >= 0; --k) {
     const int m = n - k - 1;
+    const double2* v = vpack + vpack_off(n, k);
     double sr = 0.0, si = 0.0;
     for (int i = threadIdx.x; i < m; i += 256) {
-      const double2 v = A[(size_t)(k + 1 + i) * n + k];
+      const double2 vv = v[i];
       const double2 yy = y[k + 1 + i];
-      sr += v.x * yy.x + v.y * yy.y;  // conj(v) * y
-      si += v.x * yy.y - v.y * yy.x;
+      sr += vv.x * yy.x + vv.y * yy.y;  // conj(v) * y
+      si += vv.x * yy.y - vv.y * yy.x;
     }
     sr = block_sum<256>(sr, red);
     si = block_sum<256>(si, red);
     const double2 f = zmul(tau[k], make_double2(sr, si));
     for (int i = threadIdx.x; i < m; i += 256) {
-      const double2 v = A[(size_t)(k + 1 + i) * n + k];
-      const double2 p = zmul(f, v);
+      const double2 p = zmul(f, v[i]);
       y[k + 1 + i].x -= p.x;
       y[k + 1 + i].y -= p.y;
     }
@@ -384,11 +743,18 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   const void* dtcc = nullptr;
   LITHO_RET(stage_in(ctx, ctx->tcc_c, tcc, nn * sizeof(double2), mem, &dtcc));
   LITHO_RET(ctx->eig_v.ensure(ctx, nn * sizeof(double2)));
-  // workspace: vbuf, xbuf, tau (n double2 each); d, e (n double); evals (nk);
-  // Z (nk*n double); LU scratch (5n double); Y (nk*n double2)
-  const size_t wbytes = 3 * n * sizeof(double2) + 2 * n * sizeof(double) + nk * sizeof(double) +
-                        (size_t)nk * n * sizeof(double) + 5 * n * sizeof(double) + (size_t)nk * n * sizeof(double2) +
-                        16 * 64;
+  // workspace: vbuf, xbuf, tau (n double2 each); packed reflectors (n(n-1)/2
+  // double2); per-CTA partial dots ((n+7)/8 double2); d, e (n double); evals (nk);
+  // Z (nk*n double); inverse-iteration scratch (large n only: IV_CHUNK * 6n double);
+  // Y (nk*n double2)
+  const size_t iv_smem = (size_t)5 * n * sizeof(double) + n;
+  const bool iv_in_smem = iv_smem <= 200 * 1024;
+  constexpr int IV_CHUNK = 64;
+  const size_t iv_scratch = iv_in_smem ? 0 : (size_t)IV_CHUNK * 6 * n * sizeof(double);
+  const size_t vpack_bytes = (size_t)n * (n - 1) / 2 * sizeof(double2) + sizeof(double2);
+  const size_t part_bytes = (size_t)((n + 7) / 8) * sizeof(double2);
+  const size_t wbytes = 3 * n * sizeof(double2) + vpack_bytes + part_bytes + 2 * n * sizeof(double) + nk * sizeof(double) +
+                        (size_t)nk * n * sizeof(double) + iv_scratch + (size_t)nk * n * sizeof(double2) + 16 * 64;
   LITHO_RET(ctx->eig_work.ensure(ctx, wbytes));
   char* w = ctx->eig_work.as<char>();
   auto take = [&](size_t b) {
@@ -399,30 +765,43 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   double2* vbuf = reinterpret_cast<double2*>(take(n * sizeof(double2)));
   double2* xbuf = reinterpret_cast<double2*>(take(n * sizeof(double2)));
   double2* tau = reinterpret_cast<double2*>(take(n * sizeof(double2)));
+  double2* vpack = reinterpret_cast<double2*>(take(vpack_bytes));
+  double2* part = reinterpret_cast<double2*>(take(part_bytes));
   double* d = reinterpret_cast<double*>(take(n * sizeof(double)));
   double* e = reinterpret_cast<double*>(take(n * sizeof(double)));
   double* ev = reinterpret_cast<double*>(take(nk * sizeof(double)));
   double* Z = reinterpret_cast<double*>(take((size_t)nk * n * sizeof(double)));
-  double* lu = reinterpret_cast<double*>(take(5 * n * sizeof(double)));
+  double* ivs = iv_in_smem ? nullptr : reinterpret_cast<double*>(take(iv_scratch));
   double2* Y = reinterpret_cast<double2*>(take((size_t)nk * n * sizeof(double2)));
   double2* A = ctx->eig_v.as<double2>();
   {
-    StageScope sc(ctx, LITHO_STAGE_EIG, 4 * (n > 1 ? n - 1 : 0) + 5);
+    // hermitize, 2 per reflector, last diagonal, multisection, inverse iteration
+    // (one launch, or one per chunk of IV_CHUNK vectors), cluster Rayleigh-Ritz, back-transform
+    const int iv_launches = iv_in_smem ? 1 : (nk + IV_CHUNK - 1) / IV_CHUNK;
+    StageScope sc(ctx, LITHO_STAGE_EIG, 2 * (n > 1 ? n - 1 : 0) + 5 + iv_launches);
     hermitize_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(static_cast<const double2*>(dtcc), A, n);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     LITHO_CUDA_TRY(ctx, cudaMemsetAsync(e, 0, n * sizeof(double), ctx->stream));
     for (int k = 0; k + 1 < n; ++k) {
       const int m = n - k - 1;
-      hh_kernel<<<1, 256, 0, ctx->stream>>>(A, n, k, vbuf, tau, d, e);
-      symv_kernel<<<(m + 7) / 8, 256, 0, ctx->stream>>>(A, n, k, vbuf, tau, xbuf);
-      wdot_kernel<<<1, 256, 0, ctx->stream>>>(n, k, vbuf, xbuf, tau);
-      her2_kernel<<<dim3((m + 31) / 32, (m + 31) / 32), 256, 0, ctx->stream>>>(A, n, k, vbuf, xbuf);
+      const int nb = (m + 7) / 8;
+      symv_hh_kernel<<<nb, 256, 0, ctx->stream>>>(A, n, k, vbuf, vpack, tau, d, e, xbuf, part);
+      const int nt = (m + 31) / 32;
+      her2_kernel<<<nt * (nt + 1) / 2, 256, 0, ctx->stream>>>(A, n, k, vbuf, xbuf, tau, part, nb);
     }
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     last_diag_kernel<<<1, 32, 0, ctx->stream>>>(A, n, d);
-    bisect_kernel<<<(nk + 63) / 64, 64, 0, ctx->stream>>>(d, e, n, nk, ev);
-    inviter_kernel<<<1, IV_THREADS, 0, ctx->stream>>>(d, e, n, nk, ev, Z, lu);
-    backtransform_kernel<<<nk, 256, 0, ctx->stream>>>(A, n, tau, Z, Y);
+    multisect_kernel<<<nk, MS_THREADS, 0, ctx->stream>>>(d, e, n, nk, ev);
+    if (iv_in_smem) {
+      LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(invvec_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)iv_smem));
+      invvec_kernel<true><<<nk, IV_THREADS, iv_smem, ctx->stream>>>(d, e, n, 0, ev, Z, nullptr);
+    } else {
+      for (int j0 = 0; j0 < nk; j0 += IV_CHUNK)
+        invvec_kernel<false><<<std::min(IV_CHUNK, nk - j0), IV_THREADS, 0, ctx->stream>>>(d, e, n, j0, ev, Z, ivs);
+    }
+    cluster_rr_kernel<<<nk, RR_THREADS, 0, ctx->stream>>>(d, e, n, nk, ev, Z);
+    backtransform_kernel<<<nk, 256, 0, ctx->stream>>>(vpack, n, tau, Z, Y);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   float *okr = krn_r, *oki = krn_i, *osc = scales;
