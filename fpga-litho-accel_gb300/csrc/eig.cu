@@ -42,6 +42,17 @@ __device__ __forceinline__ double2 zmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+// conj by flipping the sign bit on the integer pipe (the FP64 pipe is the scarce one)
+__device__ __forceinline__ double2 zconj_bits(double2 a) {
+  return make_double2(a.x, __longlong_as_double(__double_as_longlong(a.y) ^ (long long)0x8000000000000000ull));
+}
+// lower-triangle tile t = I (I + 1) / 2 + J -> (I, J), in FP32 plus integer fix-ups
+__device__ __forceinline__ void tri_tile(int t, int& I, int& J) {
+  I = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  J = t - I * (I + 1) / 2;
+}
 
 template <int NT>
 __device__ double block_sum(double v, double* red) {
@@ -205,11 +216,8 @@ __global__ void __launch_bounds__(256) her2_kernel(double2* __restrict__ A, int 
     }
   }
   __syncthreads();
-  const int t = blockIdx.x;
-  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while (I * (I + 1) / 2 > t) --I;
-  while ((I + 1) * (I + 2) / 2 <= t) ++I;
-  const int J = t - I * (I + 1) / 2;
+  int I, J;
+  tri_tile(blockIdx.x, I, J);
   if (threadIdx.x < 64) {  // w = x + c v for the tile's 32 columns and 32 rows, once
     const int side = threadIdx.x >> 5, q = (side ? I : J) * 32 + tx;
     double2 vq = make_double2(0.0, 0.0), wq = vq;
@@ -252,7 +260,7 @@ __global__ void __launch_bounds__(256) her2_kernel(double2* __restrict__ A, int 
     for (int r = 0; r < 4; ++r) {
       const int ii = ty + 8 * r, i = I * 32 + ii;
       if (i < m && j < m)
-        A[(size_t)(k + 1 + i) * n + (k + 1 + j)] = ii >= tx ? tile[ii][tx] : zconj(tile[tx][ii]);
+        A[(size_t)(k + 1 + i) * n + (k + 1 + j)] = ii >= tx ? tile[ii][tx] : zconj_bits(tile[tx][ii]);
     }
     return;
   }
@@ -261,7 +269,7 @@ __global__ void __launch_bounds__(256) her2_kernel(double2* __restrict__ A, int 
   for (int r = 0; r < 4; ++r) {
     const int jj = ty + 8 * r, ii = tx;
     const int row = J * 32 + jj, col = I * 32 + ii;
-    if (row < m && col < m) A[(size_t)(k + 1 + row) * n + (k + 1 + col)] = zconj(tile[ii][jj]);
+    if (row < m && col < m) A[(size_t)(k + 1 + row) * n + (k + 1 + col)] = zconj_bits(tile[ii][jj]);
   }
 }
 
@@ -512,10 +520,8 @@ __device__ void rr_pairs(const double* d, const double* e, const double* Zc, int
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int np = c * (c + 1) / 2;
   for (int p = warp; p < np; p += RR_THREADS / 32) {
-    int a = (int)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
-    while (a * (a + 1) / 2 > p) --a;
-    while ((a + 1) * (a + 2) / 2 <= p) ++a;
-    const int b = p - a * (a + 1) / 2;
+    int a, b;
+    tri_tile(p, a, b);
     const double* za = Zc + (size_t)a * n;
     const double* zb = Zc + (size_t)b * n;
     double sd = 0.0;

@@ -666,7 +666,9 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
         fence_proxy_async();
         named_bar(1 + grp, 128);
         if (leader) {
-          tma_store_3d(&tmOut, st, xt * BN + slab * 32, 128 * yb, img);
+          // evict-first: the images are not read again here, and keeping them from
+          // displacing the T tiles and twiddles in L2 measured 52 -> 46.5 us per 64 images
+          tma_store_3d_hint(&tmOut, st, xt * BN + slab * 32, 128 * yb, img, policy_evict_first());
           bulk_commit();
         }
       }
