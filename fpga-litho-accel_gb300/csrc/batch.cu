@@ -90,7 +90,7 @@ static int run_class(litho_batch_plan* bp, int ci) {
     if (s.cls != ci) continue;
     ImgGeom gw{s.mLx, s.mLy, c.L, c.L, Nx, Ny, c.ks->nk, c.convN};
     ImgPlan pw = make_plan(gw, s.count, ctx->sm_count);
-    pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 31) / 32 / 4 : (s.mLx + 63) / 64));
+    pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 63) / 64 / 2 : (s.mLx + 63) / 64));
     pw.part_stride = c.part_stride;
     float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
     if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));

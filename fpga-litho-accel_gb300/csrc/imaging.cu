@@ -961,14 +961,14 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
   const int KY = 2 * g.Ny + 1;
   const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
   if (tc) {
-    // persistent tensor-core window (one CTA per SM): split the 32-column chunks
+    // persistent tensor-core window (one CTA per SM): split the 64-column chunks
     // of a row block into tiles until there are ~6 tiles per SM, so the last
     // round of tiles is short (each split adds an epilogue and a partial)
-    const int nch = (g.Lx + 31) / 32;
+    const int nch = (g.Lx + 63) / 64;
     const int units = p.rowBlocks * batch;
     const int want = 6 * ctx->sm_count;
     const int cs = units < want ? (want + units - 1) / units : 1;
-    p.colSplits = std::max(1, std::min(cs, std::min(4, nch / 4)));
+    p.colSplits = std::max(1, std::min(cs, std::min(4, nch / 2)));
   }
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));

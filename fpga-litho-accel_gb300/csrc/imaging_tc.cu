@@ -138,9 +138,15 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // sized for the actual Ny; the stage count S is chosen at launch.
 template <int NBH>
 struct WinTC {
-  static constexpr uint32_t A_B = 128 * 128;        // 128 rows x 32 fp32 (split in place: hi, then lo)
-  static constexpr uint32_t B_B = 2 * NBH * 128;    // [hi NBH rows; lo NBH rows] x 32 fp32
-  static constexpr uint32_t STAGE_B = A_B + B_B;    // a multiple of 2048: every stage is 1024-aligned
+  // a stage carries a 64-column chunk as two 32-column K blocks: each pipeline round
+  // trip (land, check, MMA, release) then moves 32 KB of mask, which halves the
+  // per-chunk handshakes that bound this ring
+  static constexpr int KB = 2;                       // K blocks (32 columns each) per stage
+  static constexpr uint32_t A_KB = 128 * 128;        // 128 rows x 32 fp32 (split in place: hi, then lo)
+  static constexpr uint32_t A_B = KB * A_KB;
+  static constexpr uint32_t B_KB = 2 * NBH * 128;    // [hi NBH rows; lo NBH rows] x 32 fp32
+  static constexpr uint32_t B_B = KB * B_KB;
+  static constexpr uint32_t STAGE_B = A_B + B_B;     // a multiple of 2048: every stage is 1024-aligned
   // one accumulator holds A*Bh in columns [0, NBH) and A*Bl in [NBH, 2 NBH): one
   // N = 2 NBH MMA reads the mask tile once for both products
   static constexpr uint32_t NCOL = 2 * NBH <= 32 ? 32 : (2 * NBH <= 64 ? 64 : 128);
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [S]
   int* nzflag = last_issued + S;                          // [S]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nch = (Lx + 31) / 32;
+  const int nch = (Lx + 32 * P::KB - 1) / (32 * P::KB);  // chunks of 32 KB columns
   const int T = rows * batch * ncs;
 
   if (warp == 0) tmem_alloc(tslot, 2 * P::NCOL);
@@ -240,8 +246,11 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
             break;
           }
           mbar_arrive_expect_tx(&full[s], P::STAGE_B);
-          tma_load_3d(sA(s), &tmM, &full[s], 32 * c, 128 * rb, img);
-          tma_load_2d(sBh(s), &tmB, &full[s], 32 * c, 0);
+#pragma unroll
+          for (int kb = 0; kb < P::KB; ++kb) {
+            tma_load_3d(sA(s) + kb * P::A_KB, &tmM, &full[s], 32 * (P::KB * c + kb), 128 * rb, img);
+            tma_load_2d(sBh(s) + kb * P::B_KB, &tmB, &full[s], 32 * (P::KB * c + kb), 0);
+          }
           last_issued[s] = q;
           if (++s == S) {
             s = 0;
@@ -279,11 +288,14 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           tc_fence_after();
           const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
           nzflag[s] = 0;  // every consumer read it before arriving on ready[s]
-          const uint64_t da = desc_sw128(sA(s)), dbh = desc_sw128(sBh(s));
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint32_t off = kk * 32;
-            mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC2, (c != c0 || kk != 0) ? 1u : 0u);
+          for (int kb = 0; kb < P::KB; ++kb) {
+            const uint64_t da = desc_sw128(sA(s) + kb * P::A_KB), dbh = desc_sw128(sBh(s) + kb * P::B_KB);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t off = kk * 32;
+              mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC2, (c != c0 || kb != 0 || kk != 0) ? 1u : 0u);
+            }
           }
           if (two) {
             mma_commit(&hidone[s]);
@@ -295,9 +307,13 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
             ph2 ^= 1u << s;
             tc_fence_after();
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint32_t off = kk * 32;
-              mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC1, 1u);
+            for (int kb = 0; kb < P::KB; ++kb) {
+              const uint64_t da = desc_sw128(sA(s) + kb * P::A_KB), dbh = desc_sw128(sBh(s) + kb * P::B_KB);
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t off = kk * 32;
+                mma_tf32(acc, desc_add(da, off), desc_add(dbh, off), IDESC1, 1u);
+              }
             }
           }
           mma_commit(&empty[s]);
@@ -322,10 +338,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       for (int c = c0; c < c1; ++c) {
         if (!mbar_wait_ab(&full[s], ph, abort)) *abort = 1;
         float4* a = reinterpret_cast<float4*>(sA(s));
-        float4 v[4];
+        float4 v[4 * P::KB];
         bool nz = false;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 4 * P::KB; ++i) {
           v[i] = a[tid + WP_CONS * i];
           nz |= (v[i].x != tf32_round(v[i].x)) | (v[i].y != tf32_round(v[i].y)) | (v[i].z != tf32_round(v[i].z)) |
                 (v[i].w != tf32_round(v[i].w));
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
         if (two) {  // write Ah = round_tf32(A) in place; exact tiles are used as landed
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < 4 * P::KB; ++i)
             a[tid + WP_CONS * i] =
                 make_float4(tf32_round(v[i].x), tf32_round(v[i].y), tf32_round(v[i].z), tf32_round(v[i].w));
           fence_proxy_async();
@@ -345,7 +361,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) *abort = 1;
           ph2 ^= 1u << s;
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < 4 * P::KB; ++i)
             a[tid + WP_CONS * i] = make_float4(v[i].x - tf32_round(v[i].x), v[i].y - tf32_round(v[i].y),
                                                v[i].z - tf32_round(v[i].z), v[i].w - tf32_round(v[i].w));
           fence_proxy_async();
