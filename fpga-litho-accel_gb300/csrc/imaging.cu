@@ -704,8 +704,10 @@ ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count) {
   int cs = (want + p.rowBlocks * batch - 1) / (p.rowBlocks * batch);
   cs = std::max(1, std::min(cs, std::max(1, nch / 2)));
   p.colSplits = cs;
-  // SOCS is latency-bound (warp-shuffle FFT chains): aim for >= 4 CTAs (32 warps) per SM
-  int ng = (4 * sm_count + batch - 1) / batch;
+  // SOCS is latency-bound (warp-shuffle FFT chains), but every kernel group also
+  // transforms its own partial intensity: ~2.5 CTAs (20 warps) per SM measured best
+  // at 1024^2, K=24, 64 masks (4 kernels per CTA: 36.9 us; 3: 38.9; 8: 45.0)
+  int ng = (5 * sm_count + 2 * batch - 1) / (2 * batch);
   ng = std::max(1, std::min(ng, g.nk));
   p.kpg = (g.nk + ng - 1) / ng;
   p.ngroups = (g.nk + p.kpg - 1) / p.kpg;
