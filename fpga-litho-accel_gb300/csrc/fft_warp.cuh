@@ -55,14 +55,18 @@ __device__ __forceinline__ void warp_fft_dif(float2 (&x)[N / 32], const float2* 
       }
     }
   }
+  // shuffle stages, branch-free: with s = +1 (top) / -1 (bottom) and w' = 1 (top) /
+  // w (bottom), both halves are (s x + p) w': two FMAs and a complex product per
+  // element instead of both butterfly halves and a select
 #pragma unroll
   for (int h = 16; h >= 1; h >>= 1) {
     const bool bottom = (lane & h) != 0;
-    const float2 w = twid<INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+    const float s = bottom ? -1.f : 1.f;
+    const float2 w = bottom ? twid<INV>(tw, (lane & (h - 1)) * (N / (2 * h))) : make_float2(1.f, 0.f);
 #pragma unroll
     for (int j = 0; j < J; ++j) {
       const float2 p = shfl_xor2(x[j], h);
-      x[j] = bottom ? cmul(csub(p, x[j]), w) : cadd(x[j], p);
+      x[j] = cmul(make_float2(fmaf(s, x[j].x, p.x), fmaf(s, x[j].y, p.y)), w);
     }
   }
 }
@@ -70,14 +74,19 @@ __device__ __forceinline__ void warp_fft_dif(float2 (&x)[N / 32], const float2* 
 template <int N, bool INV>
 __device__ __forceinline__ void warp_fft_dit(float2 (&x)[N / 32], const float2* __restrict__ tw, int lane) {
   constexpr int J = N / 32;
+  // shuffle stages, branch-free: the bottom lane pre-multiplies its element by w
+  // (the top lane by 1) before the exchange; then both halves are s z + p_z with
+  // s = +1 (top) / -1 (bottom)
 #pragma unroll
   for (int h = 1; h <= 16; h <<= 1) {
     const bool bottom = (lane & h) != 0;
-    const float2 w = twid<INV>(tw, (lane & (h - 1)) * (N / (2 * h)));
+    const float s = bottom ? -1.f : 1.f;
+    const float2 w = bottom ? twid<INV>(tw, (lane & (h - 1)) * (N / (2 * h))) : make_float2(1.f, 0.f);
 #pragma unroll
     for (int j = 0; j < J; ++j) {
-      const float2 p = shfl_xor2(x[j], h);
-      x[j] = bottom ? csub(p, cmul(w, x[j])) : cadd(x[j], cmul(w, p));
+      const float2 z = cmul(w, x[j]);
+      const float2 p = shfl_xor2(z, h);
+      x[j] = make_float2(fmaf(s, z.x, p.x), fmaf(s, z.y, p.y));
     }
   }
 #pragma unroll

@@ -440,17 +440,30 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
   float* out = KMAJ ? nullptr : tm + (size_t)img * (4 * Ny + 1) * Lx;
   for (int fy = fy0; fy < fy1; ++fy) {
     const float4* C = sC + fy * MAXD;
-    float re = C[0].x, im = C[0].y;
+    // four independent FMA chains; without the term guard when 2Nx+1 is the table width
+    float ra = C[0].x, rb = 0.f, ia = C[0].y, ib = 0.f;
+    if (ND == MAXD) {
 #pragma unroll
-    for (int d = 1; d < MAXD; ++d) {
-      if (d < ND) {
+      for (int d = 1; d < MAXD; ++d) {
         const float4 a = C[d];
-        re = fmaf(a.x, tw[d].x, re);
-        re = fmaf(-a.y, tw[d].y, re);
-        im = fmaf(a.z, tw[d].x, im);
-        im = fmaf(a.w, tw[d].y, im);
+        ra = fmaf(a.x, tw[d].x, ra);
+        rb = fmaf(-a.y, tw[d].y, rb);
+        ia = fmaf(a.z, tw[d].x, ia);
+        ib = fmaf(a.w, tw[d].y, ib);
+      }
+    } else {
+#pragma unroll
+      for (int d = 1; d < MAXD; ++d) {
+        if (d < ND) {
+          const float4 a = C[d];
+          ra = fmaf(a.x, tw[d].x, ra);
+          rb = fmaf(-a.y, tw[d].y, rb);
+          ia = fmaf(a.z, tw[d].x, ia);
+          ib = fmaf(a.w, tw[d].y, ib);
+        }
       }
     }
+    const float re = ra + rb, im = ia + ib;
     if (!live) continue;
     if (KMAJ) {
       if (fy == 0) {
