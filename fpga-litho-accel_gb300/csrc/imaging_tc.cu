@@ -154,13 +154,17 @@ struct WinTC {
 };
 constexpr int WP_THREADS = 448;  // warps 0-7 split, 8 TMA, 9 MMA, 10-13 epilogue
 constexpr int WP_CONS = 256;     // consumer threads
-constexpr int WP_RS = 129;       // padded row stride of the epilogue buffers
+// padded row strides of the epilogue buffers: multiples of 4 floats so the row DFT
+// reads 16-byte vectors, and 33 / 65 float4 slots apart so the threads of a warp
+// (different u, different |v|) land in different bank groups
+constexpr int WP_RSR = 132;      // sR rows (fp32)
+constexpr int WP_RST = 130;      // sRT rows (float2)
 constexpr int WP_MAX_STAGES = 12;
 constexpr size_t WP_SMEM_CAP = 227 * 1024;
 
-// epilogue buffers: sR [NBH][RS] fp32 + sRT [Ny+1][RS] float2
+// epilogue buffers: sR [NBH][RSR] fp32 + sRT [Ny+1][RST] float2
 static inline size_t win_epi_bytes(int NBH, int Ny) {
-  return (size_t)NBH * WP_RS * 4 + (size_t)(Ny + 1) * WP_RS * 8;
+  return (size_t)NBH * WP_RSR * 4 + (size_t)(Ny + 1) * WP_RST * 8;
 }
 // mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES)
 static inline size_t win_bar_bytes(int S) { return (size_t)(5 * S + 5) * 8 + 16 + 8 * (size_t)S; }
@@ -176,10 +180,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  constexpr int RS = WP_RS;  // padded row stride: per-thread row walks hit distinct banks
+  constexpr int RS = WP_RSR, RT = WP_RST;
   float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [NBH][RS]
-  float2* sRT = reinterpret_cast<float2*>(sR + NBH * RS);             // [Ny+1][RS]
-  uint64_t* full = reinterpret_cast<uint64_t*>(sRT + (Ny + 1) * RS);
+  float2* sRT = reinterpret_cast<float2*>(sR + NBH * RS);             // [Ny+1][RT]
+  uint64_t* full = reinterpret_cast<uint64_t*>(sRT + (Ny + 1) * RT);
   uint64_t* ready = full + S;
   uint64_t* hidone = ready + S;
   uint64_t* ready2 = hidone + S;
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       const int y0 = 128 * rb;
       for (int i = etid; i < (Ny + 1) * 128; i += 128) {
         const int v = i >> 7, r = i & 127, y = y0 + r;
-        sRT[v * RS + r] = y < Ly ? ytab[(size_t)v * Ly + y] : make_float2(0.f, 0.f);
+        sRT[v * RT + r] = y < Ly ? ytab[(size_t)v * Ly + y] : make_float2(0.f, 0.f);
       }
       named_bar(2, 128);
       const int nps = part_stride > 0 ? part_stride : rows * ncs;
@@ -412,27 +416,43 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       // with c, s the cos / -sin accumulator columns of u (s = 0 for u = 0)
       for (int pq = etid; pq < (Ny + 1) * NU; pq += 128) {
         const int av = pq / NU, u = pq - av * NU;
-        const float* rc = sR + u * RS;
-        const float* rs = sR + (Nx + u) * RS;
-        const float2* rt = sRT + av * RS;
+        const float4* rc = reinterpret_cast<const float4*>(sR + u * RS);
+        const float4* rs = reinterpret_cast<const float4*>(sR + (Nx + u) * RS);
+        const float4* rt = reinterpret_cast<const float4*>(sRT + av * RT);  // two rows' twiddles per vector
         float s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
         if (u == 0) {
-#pragma unroll 8
-          for (int r = 0; r < 128; ++r) {
-            const float2 tw = rt[r];
-            const float c = rc[r];
-            s1 = fmaf(c, tw.x, s1);
-            s3 = fmaf(c, tw.y, s3);
+#pragma unroll 4
+          for (int r4 = 0; r4 < 32; ++r4) {
+            const float4 c = rc[r4], ta = rt[2 * r4], tb = rt[2 * r4 + 1];
+            s1 = fmaf(c.x, ta.x, s1);
+            s3 = fmaf(c.x, ta.y, s3);
+            s1 = fmaf(c.y, ta.z, s1);
+            s3 = fmaf(c.y, ta.w, s3);
+            s1 = fmaf(c.z, tb.x, s1);
+            s3 = fmaf(c.z, tb.y, s3);
+            s1 = fmaf(c.w, tb.z, s1);
+            s3 = fmaf(c.w, tb.w, s3);
           }
         } else {
-#pragma unroll 8
-          for (int r = 0; r < 128; ++r) {
-            const float2 tw = rt[r];
-            const float c = rc[r], sn = rs[r];
-            s1 = fmaf(c, tw.x, s1);
-            s2 = fmaf(sn, tw.y, s2);
-            s3 = fmaf(c, tw.y, s3);
-            s4 = fmaf(sn, tw.x, s4);
+#pragma unroll 4
+          for (int r4 = 0; r4 < 32; ++r4) {
+            const float4 c = rc[r4], sn = rs[r4], ta = rt[2 * r4], tb = rt[2 * r4 + 1];
+            s1 = fmaf(c.x, ta.x, s1);
+            s2 = fmaf(sn.x, ta.y, s2);
+            s3 = fmaf(c.x, ta.y, s3);
+            s4 = fmaf(sn.x, ta.x, s4);
+            s1 = fmaf(c.y, ta.z, s1);
+            s2 = fmaf(sn.y, ta.w, s2);
+            s3 = fmaf(c.y, ta.w, s3);
+            s4 = fmaf(sn.y, ta.z, s4);
+            s1 = fmaf(c.z, tb.x, s1);
+            s2 = fmaf(sn.z, tb.y, s2);
+            s3 = fmaf(c.z, tb.y, s3);
+            s4 = fmaf(sn.z, tb.x, s4);
+            s1 = fmaf(c.w, tb.z, s1);
+            s2 = fmaf(sn.w, tb.w, s2);
+            s3 = fmaf(c.w, tb.w, s3);
+            s4 = fmaf(sn.w, tb.z, s4);
           }
         }
         out[(Ny + av) * NU + u] = make_float2((s1 - s2) * inv_ff, (s3 + s4) * inv_ff);
