@@ -286,16 +286,36 @@ int default_conv_n(int Nx, int Ny) {
 
 }  // namespace litho
 
-// Host buffers: the batch moves in chunks of about 16 MB through three device
-// staging slots each way.  Host->device copies run on one copy stream and
-// device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
+// Host buffers: the batch moves in chunks of up to about 16 MB through three
+// device staging slots each way.  Host->device copies run on one copy stream
+// and device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
 // while chunk k is imaged on the context's stream; events order the reuse of
 // every slot, and both copy streams join the context's stream at the end.
+// Nothing overlaps the first chunk's copy in or the last chunk's copy out, so
+// the chunk sizes ramp 1, 2, 4, ... masks up at the start and back down at the
+// end (the host link, not the copy engines, bounds both directions: SM loads
+// and stores on mapped host memory reach the same rates).
+static void chunk_schedule(int batch, int CH, std::vector<int>& sizes) {
+  std::vector<int> ramp;
+  int used = 0;
+  for (int r = 1; r < CH && 2 * (used + r) + CH <= batch; r *= 2) {
+    ramp.push_back(r);
+    used += r;
+  }
+  sizes.assign(ramp.begin(), ramp.end());
+  for (int mid = batch - 2 * used; mid > 0; mid -= CH) sizes.push_back(std::min(CH, mid));
+  sizes.insert(sizes.end(), ramp.rbegin(), ramp.rend());
+}
+
 static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
                       float* images, int precision, size_t img) {
   constexpr int NS = 3;
-  // ~16 MB chunks: short pipeline fill and drain, enough masks per launch
-  const int CH = (int)std::max<size_t>(1, std::min<size_t>((size_t)batch, ((size_t)16 << 20) / img));
+  // chunks of up to ~16 MB (enough masks per launch in the steady state) and at
+  // least ~8 chunks, so small images pipeline too
+  const size_t ch_cap = std::min<size_t>(((size_t)16 << 20) / img, ((size_t)batch + 7) / 8);
+  const int CH = (int)std::max<size_t>(1, ch_cap);
+  std::vector<int> sizes;
+  chunk_schedule(batch, CH, sizes);
   if (ctx->copy_in == nullptr) {
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
@@ -306,7 +326,8 @@ static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* 
     }
     LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
   }
-  const int nslot = (batch + CH - 1) / CH < NS ? (batch + CH - 1) / CH : NS;
+  const int nchunk = (int)sizes.size();
+  const int nslot = nchunk < NS ? nchunk : NS;
   LITHO_RET(ctx->stage_in.ensure(ctx, (size_t)nslot * CH * img));
   LITHO_RET(ctx->stage_out.ensure(ctx, (size_t)nslot * CH * img));
   char* din = ctx->stage_in.as<char>();
@@ -315,10 +336,10 @@ static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* 
   LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
   LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_start, 0));
   LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_start, 0));
-  const int nchunk = (batch + CH - 1) / CH;
-  for (int k = 0; k < nchunk; ++k) {
-    const int sl = k % NS, nb = (k + 1) * CH <= batch ? CH : batch - k * CH;
-    const size_t off = (size_t)k * CH * img, bytes = (size_t)nb * img;
+  size_t off = 0;
+  for (int k = 0; k < nchunk; off += (size_t)sizes[k] * img, ++k) {
+    const int sl = k % NS, nb = sizes[k];
+    const size_t bytes = (size_t)nb * img;
     char* in = din + (size_t)sl * CH * img;
     char* out = dout + (size_t)sl * CH * img;
     if (k >= NS) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_comp[sl], 0));  // slot read

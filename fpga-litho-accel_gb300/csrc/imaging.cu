@@ -27,6 +27,7 @@
 // crop2DCentered (litho.cpp:164-177, 997-1001).
 #include "litho_internal.cuh"
 #include "fft_warp.cuh"
+#include "fft_lane8.cuh"
 #include "tc_common.cuh"
 
 #include <algorithm>
@@ -377,6 +378,159 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
       if (fx <= 2 * Nx) d = fx;
       else if (fx >= N - 2 * Nx) d = fx - N;
       if (d != (1 << 30)) band[fy * BW + d + 2 * Nx] = cscale(x[j], inv);
+    }
+  }
+}
+
+// SOCS on the 64 x 64 conv grid with the eight-lane 64-point FFTs of
+// fft_lane8.cuh: four transforms per warp, natural order throughout.  Same
+// arguments, grid and output as socs_kernel<64>.
+//   rows     : row ky = 8 q + warp of the embedded kernel * window product
+//              (q = lane group); 2Ny + 1 <= 31 rows is one round
+//   columns  : column c = warp + 8 (q + 4 m), m = 0, 1; only the embedded rows
+//              [ey, ey + 2Ny] are read (the others are zero), so the grid is
+//              never cleared; |E|^2 accumulates in registers at (t + 8 k2, c)
+//   intensity: forward column transforms of the real intensity, rows fy <= 2Ny
+//              kept, then forward row transforms of those rows -> band
+// |E|^2 does not depend on where the kernel sits in the grid (a shift is a
+// unimodular phase on E); the embedding is the centred one of socs_kernel.
+// ---------------------------------------------------------------------------
+constexpr int S64_SG = 65;  // grid row stride (float2): columns of a warp's groups 16 banks apart
+
+size_t socs64_smem_bytes(int KD) {
+  return ((size_t)64 * S64_SG + 32 + (size_t)(SOCS_THREADS / 32) * 4 * L8_SCR + KD) * sizeof(float2);
+}
+
+__global__ void __launch_bounds__(SOCS_THREADS) socs64_kernel(
+    const float2* __restrict__ win_part, int nparts, const float* __restrict__ mskf_r,
+    const float* __restrict__ mskf_i, int Fx, int Fy, int Nx, int Ny, const float2* __restrict__ krn,
+    const float* __restrict__ scales, int nk, int kpg, float2* __restrict__ band_part,
+    float* __restrict__ tmpImgp) {
+  constexpr int N = 64, SG = S64_SG, NW = SOCS_THREADS / 32;
+  extern __shared__ __align__(16) float2 sg[];
+  float2* grid = sg;                  // [N][SG]
+  float2* tw = grid + N * SG;         // [N/2]
+  float2* scr = tw + N / 2;           // [NW][4][L8_SCR]
+  float2* win = scr + NW * 4 * L8_SCR;  // [KY][KX]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = lane >> 3, t = lane & 7;
+  float2* my_scr = scr + (warp * 4 + q) * L8_SCR;
+  const int g = blockIdx.x, img = blockIdx.y, ngroups = gridDim.x;
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
+
+  for (int e = tid; e < N / 2; e += SOCS_THREADS) {
+    float s, c;
+    sincospif(2.0f * (float)e / (float)N, &s, &c);
+    tw[e] = make_float2(c, -s);
+  }
+  for (int idx = tid; idx < KD; idx += SOCS_THREADS) {
+    const int ky = idx / KX, kx = idx - ky * KX;
+    const int v = ky - Ny, u = kx - Nx;
+    float2 w;
+    if (mskf_r != nullptr) {
+      const size_t off = (size_t)img * Fx * Fy + (size_t)(Fy / 2 + v) * Fx + (Fx / 2 + u);
+      w = make_float2(mskf_r[off], mskf_i[off]);
+    } else {
+      const bool neg = u < 0;
+      const int vv = neg ? -v : v, uu = neg ? -u : u;
+      const float2* P = win_part + (size_t)img * nparts * KY * (Nx + 1) + (size_t)(vv + Ny) * (Nx + 1) + uu;
+      const float2 s = sum_strided(P, (size_t)KY * (Nx + 1), nparts);
+      w = make_float2(s.x, neg ? -s.y : s.y);
+    }
+    win[idx] = w;
+  }
+  __syncthreads();
+  float2 w64[8];
+  lane8_twiddles(w64, tw, t);
+
+  const int ex = (N - KX) / 2, ey = (N - KY) / 2;
+  float acc[2][8];
+#pragma unroll
+  for (int m = 0; m < 2; ++m)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[m][j] = 0.f;
+
+  const int k0 = g * kpg, k1 = min(nk, k0 + kpg);
+  for (int k = k0; k < k1; ++k) {
+    const float2* K = krn + (size_t)k * KD;
+    const float lam = scales[k];
+    {
+      const int ky = 8 * q + warp;
+      const bool act = ky < KY;
+      float2 x[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int kx = t + 8 * r - ex;
+        x[r] = (act && kx >= 0 && kx < KX) ? cmul(K[ky * KX + kx], win[ky * KX + kx]) : make_float2(0.f, 0.f);
+      }
+      fft64_lane8<true>(x, w64, my_scr, t);
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) grid[(ey + ky) * SG + t + 8 * j] = x[j];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int c = warp + 8 * (q + 4 * m);
+      float2 x[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int y = t + 8 * r;
+        x[r] = (unsigned)(y - ey) < (unsigned)KY ? grid[y * SG + c] : make_float2(0.f, 0.f);
+      }
+      fft64_lane8<true>(x, w64, my_scr, t);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[m][j] = fmaf(lam, fmaf(x[j].x, x[j].x, x[j].y * x[j].y), acc[m][j]);
+    }
+    __syncthreads();
+  }
+
+  if (tmpImgp != nullptr) {
+    // litho.cpp:934 myShift(tmpImg -> tmpImgp, fftshift)
+    float* T = tmpImgp + (size_t)img * N * N;
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int c = warp + 8 * (q + 4 * m);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) T[((t + 8 * j + N / 2) & (N - 1)) * N + ((c + N / 2) & (N - 1))] = acc[m][j];
+    }
+  }
+
+  // forward transform of the intensity: columns, then the rows fy <= 2Ny
+#pragma unroll
+  for (int m = 0; m < 2; ++m) {
+    const int c = warp + 8 * (q + 4 * m);
+    float2 x[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) x[r] = make_float2(acc[m][r], 0.f);
+    fft64_lane8<false>(x, w64, my_scr, t);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int fy = t + 8 * j;
+      if (fy <= 2 * Ny) grid[fy * SG + c] = x[j];
+    }
+  }
+  __syncthreads();
+  const int BW = 4 * Nx + 1;
+  const float inv = 1.0f / ((float)N * (float)N);
+  float2* band = band_part + ((size_t)img * ngroups + g) * KY * BW;
+  {
+    const int fy = 8 * q + warp;
+    const bool act = fy <= 2 * Ny;
+    float2 x[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) x[r] = act ? grid[fy * SG + t + 8 * r] : make_float2(0.f, 0.f);
+    fft64_lane8<false>(x, w64, my_scr, t);
+    if (act) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int fx = t + 8 * j;
+        int d = 1 << 30;
+        if (fx <= 2 * Nx) d = fx;
+        else if (fx >= N - 2 * Nx) d = fx - N;
+        if (d != (1 << 30)) band[fy * BW + d + 2 * Nx] = cscale(x[j], inv);
+      }
     }
   }
 }
@@ -785,8 +939,8 @@ static int launch_socs_t(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, c
                          const float* scales, float2* band_part, float* tmpImgp) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = socs_kernel<N>;
+  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(p.ngroups, p.batch);
   StageScope sc(ctx, LITHO_STAGE_SOCS);
@@ -914,8 +1068,8 @@ static cudaError_t noctx_socs_t(cudaStream_t s, const ImgPlan& p, const float2* 
                                 const float* scales, float2* band_part) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = socs_kernel<N>;
+  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<dim3(p.ngroups, p.batch), SOCS_THREADS, smem, s>>>(win_part, p.nparts(), nullptr, nullptr, g.Fx, g.Fy, g.Nx,

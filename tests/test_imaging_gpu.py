@@ -75,6 +75,21 @@ def test_calc_socs_matches_oracle_128(ctx, golden_optics, golden_kernels):
     assert R.rel_l2(tmp, ref_tmp) < TOL
 
 
+def test_calc_socs_tmpimgp_64(ctx, golden_optics, golden_kernels):
+    """64^2 conv grid (eight-lane FFT kernel): tmpImgp and image against the oracle with the
+    centred embedding (litho_thread.cpp:847)."""
+    mask = _golden_mask512()
+    mskf = R.ft_r2c_padded(mask, 512, 512)
+    krns, scales = golden_kernels
+    nx = golden_optics["Nx"]
+    ref_img, ref_tmp = R.calc_socs(mskf, 512, 512, krns, scales, 10, nx, nx, 64, None)
+    img, tmp = ctx.calc_socs(mskf.real.astype(np.float32), mskf.imag.astype(np.float32), krns, scales,
+                             nx, nx, 512, 512, want_tmpimgp=True, conv_n=64)
+    assert tmp.shape == (64, 64)
+    assert R.rel_l2(tmp, ref_tmp) < TOL
+    assert R.rel_l2(img, ref_img) < TOL
+
+
 def test_calc_socs_matches_hls_golden_32(ctx, golden_optics):
     """source/SOCS_HLS/data/hls_output_full_32.bin: nk=4 on a 32^2 conv grid."""
     h = load_golden("hls_golden.npz")

@@ -107,8 +107,9 @@ def test_mixed_unsupported_geometry(ctx, L):
 
 @pytest.mark.parametrize("prec", ["plain", "mixed"])
 def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec):
-    """Host buffers of 20 masks move through the chunked copy/compute pipeline (chunks of
-    8, 8, 4 on three staging slots); the images equal the device-pointer path's."""
+    """Host buffers of 20 masks move through the chunked copy/compute pipeline (ramped
+    chunks of 1, 2, 3, 3, 3, 3, 2, 2, 1 masks on three staging slots); the images equal
+    the device-pointer path's."""
     import torch
     from litho_gb300 import synth
     p = L.PREC_MIXED if prec == "mixed" else L.PREC_FP32
