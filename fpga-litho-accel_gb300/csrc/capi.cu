@@ -138,7 +138,7 @@ int litho_ctx_destroy(litho_ctx* ctx) {
       cudaStreamSynchronize(st);
       cudaStreamDestroy(st);
     }
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < HB_SLOTS; ++i)
     for (cudaEvent_t e : {ctx->ev_in[i], ctx->ev_comp[i], ctx->ev_out[i]})
       if (e) cudaEventDestroy(e);
   if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -286,7 +286,7 @@ int default_conv_n(int Nx, int Ny) {
 
 }  // namespace litho
 
-// Host buffers: the batch moves in chunks of up to about 16 MB through three
+// Host buffers: the batch moves in chunks of up to about 16 MB through HB_SLOTS
 // device staging slots each way.  Host->device copies run on one copy stream
 // and device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
 // while chunk k is imaged on the context's stream; events order the reuse of
@@ -309,7 +309,7 @@ static void chunk_schedule(int batch, int CH, std::vector<int>& sizes) {
 
 static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
                       float* images, int precision, size_t img) {
-  constexpr int NS = 3;
+  constexpr int NS = HB_SLOTS;
   // chunks of up to ~16 MB (enough masks per launch in the steady state) and at
   // least ~8 chunks, so small images pipeline too
   const size_t ch_cap = std::min<size_t>(((size_t)16 << 20) / img, ((size_t)batch + 7) / 8);

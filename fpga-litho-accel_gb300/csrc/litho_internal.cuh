@@ -96,6 +96,10 @@ inline bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
 }  // namespace litho
 
 // The context.  One stream, a set of grow-only workspaces and cached tables.
+// device staging slots each way of the host-buffer imaging pipeline (6 measured
+// no faster: chunked copies, not slot reuse, bound the pipeline)
+constexpr int HB_SLOTS = 3;
+
 struct litho_ctx {
   int device = 0;
   int sm_count = 0;
@@ -112,7 +116,7 @@ struct litho_ctx {
   litho::DevBuf mx_b, mx_c, mx_d;
   // host-buffer batches: copy streams and per-slot events of the staging pipeline
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
-  cudaEvent_t ev_in[3] = {}, ev_comp[3] = {}, ev_out[3] = {}, ev_start = nullptr;
+  cudaEvent_t ev_in[HB_SLOTS] = {}, ev_comp[HB_SLOTS] = {}, ev_out[HB_SLOTS] = {}, ev_start = nullptr;
   // per-stage timers
   bool timing = false;
   double stage_ms[LITHO_STAGE_COUNT] = {};
