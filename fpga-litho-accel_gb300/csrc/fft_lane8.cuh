@@ -30,6 +30,11 @@ namespace litho {
 
 constexpr int L8_SCR = 72;  // transpose scratch per group of eight lanes (float2)
 
+// complex add / subtract as one packed f32x2 add (per component the same as the
+// scalar adds; a - b is a + (-b), exact)
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+
 // a * conj(w)
 __device__ __forceinline__ float2 cmul_conj(float2 a, float2 w) {
   return make_float2(fmaf(a.x, w.x, a.y * w.y), fmaf(a.y, w.x, -a.x * w.y));
@@ -46,10 +51,10 @@ __device__ __forceinline__ float2 mul_mi(float2 a) {
 template <bool INV>
 __device__ __forceinline__ void dft8(float2 (&x)[8]) {
   constexpr float R = 0.70710678118654752f;  // 1 / sqrt(2)
-  const float2 a0 = cadd(x[0], x[4]), b0 = csub(x[0], x[4]);
-  const float2 a1 = cadd(x[1], x[5]), d1 = csub(x[1], x[5]);
-  const float2 a2 = cadd(x[2], x[6]), d2 = csub(x[2], x[6]);
-  const float2 a3 = cadd(x[3], x[7]), d3 = csub(x[3], x[7]);
+  const float2 a0 = padd(x[0], x[4]), b0 = psub(x[0], x[4]);
+  const float2 a1 = padd(x[1], x[5]), d1 = psub(x[1], x[5]);
+  const float2 a2 = padd(x[2], x[6]), d2 = psub(x[2], x[6]);
+  const float2 a3 = padd(x[3], x[7]), d3 = psub(x[3], x[7]);
   // b_n = (x_n - x_{n+4}) W8^n: W8 = (1 - i)/sqrt2, W8^2 = -i, W8^3 = (-1 - i)/sqrt2 (forward)
   const float2 b1 = INV ? make_float2((d1.x - d1.y) * R, (d1.x + d1.y) * R)
                         : make_float2((d1.x + d1.y) * R, (d1.y - d1.x) * R);
@@ -57,18 +62,18 @@ __device__ __forceinline__ void dft8(float2 (&x)[8]) {
   const float2 b3 = INV ? make_float2(-(d3.x + d3.y) * R, (d3.x - d3.y) * R)
                         : make_float2((d3.y - d3.x) * R, -(d3.x + d3.y) * R);
   // even outputs: 4-point DFT of a; odd outputs: 4-point DFT of b
-  const float2 c0 = cadd(a0, a2), e0 = csub(a0, a2);
-  const float2 c1 = cadd(a1, a3), e1 = mul_mi<INV>(csub(a1, a3));
-  const float2 f0 = cadd(b0, b2), g0 = csub(b0, b2);
-  const float2 f1 = cadd(b1, b3), g1 = mul_mi<INV>(csub(b1, b3));
-  x[0] = cadd(c0, c1);
-  x[4] = csub(c0, c1);
-  x[2] = cadd(e0, e1);
-  x[6] = csub(e0, e1);
-  x[1] = cadd(f0, f1);
-  x[5] = csub(f0, f1);
-  x[3] = cadd(g0, g1);
-  x[7] = csub(g0, g1);
+  const float2 c0 = padd(a0, a2), e0 = psub(a0, a2);
+  const float2 c1 = padd(a1, a3), e1 = mul_mi<INV>(psub(a1, a3));
+  const float2 f0 = padd(b0, b2), g0 = psub(b0, b2);
+  const float2 f1 = padd(b1, b3), g1 = mul_mi<INV>(psub(b1, b3));
+  x[0] = padd(c0, c1);
+  x[4] = psub(c0, c1);
+  x[2] = padd(e0, e1);
+  x[6] = psub(e0, e1);
+  x[1] = padd(f0, f1);
+  x[5] = psub(f0, f1);
+  x[3] = padd(g0, g1);
+  x[7] = psub(g0, g1);
 }
 
 // per-lane twiddles w[k] = W64^(t k), k = 0..7, from tw[e] = W64^e (e < 32)

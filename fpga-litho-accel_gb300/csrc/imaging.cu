@@ -540,10 +540,10 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs64_kernel(
 // (T[-fy] = conj(T[fy]) because the intensity is real).  One thread per image
 // column X and half of the fy rows; the column twiddles live in registers and
 // the band, summed over its kernel-group partials in a fixed order, sits in
-// shared memory pre-combined as C[fy][d] = (Re(p+q), Im(p-q), Im(p+q), Re(p-q))
+// shared memory pre-combined as C[fy][d] = (Re(p+q), -Im(p-q), Im(p+q), Re(p-q))
 // for p = S[fy][d], q = S[fy][-d], so that
 //   T = S0 + sum_{d>0} (p t + q conj(t)),  t = e^{+2 pi i d x'/Fx},
-// costs one broadcast shared load and four FMAs per (fy, d).
+// costs one broadcast shared load and two packed (f32x2) FMAs per (fy, d).
 // Two output layouts:
 //   plain  tm[img][r][X]: r = 0 Re T0, 1..2Ny Re T, 2Ny+1..4Ny Im T (fi_out_kernel)
 //   K-major (tensor-core FI) t0[img][X] = Re T0 and hi/lo TF32 splits of
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
       sC[fy * MAXD] = make_float4(pv.x, pv.y, 0.f, 0.f);
     } else {
       const float2 qv = sum_strided(S - d, pst, ngroups);
-      sC[fy * MAXD + d] = make_float4(pv.x + qv.x, pv.y - qv.y, pv.y + qv.y, pv.x - qv.x);
+      sC[fy * MAXD + d] = make_float4(pv.x + qv.x, -(pv.y - qv.y), pv.y + qv.y, pv.x - qv.x);
     }
   }
   if (KMAJ)
@@ -594,30 +594,28 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
   float* out = KMAJ ? nullptr : tm + (size_t)img * (4 * Ny + 1) * Lx;
   for (int fy = fy0; fy < fy1; ++fy) {
     const float4* C = sC + fy * MAXD;
-    // four independent FMA chains; without the term guard when 2Nx+1 is the table width
-    float ra = C[0].x, rb = 0.f, ia = C[0].y, ib = 0.f;
+    // four independent FMA chains as two packed pairs: (ra, rb) += (c0, c1) * t and
+    // (ia, ib) += (c2, c3) * t with t = (cos, sin) of the column, one f32x2 FMA each
+    // (per component the same fmaf); without the term guard when 2Nx+1 is the table width
+    float2 r = make_float2(C[0].x, 0.f), i2 = make_float2(C[0].y, 0.f);
     if (ND == MAXD) {
 #pragma unroll
       for (int d = 1; d < MAXD; ++d) {
         const float4 a = C[d];
-        ra = fmaf(a.x, tw[d].x, ra);
-        rb = fmaf(-a.y, tw[d].y, rb);
-        ia = fmaf(a.z, tw[d].x, ia);
-        ib = fmaf(a.w, tw[d].y, ib);
+        r = __ffma2_rn(make_float2(a.x, a.y), tw[d], r);
+        i2 = __ffma2_rn(make_float2(a.z, a.w), tw[d], i2);
       }
     } else {
 #pragma unroll
       for (int d = 1; d < MAXD; ++d) {
         if (d < ND) {
           const float4 a = C[d];
-          ra = fmaf(a.x, tw[d].x, ra);
-          rb = fmaf(-a.y, tw[d].y, rb);
-          ia = fmaf(a.z, tw[d].x, ia);
-          ib = fmaf(a.w, tw[d].y, ib);
+          r = __ffma2_rn(make_float2(a.x, a.y), tw[d], r);
+          i2 = __ffma2_rn(make_float2(a.z, a.w), tw[d], i2);
         }
       }
     }
-    const float re = ra + rb, im = ia + ib;
+    const float re = r.x + r.y, im = i2.x + i2.y;
     if (!live) continue;
     if (KMAJ) {
       if (fy == 0) {
