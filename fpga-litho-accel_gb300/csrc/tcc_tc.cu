@@ -8,11 +8,14 @@
 // BF16 hi + lo terms (hi = bf16(v), lo = bf16(v - hi)) and the GEMM issues
 // hi*hi + hi*lo + lo*hi per K slice (the three-term split product).
 //
-// split_kernel      P (complex float), J -> Ah/Al = [X; Y] and Bh/Bl = X, BF16,
-//                   K-major rows padded to Kp (multiple of 64).
-// gemm_bf16x3_kernel  128 x 128 output tile per CTA, K streamed in 64-wide
-//                   (128-byte) slices through a 3-stage TMA/mbarrier ring; one
-//                   thread issues 12 MMAs per slice; epilogue tcgen05.ld -> FP32 C.
+// split_kernel      P (complex float), J -> Ah/Al = [X; Y], BF16, K-major rows
+//                   padded to Kp (multiple of 64); the B operand X is A's first
+//                   n rows (tensor maps over the same memory).
+// gemm_bf16x3_kernel  128 x 128 output tile per CTA (only the tiles the TCC
+//                   reads), K streamed in 64-wide (128-byte) slices through a
+//                   3-stage TMA/mbarrier ring; a producer lane refills the ring
+//                   while the MMA lane issues 12 MMAs per slice; epilogue
+//                   tcgen05.ld -> FP32 C.
 // assemble_kernel   C -> interleaved complex128 TCC: upper triangle from C, the
 //                   lower triangle its conjugate mirror (litho.cpp:510-515).
 #include "litho_internal.cuh"
@@ -21,12 +24,14 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <vector>
+
 namespace litho {
 using namespace tc;
 
 __global__ void split_kernel(const float2* __restrict__ P, const float* __restrict__ J, int n, int ns, int ldp,
-                             int Kp, __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al,
-                             __nv_bfloat16* __restrict__ Bh, __nv_bfloat16* __restrict__ Bl) {
+                             int Kp, __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;  // column in [0, Kp)
   const int i = blockIdx.y;                             // pupil row in [0, n)
   if (k >= Kp || i >= n) return;
@@ -51,8 +56,6 @@ __global__ void split_kernel(const float2* __restrict__ P, const float* __restri
   Al[(size_t)i * Kp + k] = xl;
   Ah[(size_t)(n + i) * Kp + k] = yh;
   Al[(size_t)(n + i) * Kp + k] = yl;
-  Bh[(size_t)i * Kp + k] = xh;
-  Bl[(size_t)i * Kp + k] = xl;
 }
 
 constexpr int GB_STAGES = 3;
@@ -60,19 +63,28 @@ constexpr uint32_t GB_TILE = 128 * 128;          // 128 rows x 64 bf16
 constexpr uint32_t GB_STAGE_B = 4 * GB_TILE;     // Ah, Al, Bh, Bl
 constexpr size_t GB_SMEM = 1024 + (size_t)GB_STAGES * GB_STAGE_B + 256;
 
+// One 128 x 128 tile of C = A B^T per CTA, the tile taken from a list (only the
+// tiles the TCC reads, in blocks that share operand panels in L2).  Warp 0 lane 0
+// streams the K slices through the TMA ring, warp 1 lane 0 issues the MMAs as the
+// slices land (so the tensor pipe is not idle while a stage is refilled), then all
+// four warps drain TMEM with 16-byte stores (ldc a multiple of 4).
 __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tAh,
                                                              const __grid_constant__ CUtensorMap tAl,
                                                              const __grid_constant__ CUtensorMap tBh,
-                                                             const __grid_constant__ CUtensorMap tBl, int M, int N,
-                                                             int Kp, float* __restrict__ C, int* __restrict__ err) {
+                                                             const __grid_constant__ CUtensorMap tBl,
+                                                             const int2* __restrict__ tiles, int M, int N,
+                                                             int Kp, float* __restrict__ C, int ldc,
+                                                             int* __restrict__ err) {
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + GB_STAGES * GB_STAGE_B);
   uint64_t* empty = full + GB_STAGES;
   uint64_t* done = empty + GB_STAGES;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  int* s_bad = reinterpret_cast<int*>(tslot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
+  const int2 tl = tiles[blockIdx.x];
+  const int m0 = tl.x * 128, n0 = tl.y * 128;
   const int nch = Kp / 64;
 
   if (warp == 0) tmem_alloc(tslot, 128);
@@ -82,6 +94,7 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
       mbar_init(&empty[s], 1);
     }
     mbar_init(done, 1);
+    *s_bad = 0;
     fence_mbar_init();
   }
   tc_fence_before();
@@ -89,23 +102,32 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
   tc_fence_after();
   const uint32_t tmem = *tslot;
   auto tile = [&](int s, int q) { return sm + (size_t)s * GB_STAGE_B + (size_t)q * GB_TILE; };
-  auto issue = [&](int c) {
-    const int s = c % GB_STAGES;
-    mbar_arrive_expect_tx(&full[s], GB_STAGE_B);
-    tma_load_2d(tile(s, 0), &tAh, &full[s], 64 * c, m0);
-    tma_load_2d(tile(s, 1), &tAl, &full[s], 64 * c, m0);
-    tma_load_2d(tile(s, 2), &tBh, &full[s], 64 * c, n0);
-    tma_load_2d(tile(s, 3), &tBl, &full[s], 64 * c, n0);
-  };
-  constexpr uint32_t IDESC = idesc_bf16(128, 128);
-  int bad = 0, c = 0, issued = 0;
-  if (tid == 0) {
-    for (; issued < min(nch, GB_STAGES); ++issued) issue(issued);
-    for (; c < nch; ++c) {
+  volatile int* bad = s_bad;
+  if (tid == 0) {  // TMA producer
+    int issued = 0;
+    for (; issued < nch; ++issued) {
+      const int s = issued % GB_STAGES;
+      if (issued >= GB_STAGES &&
+          !mbar_wait_ab(&empty[s], (uint32_t)(issued / GB_STAGES - 1) & 1u, bad))
+        break;
+      mbar_arrive_expect_tx(&full[s], GB_STAGE_B);
+      tma_load_2d(tile(s, 0), &tAh, &full[s], 64 * issued, m0);
+      tma_load_2d(tile(s, 1), &tAl, &full[s], 64 * issued, m0);
+      tma_load_2d(tile(s, 2), &tBh, &full[s], 64 * issued, n0);
+      tma_load_2d(tile(s, 3), &tBl, &full[s], 64 * issued, n0);
+    }
+    if (issued < nch) {
+      *bad = 1;
+      // wait (bounded) for the loads still in flight before the CTA leaves
+      for (int k = (issued > GB_STAGES ? issued - GB_STAGES : 0); k < issued; ++k)
+        mbar_wait(&full[k % GB_STAGES], (uint32_t)(k / GB_STAGES) & 1u, 200u);
+    }
+  } else if (tid == 32) {  // MMA issuer
+    constexpr uint32_t IDESC = idesc_bf16(128, 128);
+    for (int c = 0; c < nch; ++c) {
       const int s = c % GB_STAGES;
-      const uint32_t ph = (uint32_t)(c / GB_STAGES) & 1u;
-      if (!mbar_wait(&full[s], ph)) {
-        bad = 1;
+      if (!mbar_wait_ab(&full[s], (uint32_t)(c / GB_STAGES) & 1u, bad)) {
+        *bad = 1;
         break;
       }
       tc_fence_after();
@@ -119,23 +141,13 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
         mma_bf16(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
       }
       mma_commit(&empty[s]);
-      if (issued < nch) {
-        if (!mbar_wait(&empty[s], ph)) {
-          bad = 1;
-          ++c;
-          break;
-        }
-        issue(issued++);
-      }
     }
-    mma_commit(done);
-    if (!mbar_wait(done, 0)) bad = 1;
-    if (bad) {
-      atomicExch(err, 1);
-      for (int k = c; k < issued; ++k) mbar_wait(&full[k % GB_STAGES], (uint32_t)(k / GB_STAGES) & 1u, 200u);
-    }
+    mma_commit(done);  // arrives once everything issued above has completed
   }
-  if (__syncthreads_or(bad)) {
+  __syncwarp();
+  if (!mbar_wait(done, 0)) *bad = 1;
+  if (__syncthreads_or(*bad)) {
+    if (tid == 0) atomicExch(err, 1);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, 128);
@@ -148,11 +160,17 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
   for (int slab = 0; slab < 4; ++slab) {
     float v[32];
     tmem_ld32(trow + (uint32_t)(slab * 32), v);
-    if (row < M) {
-      float* out = C + (size_t)row * N + n0 + slab * 32;
+    const int c0 = n0 + slab * 32;
+    if (row < M && c0 < N) {
+      float* out = C + (size_t)row * ldc + c0;
+      if (c0 + 32 <= ldc) {
 #pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (n0 + slab * 32 + j < N) out[j] = v[j];
+        for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(out + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < N) out[j] = v[j];
+      }
     }
   }
   tc_fence_before();
@@ -160,13 +178,13 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_consta
   if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
-__global__ void assemble_kernel(const float* __restrict__ C, int n, double2* __restrict__ tcc) {
+__global__ void assemble_kernel(const float* __restrict__ C, int n, int ldc, double2* __restrict__ tcc) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (i >= n || j >= n) return;
   double2 v;
-  if (i < j) v = make_double2(C[(size_t)i * n + j], C[(size_t)(n + i) * n + j]);
-  else if (i > j) v = make_double2(C[(size_t)j * n + i], -(double)C[(size_t)(n + j) * n + i]);
-  else v = make_double2(C[(size_t)i * n + i], 0.0);
+  if (i < j) v = make_double2(C[(size_t)i * ldc + j], C[(size_t)(n + i) * ldc + j]);
+  else if (i > j) v = make_double2(C[(size_t)j * ldc + i], -(double)C[(size_t)(n + j) * ldc + i]);
+  else v = make_double2(C[(size_t)i * ldc + i], 0.0);
   tcc[(size_t)i * n + j] = v;
 }
 
@@ -208,8 +226,27 @@ int tc_err_flag_public(litho_ctx* ctx, int** flag);
 int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int ns, int ldp, double2* tcc) {
   const int Kp = ((2 * ns + 63) / 64) * 64;
   const size_t op = (size_t)Kp * sizeof(__nv_bfloat16);
-  // A: 2n rows (hi, lo), B: n rows (hi, lo), C: 2n x n fp32
-  LITHO_RET(ctx->mx_c.ensure(ctx, op * (4 * (size_t)n + 2 * (size_t)n) + (size_t)2 * n * n * sizeof(float) + 4096));
+  const int ldc = (n + 3) & ~3;  // 16-byte rows for the epilogue's vector stores
+  // C = A A_top^T with A = [X; Y] (2n rows): rows < n hold X X^T (the real part,
+  // symmetric), rows >= n hold Y X^T (the imaginary part, antisymmetric).  The TCC
+  // reads C[a][b] with a <= b and C[n + a][b] with a < b, so only the tiles that
+  // hold such entries are computed (about half), in 12 x 12 blocks of tiles that
+  // share their A and B panels in L2.
+  const int MT = (2 * n + 127) / 128, NT = (n + 127) / 128;
+  std::vector<int2> tiles;
+  for (int mb = 0; mb < MT; mb += 12)
+    for (int nb = 0; nb < NT; nb += 12)
+      for (int mt = mb; mt < std::min(MT, mb + 12); ++mt)
+        for (int nt = nb; nt < std::min(NT, nb + 12); ++nt) {
+          const int r0 = mt * 128, r1 = std::min(r0 + 128, 2 * n);
+          const int cmax = std::min(nt * 128 + 127, n - 1);
+          const bool top = r0 < n && r0 <= cmax;
+          const bool bottom = r1 > n && std::max(r0, n) - n < cmax;
+          if (top || bottom) tiles.push_back(make_int2(mt, nt));
+        }
+  // A: 2n rows (hi, lo); B is A's first n rows; C: 2n x ldc fp32; the tile list
+  const size_t cbytes = (size_t)2 * n * ldc * sizeof(float);
+  LITHO_RET(ctx->mx_c.ensure(ctx, op * 4 * (size_t)n + cbytes + tiles.size() * sizeof(int2) + 4096));
   char* base = ctx->mx_c.as<char>();
   auto take = [&](size_t b) {
     char* p = base;
@@ -218,24 +255,25 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   };
   __nv_bfloat16* Ah = reinterpret_cast<__nv_bfloat16*>(take(op * 2 * n));
   __nv_bfloat16* Al = reinterpret_cast<__nv_bfloat16*>(take(op * 2 * n));
-  __nv_bfloat16* Bh = reinterpret_cast<__nv_bfloat16*>(take(op * n));
-  __nv_bfloat16* Bl = reinterpret_cast<__nv_bfloat16*>(take(op * n));
-  float* C = reinterpret_cast<float*>(take((size_t)2 * n * n * sizeof(float)));
-  split_kernel<<<dim3((Kp + 127) / 128, n), 128, 0, ctx->stream>>>(P, J, n, ns, ldp, Kp, Ah, Al, Bh, Bl);
+  float* C = reinterpret_cast<float*>(take(cbytes));
+  int2* dtiles = reinterpret_cast<int2*>(take(tiles.size() * sizeof(int2)));
+  LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+  split_kernel<<<dim3((Kp + 127) / 128, n), 128, 0, ctx->stream>>>(P, J, n, ns, ldp, Kp, Ah, Al);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   CUtensorMap mAh, mAl, mBh, mBl;
   LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n));
   LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n));
-  LITHO_RET(map_bf16(ctx, &mBh, Bh, Kp, n));
-  LITHO_RET(map_bf16(ctx, &mBl, Bl, Kp, n));
+  LITHO_RET(map_bf16(ctx, &mBh, Ah, Kp, n));
+  LITHO_RET(map_bf16(ctx, &mBl, Al, Kp, n));
   int* err = nullptr;
   LITHO_RET(tc_err_flag_public(ctx, &err));
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)GB_SMEM));
-  dim3 grid((2 * n + 127) / 128, (n + 127) / 128);
-  gemm_bf16x3_kernel<<<grid, 128, GB_SMEM, ctx->stream>>>(mAh, mAl, mBh, mBl, 2 * n, n, Kp, C, err);
+  gemm_bf16x3_kernel<<<(unsigned)tiles.size(), 128, GB_SMEM, ctx->stream>>>(mAh, mAl, mBh, mBl, dtiles, 2 * n, n, Kp,
+                                                                             C, ldc, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
-  assemble_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(C, n, tcc);
+  assemble_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(C, n, ldc, tcc);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
