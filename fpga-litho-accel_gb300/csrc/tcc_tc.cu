@@ -30,32 +30,39 @@
 namespace litho {
 using namespace tc;
 
+// eight consecutive columns k per thread: 16-byte stores of the BF16 rows
 __global__ void split_kernel(const float2* __restrict__ P, const float* __restrict__ J, int n, int ns, int ldp,
                              int Kp, __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // column in [0, Kp)
-  const int i = blockIdx.y;                             // pupil row in [0, n)
-  if (k >= Kp || i >= n) return;
-  float x = 0.f, y = 0.f;  // X[i][k], Y[i][k]
-  const int s = k < ns ? k : k - ns;
-  if (k < 2 * ns) {
-    const float w = sqrtf(J[s]);
-    const float2 p = P[(size_t)i * ldp + s];
-    const float ar = w * p.x, ai = w * p.y;
-    if (k < ns) {
-      x = ar;
-      y = ai;
-    } else {
-      x = ai;
-      y = -ar;
+  const int k0 = 8 * (blockIdx.x * blockDim.x + threadIdx.x);  // first column, in [0, Kp)
+  const int i = blockIdx.y;                                     // pupil row in [0, n)
+  if (k0 >= Kp || i >= n) return;
+  __align__(16) __nv_bfloat16 xh[8], xl[8], yh[8], yl[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = k0 + u;
+    float x = 0.f, y = 0.f;  // X[i][k], Y[i][k]
+    if (k < 2 * ns) {
+      const int s = k < ns ? k : k - ns;
+      const float w = sqrtf(J[s]);
+      const float2 p = P[(size_t)i * ldp + s];
+      const float ar = w * p.x, ai = w * p.y;
+      if (k < ns) {
+        x = ar;
+        y = ai;
+      } else {
+        x = ai;
+        y = -ar;
+      }
     }
+    xh[u] = __float2bfloat16_rn(x);
+    yh[u] = __float2bfloat16_rn(y);
+    xl[u] = __float2bfloat16_rn(x - __bfloat162float(xh[u]));
+    yl[u] = __float2bfloat16_rn(y - __bfloat162float(yh[u]));
   }
-  const __nv_bfloat16 xh = __float2bfloat16_rn(x), yh = __float2bfloat16_rn(y);
-  const __nv_bfloat16 xl = __float2bfloat16_rn(x - __bfloat162float(xh));
-  const __nv_bfloat16 yl = __float2bfloat16_rn(y - __bfloat162float(yh));
-  Ah[(size_t)i * Kp + k] = xh;
-  Al[(size_t)i * Kp + k] = xl;
-  Ah[(size_t)(n + i) * Kp + k] = yh;
-  Al[(size_t)(n + i) * Kp + k] = yl;
+  *reinterpret_cast<uint4*>(Ah + (size_t)i * Kp + k0) = *reinterpret_cast<const uint4*>(xh);
+  *reinterpret_cast<uint4*>(Al + (size_t)i * Kp + k0) = *reinterpret_cast<const uint4*>(xl);
+  *reinterpret_cast<uint4*>(Ah + (size_t)(n + i) * Kp + k0) = *reinterpret_cast<const uint4*>(yh);
+  *reinterpret_cast<uint4*>(Al + (size_t)(n + i) * Kp + k0) = *reinterpret_cast<const uint4*>(yl);
 }
 
 constexpr int GB_STAGES = 3;
@@ -259,7 +266,7 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   int2* dtiles = reinterpret_cast<int2*>(take(tiles.size() * sizeof(int2)));
   LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
                                       ctx->stream));
-  split_kernel<<<dim3((Kp + 127) / 128, n), 128, 0, ctx->stream>>>(P, J, n, ns, ldp, Kp, Ah, Al);
+  split_kernel<<<dim3((Kp / 8 + 127) / 128, n), 128, 0, ctx->stream>>>(P, J, n, ns, ldp, Kp, Ah, Al);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   CUtensorMap mAh, mAl, mBh, mBl;
   LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n));
