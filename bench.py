@@ -42,7 +42,7 @@ METRIC = "aerial images/s at 1024^2 K=24: mixed/batched/surrogate vs plain GPU a
 L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
 # DRAM bytes (read + write) per mask of the dominant kernel, from an ncu capture of one
 # win_dft_tc launch on 48 masks of this workload (the traffic scales with the masks).
-TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.668352e6 + 4.026880e6) / 48}
+TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.648128e6 + 3.824128e6) / 48}
 WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
             "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
 
