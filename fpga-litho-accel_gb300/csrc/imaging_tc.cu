@@ -17,12 +17,13 @@
 // win_dft_tc_kernel   D[y][j] = sum_x mask[y][x] * T[x][j]  (M = 128 mask rows
 //                     per tile, N = 2 NB (hi | lo) for the 2Nx+1 column twiddles
 //                     padded to NB, K = the tile's columns).  448 threads: TMA
-//                     streams 128 x 32 mask tiles (SWIZZLE_128B) through a 6-8
-//                     stage ring; warps 0-7 check each landed tile for TF32
-//                     exactness and split it in place only when it has a
-//                     residual; the accumulator is double-buffered in TMEM and
-//                     warps 10-13 run each tile's row-DFT epilogue while the next
-//                     tile streams.
+//                     streams 128 x 32 mask tiles (SWIZZLE_128B), two per
+//                     stage, through a ring of as many stages as shared memory
+//                     holds (4 at Nx = 8); warps 0-7 check each landed tile for TF32
+//                     exactness (no low 13 mantissa bit set) and split it in
+//                     place only when it has a residual; the accumulator is
+//                     double-buffered in TMEM and warps 10-13 run each tile's
+//                     row-DFT epilogue while the next tile streams.
 // fi_tc_kernel        image[Y][X] = T0[X] + sum_r Cy[Y][r] * Tm[r][X]  (M = 128
 //                     image rows, N = 2 BN per tile, K = 4Ny rows padded to
 //                     32*KBLK; the DC row T0 is added in FP32 by the epilogue).
@@ -203,9 +204,9 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&ready[s], WP_CONS);
+      mbar_init(&ready[s], WP_CONS / 32);  // one arrival per consumer warp
       mbar_init(&hidone[s], 1);
-      mbar_init(&ready2[s], WP_CONS);
+      mbar_init(&ready2[s], WP_CONS / 32);
       mbar_init(&empty[s], 1);
       last_issued[s] = -1;
       nzflag[s] = 0;
@@ -343,13 +344,14 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         if (!mbar_wait_ab(&full[s], ph, abort)) *abort = 1;
         float4* a = reinterpret_cast<float4*>(sA(s));
         float4 v[4 * P::KB];
-        bool nz = false;
+        // x is exact in TF32 (x == round_tf32(x)) iff its low 13 mantissa bits are zero
+        uint32_t low = 0;
 #pragma unroll
         for (int i = 0; i < 4 * P::KB; ++i) {
           v[i] = a[tid + WP_CONS * i];
-          nz |= (v[i].x != tf32_round(v[i].x)) | (v[i].y != tf32_round(v[i].y)) | (v[i].z != tf32_round(v[i].z)) |
-                (v[i].w != tf32_round(v[i].w));
+          low |= __float_as_uint(v[i].x) | __float_as_uint(v[i].y) | __float_as_uint(v[i].z) | __float_as_uint(v[i].w);
         }
+        const bool nz = (low & 0x1FFFu) != 0u;
         if (__any_sync(0xffffffffu, nz) && lane == 0) atomicOr(&nzflag[s], 1);
         named_bar(1, WP_CONS);
         const bool two = *reinterpret_cast<volatile int*>(&nzflag[s]) != 0;
@@ -360,7 +362,9 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
                 make_float4(tf32_round(v[i].x), tf32_round(v[i].y), tf32_round(v[i].z), tf32_round(v[i].w));
           fence_proxy_async();
         }
-        mbar_arrive(&ready[s]);  // release: Ah visible to the MMA lane
+        // release: the warp's reads of nzflag and its Ah stores precede its one arrival
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ready[s]);
         if (two) {
           if (!mbar_wait_ab(&hidone[s], (ph2 >> s) & 1u, abort)) *abort = 1;
           ph2 ^= 1u << s;
@@ -369,7 +373,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
             a[tid + WP_CONS * i] = make_float4(v[i].x - tf32_round(v[i].x), v[i].y - tf32_round(v[i].y),
                                                v[i].z - tf32_round(v[i].z), v[i].w - tf32_round(v[i].w));
           fence_proxy_async();
-          mbar_arrive(&ready2[s]);
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ready2[s]);
         }
         if (++s == S) {
           s = 0;
