@@ -266,13 +266,15 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
     const float* __restrict__ scales, int nk, int kpg, float2* __restrict__ band_part,
     float* __restrict__ tmpImgp) {
   constexpr int J = N / 32, SG = N + 1, CPW = N / 8;
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
   extern __shared__ __align__(16) float2 sg[];
-  float2* grid = sg;             // [N][SG]
-  float2* tw = grid + N * SG;    // [N/2]
+  // only the KY embedded rows of the conv grid are ever non-zero, and the forward
+  // pass keeps the rows fy <= 2Ny (= KY rows): a compact [KY][SG] grid
+  float2* grid = sg;             // [KY][SG]
+  float2* tw = grid + KY * SG;   // [N/2]
   float2* win = tw + N / 2;      // [KY][KX]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = blockIdx.x, img = blockIdx.y, ngroups = gridDim.x;
-  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
 
   for (int e = tid; e < N / 2; e += SOCS_THREADS) {
     float s, c;
@@ -295,7 +297,6 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
     }
     win[idx] = w;
   }
-  for (int i = tid; i < N * SG; i += SOCS_THREADS) grid[i] = make_float2(0.f, 0.f);
   __syncthreads();
 
   const int ex = (N - KX) / 2, ey = (N - KY) / 2;
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
       }
       warp_fft_dif<N, true>(x, tw, lane);
 #pragma unroll
-      for (int j = 0; j < J; ++j) grid[(ey + ky) * SG + lane + 32 * j] = x[j];
+      for (int j = 0; j < J; ++j) grid[ky * SG + lane + 32 * j] = x[j];
     }
     __syncthreads();
 #pragma unroll
@@ -326,7 +327,10 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs_kernel(
       const int c = warp + 8 * m;
       float2 x[J];
 #pragma unroll
-      for (int j = 0; j < J; ++j) x[j] = grid[(lane + 32 * j) * SG + c];
+      for (int j = 0; j < J; ++j) {
+        const int y = lane + 32 * j;  // rows outside the embedded band are zero
+        x[j] = (unsigned)(y - ey) < (unsigned)KY ? grid[(y - ey) * SG + c] : make_float2(0.f, 0.f);
+      }
       warp_fft_dif<N, true>(x, tw, lane);
 #pragma unroll
       for (int j = 0; j < J; ++j) acc[m][j] = fmaf(lam, fmaf(x[j].x, x[j].x, x[j].y * x[j].y), acc[m][j]);
@@ -937,7 +941,7 @@ static int launch_socs_t(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, c
                          const float* scales, float2* band_part, float* tmpImgp) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
   auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(p.ngroups, p.batch);
@@ -1066,7 +1070,7 @@ static cudaError_t noctx_socs_t(cudaStream_t s, const ImgPlan& p, const float2* 
                                 const float* scales, float2* band_part) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)N * (N + 1) + N / 2 + KD) * sizeof(float2);
+  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
   auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
