@@ -1,5 +1,5 @@
-// 64-point FFTs on groups of eight lanes: four transforms per warp, natural order
-// in and out.
+// 64-point FFTs on groups of eight lanes (four transforms per warp, natural order
+// in and out) and 128-point FFTs on groups of sixteen lanes built from them.
 //
 // Lane t (t = lane & 7) of a group holds x[r] = v[t + 8r], r = 0..7.  The
 // transform is the 8 x 8 Cooley-Tukey split of 64 = 8 * 8:
@@ -100,6 +100,51 @@ __device__ __forceinline__ void fft64_lane8(float2 (&x)[8], const float2 (&w)[8]
   for (int s = 0; s < 8; ++s) x[s] = scr[t * 9 + s];
   __syncwarp();  // the scratch may be rewritten by the next transform
   dft8<INV>(x);
+}
+
+// 128-point transforms on groups of sixteen lanes (two transforms per warp): one
+// radix-2 stage across the two eight-lane halves of the group (lane bit 3, h) and
+// a 64-point transform (fft64_lane8) in each half.  t = lane & 7.
+//
+// Inverse, decimation in frequency: lane (t, h) holds v[t + 8i + 64h] in x[i];
+//   u = v[n], w = v[n + 64] (n = t + 8i): half 0 forms u + w, half 1 forms
+//   (u - w) conj(W128^n); then each half runs the inverse 64-point transform, so
+//   lane (t, h) ends holding V[2(t + 8i) + h] = V[2t + h + 16i].
+// Forward, decimation in time: lane (t, h) holds v[2t + h + 16i] (half 0 the even
+//   samples, half 1 the odd ones); each half runs the forward 64-point transform
+//   (E, O at k = t + 8i), half 1 multiplies by W128^k, and the halves exchange:
+//   lane (t, h) ends holding V[t + 8i + 64h] = E[k] + (-1)^h W128^k O[k].
+// So the inverse takes the forward's output layout and gives the forward's input
+// layout: an inverse pass followed by a forward pass needs no reordering.
+// tw128[e] = W128^e for e < 64; the half-1 factors are read per call (registers).
+template <bool INV>
+__device__ __forceinline__ float2 l16_twiddle(const float2* tw128, int t, int i, int h) {
+  const float2 v = tw128[t + 8 * i];
+  return h ? (INV ? make_float2(v.x, -v.y) : v) : make_float2(1.f, 0.f);
+}
+
+__device__ __forceinline__ void fft128_inv_dif(float2 (&x)[8], const float2 (&w64)[8], const float2* tw128,
+                                               float2* scr, int t, int h) {
+  const float s = h ? -1.f : 1.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float2 p = shfl_xor2(x[i], 8);
+    const float2 y = make_float2(fmaf(s, x[i].x, p.x), fmaf(s, x[i].y, p.y));
+    x[i] = cmul(y, l16_twiddle<true>(tw128, t, i, h));
+  }
+  fft64_lane8<true>(x, w64, scr, t);
+}
+
+__device__ __forceinline__ void fft128_fwd_dit(float2 (&x)[8], const float2 (&w64)[8], const float2* tw128,
+                                               float2* scr, int t, int h) {
+  fft64_lane8<false>(x, w64, scr, t);
+  const float s = h ? -1.f : 1.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float2 z = cmul(x[i], l16_twiddle<false>(tw128, t, i, h));
+    const float2 p = shfl_xor2(z, 8);
+    x[i] = make_float2(fmaf(s, z.x, p.x), fmaf(s, z.y, p.y));
+  }
 }
 
 }  // namespace litho

@@ -539,6 +539,167 @@ __global__ void __launch_bounds__(SOCS_THREADS) socs64_kernel(
   }
 }
 
+// SOCS on the 128 x 128 conv grid with the sixteen-lane 128-point FFTs of
+// fft_lane8.cuh (two transforms per warp), 512 threads so that each lane keeps
+// four columns' intensities in registers.  Same arguments, grid and output as
+// socs_kernel<128>.  Lane (t, h, slot): t = lane & 7, h = (lane >> 3) & 1,
+// slot = lane >> 4; transform slot sl = 16 slot + warp of a round (32 per round).
+//   rows     : row ky = 32 r + sl of the embedded product, read at columns
+//              t + 8i + 64h (inverse, DIF) and stored at columns 2t + h + 16i
+//   columns  : column c = 32 m + sl, m = 0..3, read at rows t + 8i + 64h of the
+//              compact grid (only the 2Ny + 1 embedded rows exist); |E|^2 lands
+//              at rows 2t + h + 16i
+//   intensity: forward column transforms (DIT) take that layout and give
+//              fy = t + 8i + 64h, rows fy <= 2Ny kept; forward row transforms read
+//              columns 2t + h + 16i and give fx = t + 8i + 64h -> band
+// ---------------------------------------------------------------------------
+constexpr int S128_SG = 129;       // compact grid row stride (float2)
+constexpr int S128_THREADS = 512;
+
+size_t socs128_smem_bytes(int KY, int KD) {
+  return ((size_t)KY * S128_SG + 64 + 32 + (size_t)(S128_THREADS / 32) * 4 * L8_SCR + KD) * sizeof(float2);
+}
+
+__global__ void __launch_bounds__(S128_THREADS) socs128_kernel(
+    const float2* __restrict__ win_part, int nparts, const float* __restrict__ mskf_r,
+    const float* __restrict__ mskf_i, int Fx, int Fy, int Nx, int Ny, const float2* __restrict__ krn,
+    const float* __restrict__ scales, int nk, int kpg, float2* __restrict__ band_part,
+    float* __restrict__ tmpImgp) {
+  constexpr int N = 128, SG = S128_SG, NW = S128_THREADS / 32;
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
+  extern __shared__ __align__(16) float2 sg[];
+  float2* grid = sg;                     // [KY][SG]
+  float2* tw128 = grid + KY * SG;        // [64]
+  float2* tw64 = tw128 + 64;             // [32]
+  float2* scr = tw64 + 32;               // [NW][4][L8_SCR]
+  float2* win = scr + NW * 4 * L8_SCR;   // [KY][KX]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t = lane & 7, h = (lane >> 3) & 1, sl = 16 * (lane >> 4) + warp;
+  float2* my_scr = scr + (warp * 4 + (lane >> 3)) * L8_SCR;
+  const int g = blockIdx.x, img = blockIdx.y, ngroups = gridDim.x;
+
+  for (int e = tid; e < 64; e += S128_THREADS) {
+    float sn, cs;
+    sincospif((float)e / 64.0f, &sn, &cs);  // W128^e = exp(-2 pi i e / 128)
+    tw128[e] = make_float2(cs, -sn);
+    if (e < 32) {
+      sincospif((float)e / 32.0f, &sn, &cs);
+      tw64[e] = make_float2(cs, -sn);
+    }
+  }
+  for (int idx = tid; idx < KD; idx += S128_THREADS) {
+    const int ky = idx / KX, kx = idx - ky * KX;
+    const int v = ky - Ny, u = kx - Nx;
+    float2 w;
+    if (mskf_r != nullptr) {
+      const size_t off = (size_t)img * Fx * Fy + (size_t)(Fy / 2 + v) * Fx + (Fx / 2 + u);
+      w = make_float2(mskf_r[off], mskf_i[off]);
+    } else {
+      const bool neg = u < 0;
+      const int vv = neg ? -v : v, uu = neg ? -u : u;
+      const float2* P = win_part + (size_t)img * nparts * KY * (Nx + 1) + (size_t)(vv + Ny) * (Nx + 1) + uu;
+      const float2 sm = sum_strided(P, (size_t)KY * (Nx + 1), nparts);
+      w = make_float2(sm.x, neg ? -sm.y : sm.y);
+    }
+    win[idx] = w;
+  }
+  __syncthreads();
+  float2 w64[8];
+  lane8_twiddles(w64, tw64, t);
+
+  const int ex = (N - KX) / 2, ey = (N - KY) / 2;
+  float acc[4][8];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[m][j] = 0.f;
+
+  const int k0 = g * kpg, k1 = min(nk, k0 + kpg);
+  for (int k = k0; k < k1; ++k) {
+    const float2* K = krn + (size_t)k * KD;
+    const float lam = scales[k];
+    for (int r0 = 0; r0 < KY; r0 += 32) {  // uniform bound: every lane takes every round
+      const int ky = r0 + sl;
+      const bool act = ky < KY;
+      float2 x[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int kx = t + 8 * i + 64 * h - ex;
+        x[i] = (act && kx >= 0 && kx < KX) ? cmul(K[ky * KX + kx], win[ky * KX + kx]) : make_float2(0.f, 0.f);
+      }
+      fft128_inv_dif(x, w64, tw128, my_scr, t, h);
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) grid[ky * SG + 2 * t + h + 16 * i] = x[i];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int c = 32 * m + sl;
+      float2 x[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int y = t + 8 * i + 64 * h;
+        x[i] = (unsigned)(y - ey) < (unsigned)KY ? grid[(y - ey) * SG + c] : make_float2(0.f, 0.f);
+      }
+      fft128_inv_dif(x, w64, tw128, my_scr, t, h);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) acc[m][i] = fmaf(lam, fmaf(x[i].x, x[i].x, x[i].y * x[i].y), acc[m][i]);
+    }
+    __syncthreads();
+  }
+
+  if (tmpImgp != nullptr) {
+    // litho.cpp:934 myShift(tmpImg -> tmpImgp, fftshift)
+    float* T = tmpImgp + (size_t)img * N * N;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int c = 32 * m + sl;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        T[((2 * t + h + 16 * i + N / 2) & (N - 1)) * N + ((c + N / 2) & (N - 1))] = acc[m][i];
+    }
+  }
+
+  // forward transform of the intensity: columns, then the rows fy <= 2Ny
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int c = 32 * m + sl;
+    float2 x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = make_float2(acc[m][i], 0.f);
+    fft128_fwd_dit(x, w64, tw128, my_scr, t, h);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int fy = t + 8 * i + 64 * h;
+      if (fy <= 2 * Ny) grid[fy * SG + c] = x[i];
+    }
+  }
+  __syncthreads();
+  const int BW = 4 * Nx + 1;
+  const float inv = 1.0f / ((float)N * (float)N);
+  float2* band = band_part + ((size_t)img * ngroups + g) * KY * BW;
+  for (int r0 = 0; r0 < KY; r0 += 32) {
+    const int fy = r0 + sl;
+    const bool act = fy <= 2 * Ny;
+    float2 x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = act ? grid[fy * SG + 2 * t + h + 16 * i] : make_float2(0.f, 0.f);
+    fft128_fwd_dit(x, w64, tw128, my_scr, t, h);
+    if (act) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int fx = t + 8 * i + 64 * h;
+        int d = 1 << 30;
+        if (fx <= 2 * Nx) d = fx;
+        else if (fx >= N - 2 * Nx) d = fx - N;
+        if (d != (1 << 30)) band[fy * BW + d + 2 * Nx] = cscale(x[i], inv);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // FI, step 1: T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx} for fy = 0..2Ny
 // (T[-fy] = conj(T[fy]) because the intensity is real).  One thread per image
@@ -941,12 +1102,15 @@ static int launch_socs_t(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, c
                          const float* scales, float2* band_part, float* tmpImgp) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
+  const size_t smem = N == 64    ? socs64_smem_bytes(KD)
+                      : N == 128 ? socs128_smem_bytes(2 * g.Ny + 1, KD)
+                                 : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = N == 64 ? socs64_kernel : N == 128 ? socs128_kernel : socs_kernel<N>;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(p.ngroups, p.batch);
   StageScope sc(ctx, LITHO_STAGE_SOCS);
-  k<<<grid, SOCS_THREADS, smem, ctx->stream>>>(w.part, w.nparts, w.mskf_r, w.mskf_i, g.Fx, g.Fy, g.Nx, g.Ny, krn,
+  k<<<grid, N == 128 ? S128_THREADS : SOCS_THREADS, smem, ctx->stream>>>(w.part, w.nparts, w.mskf_r, w.mskf_i, g.Fx,
+                                                                       g.Fy, g.Nx, g.Ny, krn,
                                                 scales, g.nk, p.kpg, band_part, tmpImgp);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
@@ -1070,11 +1234,14 @@ static cudaError_t noctx_socs_t(cudaStream_t s, const ImgPlan& p, const float2* 
                                 const float* scales, float2* band_part) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64 ? socs64_smem_bytes(KD) : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = N == 64 ? socs64_kernel : socs_kernel<N>;
+  const size_t smem = N == 64    ? socs64_smem_bytes(KD)
+                      : N == 128 ? socs128_smem_bytes(2 * g.Ny + 1, KD)
+                                 : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
+  auto k = N == 64 ? socs64_kernel : N == 128 ? socs128_kernel : socs_kernel<N>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<dim3(p.ngroups, p.batch), SOCS_THREADS, smem, s>>>(win_part, p.nparts(), nullptr, nullptr, g.Fx, g.Fy, g.Nx,
+  k<<<dim3(p.ngroups, p.batch), N == 128 ? S128_THREADS : SOCS_THREADS, smem, s>>>(win_part, p.nparts(), nullptr,
+                                                                                 nullptr, g.Fx, g.Fy, g.Nx,
                                                           g.Ny, krn, scales, g.nk, p.kpg, band_part, nullptr);
   return cudaGetLastError();
 }
