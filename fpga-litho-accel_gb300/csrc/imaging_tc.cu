@@ -489,8 +489,11 @@ struct FiTC {
   static constexpr uint32_t B_KB = BN * 128;      // BN rows x 32 fp32
   static constexpr uint32_t A_BYTES = 2 * KBLK * A_KB;
   static constexpr uint32_t B_BYTES = 2 * KBLK * B_KB;
-  static constexpr int NS = KBLK == 1 ? 3 : 2;    // B stages
-  static constexpr int NOUT = KBLK == 1 ? 2 : 1;  // staging tiles per epilogue group
+  // B stages and staging tiles per epilogue group: three and two whenever shared
+  // memory holds them (K = 64 rows with 128-column tiles does not)
+  static constexpr bool ROOMY = KBLK == 1 || BN <= 64;
+  static constexpr int NS = ROOMY ? 3 : 2;
+  static constexpr int NOUT = ROOMY ? 2 : 1;
   static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
   static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
@@ -659,11 +662,11 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
     unsigned char* stg = sOut + (size_t)grp * NOUT * P::OUT_B;
     int slab_count = 0;
     // the DC row of the next tile is fetched one tile ahead (its latency hides behind a tile)
-    auto t0_of = [&](int i) {
+    auto t0_of = [&](int i) {  // thread gtid < BN holds column gtid of the tile
       int yb, img, xt;
       decode(i, yb, img, xt);
       const int X = xt * BN + gtid;
-      return X < Lx ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
+      return (gtid < BN && X < Lx) ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
     };
     float t0n = i0 < i1 ? t0_of(i0) : 0.f;
     for (int i = i0; i < i1; ++i) {
@@ -671,7 +674,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       int yb, img, xt;
       decode(i, yb, img, xt);
       // every reader of the previous tile's DC row has passed its last slab's second barrier
-      t0s[gtid] = t0n;
+      if (gtid < BN) t0s[gtid] = t0n;
       if (i + 1 < i1) t0n = t0_of(i + 1);
       // a wait that gives up flags the error and carries on with the rest of the
       // group (later waits return at once): a thread that left the loop alone
@@ -950,7 +953,8 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     LITHO_CUDA_TRY(ctx, launch_fi_rows(ctx->stream, p, band_part, twF, KP, nullptr, tmh, tml, t0));
   }
   if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
-  return launch_fi_tc<2, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
+  // K = 64: 64-column tiles keep three B stages and two staging tiles per group
+  return launch_fi_tc<2, 64>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
 }
 
 }  // namespace litho
