@@ -255,7 +255,9 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
 
 // ---------------------------------------------------------------------------
 // SOCS: K inverse FFTs on the N x N conv grid, intensity accumulation in
-// registers, forward FFT of the intensity, band output.
+// registers, forward FFT of the intensity, band output.  socs_kernel<N> uses the
+// warp-shuffle transforms of fft_warp.cuh and serves the 32 x 32 grid; the 64 and
+// 128 grids have their own kernels on the lane-group transforms of fft_lane8.cuh.
 // ---------------------------------------------------------------------------
 constexpr int SOCS_THREADS = 256;
 
@@ -1102,10 +1104,18 @@ static int launch_socs_t(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, c
                          const float* scales, float2* band_part, float* tmpImgp) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64    ? socs64_smem_bytes(KD)
-                      : N == 128 ? socs128_smem_bytes(2 * g.Ny + 1, KD)
-                                 : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = N == 64 ? socs64_kernel : N == 128 ? socs128_kernel : socs_kernel<N>;
+  size_t smem;
+  decltype(&socs64_kernel) k;
+  if constexpr (N == 64) {
+    smem = socs64_smem_bytes(KD);
+    k = socs64_kernel;
+  } else if constexpr (N == 128) {
+    smem = socs128_smem_bytes(2 * g.Ny + 1, KD);
+    k = socs128_kernel;
+  } else {
+    smem = ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
+    k = socs_kernel<N>;
+  }
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(p.ngroups, p.batch);
   StageScope sc(ctx, LITHO_STAGE_SOCS);
@@ -1234,10 +1244,18 @@ static cudaError_t noctx_socs_t(cudaStream_t s, const ImgPlan& p, const float2* 
                                 const float* scales, float2* band_part) {
   const ImgGeom& g = p.g;
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1);
-  const size_t smem = N == 64    ? socs64_smem_bytes(KD)
-                      : N == 128 ? socs128_smem_bytes(2 * g.Ny + 1, KD)
-                                 : ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
-  auto k = N == 64 ? socs64_kernel : N == 128 ? socs128_kernel : socs_kernel<N>;
+  size_t smem;
+  decltype(&socs64_kernel) k;
+  if constexpr (N == 64) {
+    smem = socs64_smem_bytes(KD);
+    k = socs64_kernel;
+  } else if constexpr (N == 128) {
+    smem = socs128_smem_bytes(2 * g.Ny + 1, KD);
+    k = socs128_kernel;
+  } else {
+    smem = ((size_t)(2 * g.Ny + 1) * (N + 1) + N / 2 + KD) * sizeof(float2);
+    k = socs_kernel<N>;
+  }
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<dim3(p.ngroups, p.batch), N == 128 ? S128_THREADS : SOCS_THREADS, smem, s>>>(win_part, p.nparts(), nullptr,
