@@ -622,43 +622,81 @@ __global__ void __launch_bounds__(RR_THREADS) cluster_rr_kernel(const double* __
   }
   // Rayleigh-Ritz: H = Z_c^T T Z_c
   rr_pairs(d, e, Zc, n, c, true, H);
+  for (int i = threadIdx.x; i < c * c; i += RR_THREADS) V[i / c][i % c] = (i / c == i % c) ? 1.0 : 0.0;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // cyclic Jacobi on the c x c symmetric H; V accumulates the rotations
-    for (int a = 0; a < c; ++a)
-      for (int b = 0; b < c; ++b) V[a][b] = a == b ? 1.0 : 0.0;
+  // cyclic Jacobi on the c x c symmetric H, V accumulating the rotations, in
+  // round-robin order: a sweep is cp - 1 rounds (cp = c rounded up to even; index
+  // c is a dummy when c is odd), each rotating cp/2 disjoint pairs (p, q) at once.
+  // A pair's rotation is computed from the matrix before its round (the 2 x 2
+  // block of (p, q) is touched by no other rotation of the round), then all
+  // column rotations (H <- H J, V <- V J) and all row rotations (H <- J^T H)
+  // are applied by the whole block.  Same rotation formulas as the serial
+  // cyclic method; the circle method pairs every (p, q) once per sweep.
+  {
+    __shared__ double s_cs[RR_MAXC / 2], s_sn[RR_MAXC / 2];
+    __shared__ int s_p[RR_MAXC / 2], s_q[RR_MAXC / 2];
+    __shared__ int s_done;
+    const int cp = c + (c & 1), np = cp / 2;
     for (int sweep = 0; sweep < 30; ++sweep) {
-      double off = 0.0, dia = 0.0;
-      for (int a = 0; a < c; ++a) {
-        dia += H[a][a] * H[a][a];
-        for (int b = a + 1; b < c; ++b) off += H[a][b] * H[a][b];
+      if (threadIdx.x == 0) {
+        double off = 0.0, dia = 0.0;
+        for (int a = 0; a < c; ++a) {
+          dia += H[a][a] * H[a][a];
+          for (int b = a + 1; b < c; ++b) off += H[a][b] * H[a][b];
+        }
+        s_done = off <= 1e-32 * dia;
       }
-      if (off <= 1e-32 * dia) break;
-      for (int p = 0; p < c - 1; ++p)
-        for (int q = p + 1; q < c; ++q) {
-          const double apq = H[p][q];
-          if (apq == 0.0) continue;
-          const double theta = (H[q][q] - H[p][p]) / (2.0 * apq);
-          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-          for (int k = 0; k < c; ++k) {  // H <- J^T H J
-            const double hkp = H[k][p], hkq = H[k][q];
-            H[k][p] = cs * hkp - sn * hkq;
-            H[k][q] = sn * hkp + cs * hkq;
+      __syncthreads();
+      if (s_done) break;
+      for (int r = 0; r < cp - 1; ++r) {
+        if (threadIdx.x < np) {
+          const int i = threadIdx.x, j = cp - 1 - i;
+          const int a = i == 0 ? 0 : (i - 1 + r) % (cp - 1) + 1;
+          const int b = (j - 1 + r) % (cp - 1) + 1;
+          const int pp = min(a, b), qq = max(a, b);
+          double cs = 1.0, sn = 0.0;
+          if (qq < c) {
+            const double apq = H[pp][qq];
+            if (apq != 0.0) {
+              const double theta = (H[qq][qq] - H[pp][pp]) / (2.0 * apq);
+              const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+              cs = 1.0 / sqrt(t * t + 1.0);
+              sn = t * cs;
+            }
           }
-          for (int k = 0; k < c; ++k) {
-            const double hpk = H[p][k], hqk = H[q][k];
-            H[p][k] = cs * hpk - sn * hqk;
-            H[q][k] = sn * hpk + cs * hqk;
-          }
-          for (int k = 0; k < c; ++k) {
-            const double vkp = V[k][p], vkq = V[k][q];
-            V[k][p] = cs * vkp - sn * vkq;
-            V[k][q] = sn * vkp + cs * vkq;
+          s_p[i] = pp;
+          s_q[i] = qq;
+          s_cs[i] = cs;
+          s_sn[i] = sn;
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < np * c; w += RR_THREADS) {  // columns p, q of H and V
+          const int i = w / c, k = w - i * c, pp = s_p[i], qq = s_q[i];
+          if (qq < c) {
+            const double cs = s_cs[i], sn = s_sn[i];
+            const double hkp = H[k][pp], hkq = H[k][qq];
+            H[k][pp] = cs * hkp - sn * hkq;
+            H[k][qq] = sn * hkp + cs * hkq;
+            const double vkp = V[k][pp], vkq = V[k][qq];
+            V[k][pp] = cs * vkp - sn * vkq;
+            V[k][qq] = sn * vkp + cs * vkq;
           }
         }
+        __syncthreads();
+        for (int w = threadIdx.x; w < np * c; w += RR_THREADS) {  // rows p, q of H
+          const int i = w / c, k = w - i * c, pp = s_p[i], qq = s_q[i];
+          if (qq < c) {
+            const double cs = s_cs[i], sn = s_sn[i];
+            const double hpk = H[pp][k], hqk = H[qq][k];
+            H[pp][k] = cs * hpk - sn * hqk;
+            H[qq][k] = sn * hpk + cs * hqk;
+          }
+        }
+        __syncthreads();
+      }
     }
-    // descending Ritz values
+  }
+  if (threadIdx.x == 0) {  // descending Ritz values
     for (int a = 0; a < c; ++a) s_order[a] = a;
     for (int a = 1; a < c; ++a) {
       const int key = s_order[a];
