@@ -524,8 +524,27 @@ __device__ void rr_pairs(const double* d, const double* e, const double* Zc, int
     tri_tile(p, a, b);
     const double* za = Zc + (size_t)a * n;
     const double* zb = Zc + (size_t)b * n;
-    double sd = 0.0;
-    for (int i = lane; i < n; i += 32) sd += za[i] * (withT ? tri_mul(d, e, zb, n, i) : zb[i]);
+    // four independent partial sums: four loads of each row in flight per lane
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = lane;
+    if (withT) {
+      for (; i + 96 < n; i += 128) {
+        s0 += za[i] * tri_mul(d, e, zb, n, i);
+        s1 += za[i + 32] * tri_mul(d, e, zb, n, i + 32);
+        s2 += za[i + 64] * tri_mul(d, e, zb, n, i + 64);
+        s3 += za[i + 96] * tri_mul(d, e, zb, n, i + 96);
+      }
+      for (; i < n; i += 32) s0 += za[i] * tri_mul(d, e, zb, n, i);
+    } else {
+      for (; i + 96 < n; i += 128) {
+        s0 += za[i] * zb[i];
+        s1 += za[i + 32] * zb[i + 32];
+        s2 += za[i + 64] * zb[i + 64];
+        s3 += za[i + 96] * zb[i + 96];
+      }
+      for (; i < n; i += 32) s0 += za[i] * zb[i];
+    }
+    double sd = (s0 + s1) + (s2 + s3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
     if (lane == 0) {
