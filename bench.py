@@ -73,6 +73,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(dist, x, device):
+    """The largest x over all ranks (every rank passes its own); x itself without a
+    process group.  A step's time is the slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_images_per_s(world, batch, steps, seconds):
+    """Whole-job throughput: every rank images its own batch per step (weak scaling,
+    replicas), over the slowest rank's time."""
+    return world * batch * steps / seconds
+
+
 def make_masks(n, seed0=100):
     import numpy as np
     from litho_gb300 import synth
@@ -439,11 +456,7 @@ def main():
             step(form)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(dist, e0.elapsed_time(e1), "cuda")
         ctx.enable_timing(False)
         return ms, ctx.stage_times(reset=True)
 
@@ -470,8 +483,8 @@ def main():
     other = "plain" if head == "mixed" else "mixed"
     ms_o, _ = timed(other, args.steps, False)
     ms, st_v = timed(head, args.steps, False)
-    value = ws * B * args.steps / (ms / 1e3)
-    value_o = ws * B * args.steps / (ms_o / 1e3)
+    value = job_images_per_s(ws, B, args.steps, ms / 1e3)
+    value_o = job_images_per_s(ws, B, args.steps, ms_o / 1e3)
     launches = sum(n for _, n in st_v.values())
     # per-kernel durations: a shorter pass with every launch bracketed by CUDA events
     ksteps = max(10, args.steps // 5)
@@ -510,12 +523,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx.image_batch(ks[head], hin, hout, precision=prec[head])
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = ws * B * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0, "cuda")
+    e2e = job_images_per_s(ws, B, e2e_steps, e2e_s)
     clk = clocks.stop()
 
     forms = {head: {"images_per_s": value, "ms_per_step": ms / args.steps,
