@@ -743,33 +743,53 @@ __global__ void __launch_bounds__(RR_THREADS) cluster_rr_kernel(const double* __
 
 // y = H_0 H_1 ... H_{n-2} z for eigenvector j = blockIdx.x; H_k = I - tau_k v_k v_k^H
 // acting on rows k+1..n-1, v_k packed contiguously in vpack.
+// y_j = H_0 H_1 ... H_{n-2} z_j, one CTA per vector.  Thread t owns the elements
+// y[t + 256 s] for the whole loop, so a reflector's update touches only what its
+// own dot-product terms read: the one barrier per reflector is the one inside the
+// reduction (the warps' partials double-buffered by reflector parity, summed by
+// every thread in a fixed order).
 __global__ void __launch_bounds__(256) backtransform_kernel(const double2* __restrict__ vpack, int n,
                                                             const double2* __restrict__ tau,
                                                             const double* __restrict__ Z, double2* __restrict__ Y) {
-  __shared__ double red[32];
-  const int j = blockIdx.x;
+  __shared__ double2 red[2][8];
+  const int j = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
   double2* y = Y + (size_t)j * n;
-  for (int i = threadIdx.x; i < n; i += 256) y[i] = make_double2(Z[(size_t)j * n + i], 0.0);
-  __syncthreads();
-  for (int k = n - 2; k >= 0; --k) {
-    const int m = n - k - 1;
-    const double2* v = vpack + vpack_off(n, k);
+  for (int i = t; i < n; i += 256) y[i] = make_double2(Z[(size_t)j * n + i], 0.0);
+  int par = 0;
+  for (int k = n - 2; k >= 0; --k, par ^= 1) {
+    const double2* v = vpack + vpack_off(n, k) - (k + 1);  // v[r] for rows r in [k+1, n)
+    int r0 = t;
+    if (r0 < k + 1) r0 += ((k + 1 - r0 + 255) / 256) * 256;
+    // conj(v) * y as FMA chains (two FP64 FMAs per component and element; GB300
+    // issues two FP64 FMAs per clock per SM, and this phase runs one CTA per vector)
     double sr = 0.0, si = 0.0;
-    for (int i = threadIdx.x; i < m; i += 256) {
-      const double2 vv = v[i];
-      const double2 yy = y[k + 1 + i];
-      sr += vv.x * yy.x + vv.y * yy.y;  // conj(v) * y
-      si += vv.x * yy.y - vv.y * yy.x;
+    for (int r = r0; r < n; r += 256) {
+      const double2 vv = v[r];
+      const double2 yy = y[r];
+      sr = fma(vv.x, yy.x, fma(vv.y, yy.y, sr));
+      si = fma(vv.x, yy.y, fma(-vv.y, yy.x, si));
     }
-    sr = block_sum<256>(sr, red);
-    si = block_sum<256>(si, red);
-    const double2 f = zmul(tau[k], make_double2(sr, si));
-    for (int i = threadIdx.x; i < m; i += 256) {
-      const double2 p = zmul(f, v[i]);
-      y[k + 1 + i].x -= p.x;
-      y[k + 1 + i].y -= p.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
     }
+    if (lane == 0) red[par][w] = make_double2(sr, si);
     __syncthreads();
+    double2 sum = red[par][0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+      sum.x += red[par][q].x;
+      sum.y += red[par][q].y;
+    }
+    const double2 f = zmul(tau[k], sum);
+    for (int r = r0; r < n; r += 256) {  // y -= f v, as FMA chains
+      const double2 vv = v[r];
+      double2 yy = y[r];
+      yy.x = fma(-f.x, vv.x, fma(f.y, vv.y, yy.x));
+      yy.y = fma(-f.x, vv.y, fma(-f.y, vv.x, yy.y));
+      y[r] = yy;
+    }
   }
 }
 
