@@ -277,15 +277,38 @@ __global__ void last_diag_kernel(const double2* __restrict__ A, int n, double* _
   if (threadIdx.x == 0) d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)].x;
 }
 
-__device__ int sturm_count_lt(const double* d, const double* e, int n, double x, double pivmin) {
+__global__ void square_kernel(const double* __restrict__ e, double* __restrict__ e2, int m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) e2[i] = e[i] * e[i];
+}
+
+// Number of eigenvalues of T below x: the sign changes of the leading principal
+// minors p_i of T - xI, p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2} (p_{-1} = 1),
+// i.e. the rows with q_i = p_i / p_{i-1} < 0 of the classical ratio recurrence,
+// without its division per row (a division is some ten FP64 operations, and
+// GB300 issues two FP64 FMAs per clock per SM).  A minor that comes out zero is
+// replaced by -pivmin p_{i-1} (the ratio recurrence's q_i = -pivmin).  p_{i-1},
+// p_i are rescaled together by 2^-256 / 2^256 (exact) when p_i leaves
+// [2^-256, 2^256), so both stay below 2^512 and a step cannot overflow; the
+// test reads the exponent bits on the integer pipe.
+__device__ int sturm_count_lt(const double* d, const double* e2, int n, double x, double pivmin) {
   int c = 0;
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  if (q < 0.0) ++c;
+  double pm = 1.0;       // p_{i-1}
+  double p = d[0] - x;   // p_i
+  if (p == 0.0) p = -pivmin;
+  c += p < 0.0;
   for (int i = 1; i < n; ++i) {
-    q = d[i] - x - e[i - 1] * e[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) ++c;
+    double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
+    if (pn == 0.0) pn = -pivmin * p;
+    c += (__double_as_longlong(pn) ^ __double_as_longlong(p)) < 0;  // sign change
+    pm = p;
+    p = pn;
+    const unsigned ex = (unsigned)(__double_as_longlong(p) >> 52) & 0x7FFu;
+    if (ex - 767u >= 512u) {  // |p| outside [2^-256, 2^256) (or subnormal)
+      const int sh = ex >= 1279u ? -256 : 256;
+      p = ldexp(p, sh);
+      pm = ldexp(pm, sh);
+    }
   }
   return c;
 }
@@ -301,7 +324,8 @@ __device__ int sturm_count_lt(const double* d, const double* e, int n, double x,
 constexpr int MS_THREADS = 128;
 
 __global__ void __launch_bounds__(MS_THREADS) multisect_kernel(const double* __restrict__ d,
-                                                               const double* __restrict__ e, int n, int nk,
+                                                               const double* __restrict__ e,
+                                                               const double* __restrict__ e2, int n, int nk,
                                                                double* __restrict__ evals) {
   __shared__ double sh[3][MS_THREADS / 32];
   __shared__ unsigned masks[MS_THREADS / 32];
@@ -340,7 +364,7 @@ __global__ void __launch_bounds__(MS_THREADS) multisect_kernel(const double* __r
     // every thread evaluates the same expressions, so lo, hi stay identical in all
     const double w = (hi - lo) / (double)(MS_THREADS + 1);
     const double x = lo + w * (double)(t + 1);
-    const bool above = x > lo && x < hi && sturm_count_lt(d, e, n, x, pivmin) > m;
+    const bool above = x > lo && x < hi && sturm_count_lt(d, e2, n, x, pivmin) > m;
     const unsigned up = __ballot_sync(0xffffffffu, above);
     __syncthreads();  // the previous round's masks have been read
     if (lane == 0) masks[warp] = up;
@@ -836,7 +860,7 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   const size_t iv_scratch = iv_in_smem ? 0 : (size_t)IV_CHUNK * 6 * n * sizeof(double);
   const size_t vpack_bytes = (size_t)n * (n - 1) / 2 * sizeof(double2) + sizeof(double2);
   const size_t part_bytes = (size_t)((n + 7) / 8) * sizeof(double2);
-  const size_t wbytes = 3 * n * sizeof(double2) + vpack_bytes + part_bytes + 2 * n * sizeof(double) + nk * sizeof(double) +
+  const size_t wbytes = 3 * n * sizeof(double2) + vpack_bytes + part_bytes + 3 * n * sizeof(double) + nk * sizeof(double) +
                         (size_t)nk * n * sizeof(double) + iv_scratch + (size_t)nk * n * sizeof(double2) + 16 * 64;
   LITHO_RET(ctx->eig_work.ensure(ctx, wbytes));
   char* w = ctx->eig_work.as<char>();
@@ -852,16 +876,17 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   double2* part = reinterpret_cast<double2*>(take(part_bytes));
   double* d = reinterpret_cast<double*>(take(n * sizeof(double)));
   double* e = reinterpret_cast<double*>(take(n * sizeof(double)));
+  double* e2 = reinterpret_cast<double*>(take(n * sizeof(double)));
   double* ev = reinterpret_cast<double*>(take(nk * sizeof(double)));
   double* Z = reinterpret_cast<double*>(take((size_t)nk * n * sizeof(double)));
   double* ivs = iv_in_smem ? nullptr : reinterpret_cast<double*>(take(iv_scratch));
   double2* Y = reinterpret_cast<double2*>(take((size_t)nk * n * sizeof(double2)));
   double2* A = ctx->eig_v.as<double2>();
   {
-    // hermitize, 2 per reflector, last diagonal, multisection, inverse iteration
+    // hermitize, 2 per reflector, last diagonal, e^2, multisection, inverse iteration
     // (one launch, or one per chunk of IV_CHUNK vectors), cluster Rayleigh-Ritz, back-transform
     const int iv_launches = iv_in_smem ? 1 : (nk + IV_CHUNK - 1) / IV_CHUNK;
-    StageScope sc(ctx, LITHO_STAGE_EIG, 2 * (n > 1 ? n - 1 : 0) + 5 + iv_launches);
+    StageScope sc(ctx, LITHO_STAGE_EIG, 2 * (n > 1 ? n - 1 : 0) + 6 + iv_launches);
     hermitize_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(static_cast<const double2*>(dtcc), A, n);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     LITHO_CUDA_TRY(ctx, cudaMemsetAsync(e, 0, n * sizeof(double), ctx->stream));
@@ -874,7 +899,8 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
     }
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     last_diag_kernel<<<1, 32, 0, ctx->stream>>>(A, n, d);
-    multisect_kernel<<<nk, MS_THREADS, 0, ctx->stream>>>(d, e, n, nk, ev);
+    square_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(e, e2, n - 1);
+    multisect_kernel<<<nk, MS_THREADS, 0, ctx->stream>>>(d, e, e2, n, nk, ev);
     if (iv_in_smem) {
       LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(invvec_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)iv_smem));
