@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(IV_THREADS) invvec_kernel(const double* __rest
   const int j = j0 + blockIdx.x;
   double* base = SMEM ? ivs : scratch + (size_t)blockIdx.x * 6 * n;
   double* dl = base;           // L multipliers
-  double* dd = base + n;       // U diagonal
+  double* dd = base + n;       // U diagonal (its reciprocal after the factorisation)
   double* du = base + 2 * n;   // U first super-diagonal
   double* du2 = base + 3 * n;  // U second super-diagonal
   double* z = base + 4 * n;
@@ -484,8 +484,15 @@ __global__ void __launch_bounds__(IV_THREADS) invvec_kernel(const double* __rest
       else pivd[i] = sw ? 1.0 : 0.0;
     }
     if (dd[n - 1] == 0.0) dd[n - 1] = tiny;
-    for (int i = 0; i < n; ++i)
-      if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
+  }
+  __syncthreads();
+  // U's diagonal, clamped away from zero, is kept as its reciprocal: the serial
+  // back substitutions multiply (an FP64 division is a multi-instruction sequence,
+  // and GB300 issues two FP64 operations per clock per SM)
+  for (int i = threadIdx.x; i < n; i += IV_THREADS) {
+    double v = dd[i];
+    if (fabs(v) < tiny) v = v < 0.0 ? -tiny : tiny;
+    dd[i] = 1.0 / v;
   }
   __syncthreads();
   for (int it = 0; it < IV_ITERS; ++it) {
@@ -500,9 +507,9 @@ __global__ void __launch_bounds__(IV_THREADS) invvec_kernel(const double* __rest
           z[i + 1] = t - dl[i] * z[i];
         }
       }
-      z[n - 1] /= dd[n - 1];
-      if (n > 1) z[n - 2] = (z[n - 2] - du[n - 2] * z[n - 1]) / dd[n - 2];
-      for (int i = n - 3; i >= 0; --i) z[i] = (z[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) / dd[i];
+      z[n - 1] *= dd[n - 1];
+      if (n > 1) z[n - 2] = (z[n - 2] - du[n - 2] * z[n - 1]) * dd[n - 2];
+      for (int i = n - 3; i >= 0; --i) z[i] = (z[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) * dd[i];
     }
     __syncthreads();
     double sq = 0.0;
