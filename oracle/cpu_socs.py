@@ -1,6 +1,6 @@
 """Multi-threaded CPU restatement of litho.cpp Modules 3 + 7 (the timed CPU baseline).
 
-TEST/BASELINE INFRASTRUCTURE ONLY: imported by ``bench.py`` for its
+TEST INFRASTRUCTURE ONLY (and the bench's CPU leg): imported by ``bench.py`` for its
 ``cpu_baseline`` leg and for ``--impl reference`` (the reference's CPU path timed
 on the host cores), never by the product.
 
