@@ -44,7 +44,7 @@ extern "C" {
 #define LITHO_ERR_NAN          4  /* non-finite input or output detected */
 #define LITHO_ERR_NOMEM        5  /* device or pinned allocation failed */
 #define LITHO_ERR_IO           6  /* file read/write failed (BIN / JSON helpers) */
-#define LITHO_ERR_UNSUPPORTED  7  /* size or mode outside what this build implements */
+#define LITHO_ERR_UNSUPPORTED  7  /* size or mode outside what the library implements */
 #define LITHO_ERR_TIMEOUT      8  /* a bounded device-side wait gave up */
 
 #define LITHO_MEM_HOST   0

@@ -1,6 +1,6 @@
 """CPU oracle for the Fourier-neural-operator surrogate -- TEST INFRASTRUCTURE ONLY.
 
-Nothing in the product imports this module: it is the checker for the GPU
+Nothing in the product imports this module: it is the oracle for the GPU
 surrogate kernels (tests, ``__graft_entry__.smoke`` and ``bench.py``'s CPU leg).
 
 The surrogate has no counterpart in the reference (the reference images every

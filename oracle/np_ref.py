@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  This module is the oracle that the GPU library is
 checked against.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs
-of ``bench.py`` may import it, and only as the checker or as the timed CPU
+of ``bench.py`` may import it, and only to check results or as the timed CPU
 baseline; the product (``liblitho_gb300.so`` and the ``litho_gb300`` Python
 binding) never calls into it.
 
