@@ -493,7 +493,7 @@ struct FiTC {
   // memory holds them (K = 64 rows with 128-column tiles does not)
   static constexpr bool ROOMY = KBLK == 1 || BN <= 64;
   static constexpr int NS = ROOMY ? 3 : 2;
-  static constexpr int NOUT = ROOMY ? 2 : 1;
+  static constexpr int NOUT = KBLK == 1 && BN == 128 ? 3 : (ROOMY ? 2 : 1);
   static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
   static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
@@ -689,10 +689,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
         tmem_ld32_async(trow + (uint32_t)(BN + slab * 32), w);
         tmem_ld_wait();
         unsigned char* st = stg + (size_t)(slab_count % NOUT) * P::OUT_B;
-        if (leader) {  // the store that used this staging tile has read it
-          if (NOUT == 2) bulk_wait_read1();
-          else bulk_wait_read0();
-        }
+        if (leader) bulk_wait_read<NOUT - 1>();  // the store that used this staging tile has read it
         named_bar(1 + grp, 128);  // ... and t0s holds this tile's DC row
         const float4* t04 = reinterpret_cast<const float4*>(t0s + slab * 32);
         float4 d[8];
