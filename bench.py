@@ -5,8 +5,11 @@ Workload (one "step"): a batch of B seeded 1024x1024 float32 Manhattan masks
 (line/space gratings and contact arrays, ~50 % density) imaged with K=24 fixed
 SOCS kernels.  The kernels come from this library's own GPU TCC + FP64
 eigensolver for a quasar source (4 poles at 45/135/225/315 deg, sigma 0.7-0.9,
-~2000 lit points), NA 0.8, lambda 193 nm, defocus 0.  B=64 masks are 256 MB in
-and 256 MB out per step, larger than the 129 MB L2, so no flush is needed.
+~2000 lit points), NA 0.8, lambda 193 nm, defocus 0.  B=256 masks (the size of
+the batched workload) are 1 GiB in and 1 GiB out per step, far larger than the
+129 MB L2, so no flush is needed.  Smaller steps pay a fixed per-step cost (the
+previous step's image writes still dirty in L2, kernel tails and launch gaps)
+over fewer masks: 64 masks per step run at ~0.83 of the 256-mask throughput.
 
   value : images/s with masks resident in HBM (litho_image_batch on device
           pointers), timed with CUDA events over K steps on the library's stream.
@@ -40,9 +43,13 @@ sys.path.insert(0, os.path.join(ROOT, "fpga-litho-accel_gb300"))
 
 METRIC = "aerial images/s at 1024^2 K=24: mixed/batched/surrogate vs plain GPU at stated rel-L2"
 L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
-# DRAM bytes (read + write) per mask of the dominant kernel, from an ncu capture of one
-# win_dft_tc launch on 48 masks of this workload (the traffic scales with the masks).
-TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.648128e6 + 3.824128e6) / 48}
+# DRAM bytes (read + write) per mask of the mixed form's two HBM-bound kernels, from an
+# ncu capture of one launch of each on 48 masks of this workload (the traffic scales with
+# the masks).  The FI kernel's figure is what DRAM saw during its launch: part of its
+# image writes is still in L2 when it ends and drains during the next launch.
+TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.648128e6 + 3.824128e6) / 48,
+                     ("mixed", "fi_out"): (13.070848e6 + 141.268992e6) / 48}
+TRAFFIC_KERNEL = {"win_dft": "win_dft_tc", "fi_out": "fi_tc"}
 WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
             "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
 
@@ -53,7 +60,7 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--batch", type=int, default=256)
     p.add_argument("--cpu-budget-s", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])
@@ -550,8 +557,8 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm,
                          "traffic": (B * TRAFFIC_PER_IMAGE[(head, dom)]) if (head, dom) in TRAFFIC_PER_IMAGE else None,
-                         "traffic_source": "ncu dram__bytes_read+write of one win_dft_tc launch at 1024^2, K=24, "
-                                           "48 masks, scaled per mask to the batch",
+                         "traffic_source": (f"ncu dram__bytes_read+write of one {TRAFFIC_KERNEL.get(dom, dom)} launch "
+                                            "at 1024^2, K=24, 48 masks, scaled per mask to the batch"),
                          "peak_source": "measured (MEASURED_PEAKS.json)" if peaks else "fallback",
                          "shares": shares, "kernel_gbs": kern_gbs,
                          "bytes_per_image": 2 * img_bytes + kb,
