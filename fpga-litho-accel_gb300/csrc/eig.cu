@@ -774,51 +774,135 @@ __global__ void __launch_bounds__(RR_THREADS) cluster_rr_kernel(const double* __
 
 // y = H_0 H_1 ... H_{n-2} z for eigenvector j = blockIdx.x; H_k = I - tau_k v_k v_k^H
 // acting on rows k+1..n-1, v_k packed contiguously in vpack.
-// y_j = H_0 H_1 ... H_{n-2} z_j, one CTA per vector.  Thread t owns the elements
-// y[t + 256 s] for the whole loop, so a reflector's update touches only what its
-// own dot-product terms read: the one barrier per reflector is the one inside the
-// reduction (the warps' partials double-buffered by reflector parity, summed by
-// every thread in a fixed order).
-__global__ void __launch_bounds__(256) backtransform_kernel(const double2* __restrict__ vpack, int n,
-                                                            const double2* __restrict__ tau,
-                                                            const double* __restrict__ Z, double2* __restrict__ Y) {
-  __shared__ double2 red[2][8];
-  const int j = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
-  double2* y = Y + (size_t)j * n;
-  for (int i = t; i < n; i += 256) y[i] = make_double2(Z[(size_t)j * n + i], 0.0);
-  int par = 0;
-  for (int k = n - 2; k >= 0; --k, par ^= 1) {
-    const double2* v = vpack + vpack_off(n, k) - (k + 1);  // v[r] for rows r in [k+1, n)
-    int r0 = t;
-    if (r0 < k + 1) r0 += ((k + 1 - r0 + 255) / 256) * 256;
-    // conj(v) * y as FMA chains (two FP64 FMAs per component and element; GB300
-    // issues two FP64 FMAs per clock per SM, and this phase runs one CTA per vector)
-    double sr = 0.0, si = 0.0;
-    for (int r = r0; r < n; r += 256) {
-      const double2 vv = v[r];
-      const double2 yy = y[r];
-      sr = fma(vv.x, yy.x, fma(vv.y, yy.y, sr));
-      si = fma(vv.x, yy.y, fma(-vv.y, yy.x, si));
+// y_j = H_0 H_1 ... H_{n-2} z_j for every eigenvector j, with the reflectors taken
+// WY_NB at a time in compact WY form: H_k0 ... H_{k0+nb-1} = I - V T V^H (V the
+// block's reflectors as columns, T upper triangular: T_jj = tau_j,
+// T[0:j, j] = -tau_j T[0:j, 0:j] (V[:, 0:j]^H v_j)), so a block costs three block
+// barriers (w = V^H y reduced over the CTA, u = T w, y -= V u) instead of one per
+// reflector, for the same FP64 work.
+constexpr int WY_NB = 16;
+
+// T of every block (one CTA per block): the Gram products v_i^H v_j (i < j, over
+// v_j's support) one warp per pair, then the triangular recurrence on one thread
+__global__ void __launch_bounds__(256) wy_t_kernel(const double2* __restrict__ vpack,
+                                                   const double2* __restrict__ tau, int n,
+                                                   double2* __restrict__ Tg) {
+  __shared__ double2 G[WY_NB][WY_NB];
+  __shared__ double2 T[WY_NB][WY_NB];
+  const int b = blockIdx.x, k0 = b * WY_NB, nbb = min(WY_NB, n - 1 - k0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int np = nbb * (nbb - 1) / 2;
+  for (int p = warp; p < np; p += 8) {
+    int j = 1;
+    while ((j + 1) * j / 2 <= p) ++j;  // p = j (j - 1) / 2 + i, i < j
+    const int i = p - j * (j - 1) / 2;
+    const int ki = k0 + i, kj = k0 + j;
+    const double2* vi = vpack + vpack_off(n, ki) - (ki + 1);  // v_i[r], r in [ki+1, n)
+    const double2* vj = vpack + vpack_off(n, kj) - (kj + 1);
+    double sr = 0.0, si = 0.0;  // conj(v_i) . v_j
+    for (int r = kj + 1 + lane; r < n; r += 32) {
+      const double2 a = vi[r], c = vj[r];
+      sr = fma(a.x, c.x, fma(a.y, c.y, sr));
+      si = fma(a.x, c.y, fma(-a.y, c.x, si));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       sr += __shfl_xor_sync(0xffffffffu, sr, o);
       si += __shfl_xor_sync(0xffffffffu, si, o);
     }
-    if (lane == 0) red[par][w] = make_double2(sr, si);
-    __syncthreads();
-    double2 sum = red[par][0];
-#pragma unroll
-    for (int q = 1; q < 8; ++q) {
-      sum.x += red[par][q].x;
-      sum.y += red[par][q].y;
+    if (lane == 0) G[i][j] = make_double2(sr, si);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int jj = 0; jj < WY_NB; ++jj)
+      for (int ii = 0; ii < WY_NB; ++ii) T[ii][jj] = make_double2(0.0, 0.0);
+    for (int jj = 0; jj < nbb; ++jj) {
+      const double2 tj = tau[k0 + jj];
+      T[jj][jj] = tj;
+      for (int ii = 0; ii < jj; ++ii) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int l = ii; l < jj; ++l) {
+          const double2 t = T[ii][l], g = G[l][jj];
+          acc.x += t.x * g.x - t.y * g.y;
+          acc.y += t.x * g.y + t.y * g.x;
+        }
+        T[ii][jj] = make_double2(-(tj.x * acc.x - tj.y * acc.y), -(tj.x * acc.y + tj.y * acc.x));
+      }
     }
-    const double2 f = zmul(tau[k], sum);
-    for (int r = r0; r < n; r += 256) {  // y -= f v, as FMA chains
-      const double2 vv = v[r];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < WY_NB * WY_NB; e += 256) Tg[(size_t)b * WY_NB * WY_NB + e] = T[e / WY_NB][e % WY_NB];
+}
+
+// one CTA per vector; thread t owns the elements y[t + 256 s] for the whole loop
+__global__ void __launch_bounds__(256) backtransform_kernel(const double2* __restrict__ vpack, int n,
+                                                            const double2* __restrict__ Tg,
+                                                            const double* __restrict__ Z, double2* __restrict__ Y) {
+  __shared__ double2 red[8][WY_NB];
+  __shared__ double2 s_w[WY_NB], s_u[WY_NB];
+  __shared__ long long s_base[WY_NB];  // v_i[r] = vpack[s_base[i] + r]
+  const int j = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  double2* y = Y + (size_t)j * n;
+  for (int i = t; i < n; i += 256) y[i] = make_double2(Z[(size_t)j * n + i], 0.0);
+  const int nblk = (n - 1 + WY_NB - 1) / WY_NB;
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int k0 = b * WY_NB, nbb = min(WY_NB, n - 1 - k0);
+    if (t < WY_NB) s_base[t] = t < nbb ? (long long)vpack_off(n, k0 + t) - (k0 + t + 1) : 0;
+    __syncthreads();  // s_base; also, every thread is past the previous block's reads of s_u
+    int r0 = t;
+    if (r0 < k0 + 1) r0 += ((k0 + 1 - r0 + 255) / 256) * 256;
+    double ar[WY_NB], ai[WY_NB];
+#pragma unroll
+    for (int i = 0; i < WY_NB; ++i) ar[i] = ai[i] = 0.0;
+    for (int r = r0; r < n; r += 256) {
+      const double2 yy = y[r];
+#pragma unroll
+      for (int i = 0; i < WY_NB; ++i)
+        if (i < nbb && r > k0 + i) {
+          const double2 vv = vpack[s_base[i] + r];
+          ar[i] = fma(vv.x, yy.x, fma(vv.y, yy.y, ar[i]));  // conj(v) * y
+          ai[i] = fma(vv.x, yy.y, fma(-vv.y, yy.x, ai[i]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < WY_NB; ++i) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ar[i] += __shfl_xor_sync(0xffffffffu, ar[i], o);
+        ai[i] += __shfl_xor_sync(0xffffffffu, ai[i], o);
+      }
+      if (lane == 0) red[w][i] = make_double2(ar[i], ai[i]);
+    }
+    __syncthreads();
+    if (t < WY_NB) {
+      double2 sm = red[0][t];
+      for (int q = 1; q < 8; ++q) {
+        sm.x += red[q][t].x;
+        sm.y += red[q][t].y;
+      }
+      s_w[t] = sm;
+    }
+    __syncthreads();
+    if (t < WY_NB) {  // u = T w (T upper triangular)
+      const double2* Tb = Tg + (size_t)b * WY_NB * WY_NB + (size_t)t * WY_NB;
+      double2 u = make_double2(0.0, 0.0);
+      for (int l = t; l < nbb; ++l) {
+        const double2 a = Tb[l], c = s_w[l];
+        u.x += a.x * c.x - a.y * c.y;
+        u.y += a.x * c.y + a.y * c.x;
+      }
+      s_u[t] = u;
+    }
+    __syncthreads();
+    for (int r = r0; r < n; r += 256) {  // y -= V u
       double2 yy = y[r];
-      yy.x = fma(-f.x, vv.x, fma(f.y, vv.y, yy.x));
-      yy.y = fma(-f.x, vv.y, fma(-f.y, vv.x, yy.y));
+#pragma unroll
+      for (int i = 0; i < WY_NB; ++i)
+        if (i < nbb && r > k0 + i) {
+          const double2 vv = vpack[s_base[i] + r], u = s_u[i];
+          yy.x = fma(-u.x, vv.x, fma(u.y, vv.y, yy.x));
+          yy.y = fma(-u.x, vv.y, fma(-u.y, vv.x, yy.y));
+        }
       y[r] = yy;
     }
   }
@@ -868,7 +952,8 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   const size_t vpack_bytes = (size_t)n * (n - 1) / 2 * sizeof(double2) + sizeof(double2);
   const size_t part_bytes = (size_t)((n + 7) / 8) * sizeof(double2);
   const size_t wbytes = 3 * n * sizeof(double2) + vpack_bytes + part_bytes + 3 * n * sizeof(double) + nk * sizeof(double) +
-                        (size_t)nk * n * sizeof(double) + iv_scratch + (size_t)nk * n * sizeof(double2) + 16 * 64;
+                        (size_t)nk * n * sizeof(double) + iv_scratch + (size_t)nk * n * sizeof(double2) +
+                        (size_t)((n + WY_NB - 1) / WY_NB + 1) * WY_NB * WY_NB * sizeof(double2) + 17 * 64;
   LITHO_RET(ctx->eig_work.ensure(ctx, wbytes));
   char* w = ctx->eig_work.as<char>();
   auto take = [&](size_t b) {
@@ -888,12 +973,14 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
   double* Z = reinterpret_cast<double*>(take((size_t)nk * n * sizeof(double)));
   double* ivs = iv_in_smem ? nullptr : reinterpret_cast<double*>(take(iv_scratch));
   double2* Y = reinterpret_cast<double2*>(take((size_t)nk * n * sizeof(double2)));
+  const int wy_blocks = n > 1 ? (n - 1 + WY_NB - 1) / WY_NB : 0;
+  double2* Tg = reinterpret_cast<double2*>(take((size_t)(wy_blocks > 0 ? wy_blocks : 1) * WY_NB * WY_NB * sizeof(double2)));
   double2* A = ctx->eig_v.as<double2>();
   {
     // hermitize, 2 per reflector, last diagonal, e^2, multisection, inverse iteration
-    // (one launch, or one per chunk of IV_CHUNK vectors), cluster Rayleigh-Ritz, back-transform
+    // (one launch, or one per chunk of IV_CHUNK vectors), cluster Rayleigh-Ritz, WY factors, back-transform
     const int iv_launches = iv_in_smem ? 1 : (nk + IV_CHUNK - 1) / IV_CHUNK;
-    StageScope sc(ctx, LITHO_STAGE_EIG, 2 * (n > 1 ? n - 1 : 0) + 6 + iv_launches);
+    StageScope sc(ctx, LITHO_STAGE_EIG, 2 * (n > 1 ? n - 1 : 0) + 6 + (wy_blocks > 0 ? 1 : 0) + iv_launches);
     hermitize_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(static_cast<const double2*>(dtcc), A, n);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     LITHO_CUDA_TRY(ctx, cudaMemsetAsync(e, 0, n * sizeof(double), ctx->stream));
@@ -917,7 +1004,8 @@ extern "C" int litho_calc_kernels(litho_ctx* ctx, const double* tcc, int tccSize
         invvec_kernel<false><<<std::min(IV_CHUNK, nk - j0), IV_THREADS, 0, ctx->stream>>>(d, e, n, j0, ev, Z, ivs);
     }
     cluster_rr_kernel<<<nk, RR_THREADS, 0, ctx->stream>>>(d, e, n, nk, ev, Z);
-    backtransform_kernel<<<nk, 256, 0, ctx->stream>>>(vpack, n, tau, Z, Y);
+    if (wy_blocks > 0) wy_t_kernel<<<wy_blocks, 256, 0, ctx->stream>>>(vpack, tau, n, Tg);
+    backtransform_kernel<<<nk, 256, 0, ctx->stream>>>(vpack, n, Tg, Z, Y);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   float *okr = krn_r, *oki = krn_i, *osc = scales;
