@@ -67,6 +67,9 @@ def parse():
     p.add_argument("--no-surrogate", action="store_true")
     p.add_argument("--no-large-tcc", action="store_true")
     p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--profile-tcc", action="store_true",
+                   help="the large-TCC workload's GPU stages only (split-BF16 TCC twice, FP64 TCC, top-48 FP64 "
+                        "eigensolve), for ncu captures")
     p.add_argument("--profile", action="store_true",
                    help="warm-up + timed steps of both forms only (no clock sampling, e2e, CPU or surrogate legs)")
     p.add_argument("--surrogate-epochs", type=int, default=10)
@@ -306,6 +309,23 @@ def batched_leg(ctx, setup, reps=20):
     return res
 
 
+def profile_tcc(device):
+    """The launch sequence an ncu capture of the large-TCC kernels needs: the workload of
+    large_tcc_leg, split-BF16 TCC twice, the FP64 TCC once and its top-48 eigensolve."""
+    import litho_gb300 as LG
+    from litho_gb300 import synth
+    ctx = LG.Context(device)
+    src = synth.annular_source(113, 0.7, 0.95)
+    sig = LG.outer_sigma(src)
+    nx = LG.optics_n(1.35, 2048, sig, 193.0)
+    for _ in range(2):
+        ctx.calc_tcc(src, sig, 193.0, 1.35, 0.0, 2048, 2048, nx, nx, precision=LG.TCC_SPLIT_BF16, n_medium=1.44)
+    tcc = ctx.calc_tcc(src, sig, 193.0, 1.35, 0.0, 2048, 2048, nx, nx, precision=LG.TCC_FP64, n_medium=1.44)
+    ctx.calc_kernels(tcc, 48)
+    ctx.close()
+    print(json.dumps({"profile_tcc": True, "tcc": int(tcc.shape[0]), "K": 48}), flush=True)
+
+
 def large_tcc_leg(ctx):
     """The large-TCC workload: 2048^2 period at 1 nm/px, NA 1.35 (immersion, n = 1.44),
     193 nm, annular source sigma 0.7-0.95 on a 113^2 grid (4,044 points): Nx = 27 by the
@@ -427,6 +447,8 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.profile_tcc:
+        return profile_tcc(local)
     import numpy as np
     import torch
     import litho_gb300 as L
