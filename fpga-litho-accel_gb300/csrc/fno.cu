@@ -1088,40 +1088,41 @@ __global__ void __launch_bounds__(THREADS, 1) row_bwd_kernel(const RowBwd a) {
     sRed[i] = s;  // slot 0 of warp 0 is read only by this thread
   }
   __syncthreads();
-  if (HEAD == HEAD_LIFT) {
+  if constexpr (HEAD == HEAD_LIFT) {
     for (int i = tid; i < C; i += THREADS) {
       gp[Dn::Pb + i] = sRed[i];
       gp[Dn::Pw + i] = sRed[C + i];
     }
     return;
-  }
-  for (int i = tid; i < C; i += THREADS) gp[Dn::Wb + l * C + i] = sRed[i];
-  {
-    const int mt2 = warp >> 2, nt = warp & 3;
-    const int o = 16 * mt2 + g, c = 8 * nt + 2 * t;
-    float* w = gp + Dn::W + l * C * C;
-    w[o * C + c] = dW[0];
-    w[o * C + c + 1] = dW[1];
-    w[(o + 8) * C + c] = dW[2];
-    w[(o + 8) * C + c + 1] = dW[3];
-  }
-  if (HEAD == HEAD_PROJ) {
-    for (int i = tid; i < H; i += THREADS) {
-      gp[Dn::q1b + i] = sRed[2 * C + i];
-      gp[Dn::Q2 + i] = sRed[2 * C + H + i];
+  } else {
+    for (int i = tid; i < C; i += THREADS) gp[Dn::Wb + l * C + i] = sRed[i];
+    {
+      const int mt2 = warp >> 2, nt = warp & 3;
+      const int o = 16 * mt2 + g, c = 8 * nt + 2 * t;
+      float* w = gp + Dn::W + l * C * C;
+      w[o * C + c] = dW[0];
+      w[o * C + c + 1] = dW[1];
+      w[(o + 8) * C + c] = dW[2];
+      w[(o + 8) * C + c + 1] = dW[3];
     }
-    if (tid == 0) gp[Dn::q2b] = sRed[2 * C + 2 * H];
+    if (HEAD == HEAD_PROJ) {
+      for (int i = tid; i < H; i += THREADS) {
+        gp[Dn::q1b + i] = sRed[2 * C + i];
+        gp[Dn::Q2 + i] = sRed[2 * C + H + i];
+      }
+      if (tid == 0) gp[Dn::q2b] = sRed[2 * C + 2 * H];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int tile = 4 * warp + q, mh = tile >> 2, nt = tile & 3;
-      const int h = 16 * mh + g, c = 8 * nt + 2 * t;
-      float* w = gp + Dn::Q1;
-      w[h * C + c] = dQ1[q][0];
-      w[h * C + c + 1] = dQ1[q][1];
-      w[(h + 8) * C + c] = dQ1[q][2];
-      w[(h + 8) * C + c + 1] = dQ1[q][3];
+      for (int q = 0; q < 4; ++q) {
+        const int tile = 4 * warp + q, mh = tile >> 2, nt = tile & 3;
+        const int h = 16 * mh + g, c = 8 * nt + 2 * t;
+        float* w = gp + Dn::Q1;
+        w[h * C + c] = dQ1[q][0];
+        w[h * C + c + 1] = dQ1[q][1];
+        w[(h + 8) * C + c] = dQ1[q][2];
+        w[(h + 8) * C + c + 1] = dQ1[q][3];
+      }
     }
-  }
+  }  // HEAD != HEAD_LIFT
 }
 
 // dense partials -> gradient vector
