@@ -93,7 +93,7 @@ def main(argv=None):
     rep["alpha"] = alpha
     rep["calib_err_quantiles"] = np.quantile(raw_err, [0.5, 0.9, 0.99, 1.0]).tolist()
 
-    # held-out evaluation, SOCS as the judge
+    # held-out evaluation against SOCS images
     errs, ests, used = [], [], []
     for s0 in range(0, a.eval, 256):
         img, est, u = model.image(ks, em[s0:s0 + 256], a.threshold)
