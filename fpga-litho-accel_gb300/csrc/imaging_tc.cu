@@ -492,8 +492,9 @@ struct FiTC {
   // B stages and staging tiles per epilogue group: three and two whenever shared
   // memory holds them (K = 64 rows with 128-column tiles does not)
   static constexpr bool ROOMY = KBLK == 1 || BN <= 64;
-  static constexpr int NS = ROOMY ? 3 : 2;
-  static constexpr int NOUT = KBLK == 1 && BN == 128 ? 3 : (ROOMY ? 2 : 1);
+  static constexpr bool WIDE_OUT = KBLK == 1 && BN == 128;  // two B stages, four staging tiles per group
+  static constexpr int NS = WIDE_OUT ? 2 : (ROOMY ? 3 : 2);
+  static constexpr int NOUT = WIDE_OUT ? 4 : (ROOMY ? 2 : 1);
   static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
   static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
@@ -896,6 +897,7 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   LITHO_RET(make_map(ctx, &mTh, tmh, 3, KP, g.Lx, p.batch, BN));
   LITHO_RET(make_map(ctx, &mTl, tml, 3, KP, g.Lx, p.batch, BN));
   LITHO_RET(make_map(ctx, &mO, images, 3, g.Lx, g.Ly, p.batch, 128));
+  static_assert(FiTC<KBLK, BN>::SMEM <= 227 * 1024, "FI tiles exceed the shared memory of one CTA");
   const size_t smem = FiTC<KBLK, BN>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
