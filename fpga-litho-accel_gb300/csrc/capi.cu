@@ -1,6 +1,7 @@
 // C ABI of liblitho_gb300.so: contexts, host/device staging and the imaging
 // entry points.  TCC and eigensolver entry points live in tcc.cu / eig.cu.
 #include "litho_internal.cuh"
+#include "host_chunks.hpp"
 
 #include <cmath>
 #include <cstring>
@@ -295,27 +296,12 @@ int default_conv_n(int Nx, int Ny) {
 // the chunk sizes ramp 1, 2, 4, ... masks up at the start and back down at the
 // end (the host link, not the copy engines, bounds both directions: SM loads
 // and stores on mapped host memory reach the same rates).
-static void chunk_schedule(int batch, int CH, std::vector<int>& sizes) {
-  std::vector<int> ramp;
-  int used = 0;
-  for (int r = 1; r < CH && 2 * (used + r) + CH <= batch; r *= 2) {
-    ramp.push_back(r);
-    used += r;
-  }
-  sizes.assign(ramp.begin(), ramp.end());
-  for (int mid = batch - 2 * used; mid > 0; mid -= CH) sizes.push_back(std::min(CH, mid));
-  sizes.insert(sizes.end(), ramp.rbegin(), ramp.rend());
-}
-
 static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
                       float* images, int precision, size_t img) {
   constexpr int NS = HB_SLOTS;
-  // chunks of up to ~16 MB (enough masks per launch in the steady state) and at
-  // least ~8 chunks, so small images pipeline too
-  const size_t ch_cap = std::min<size_t>(((size_t)16 << 20) / img, ((size_t)batch + 7) / 8);
-  const int CH = (int)std::max<size_t>(1, ch_cap);
+  const int CH = litho::host_chunk_masks(batch, img);
   std::vector<int> sizes;
-  chunk_schedule(batch, CH, sizes);
+  litho::chunk_schedule(batch, CH, sizes);
   if (ctx->copy_in == nullptr) {
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
     LITHO_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
