@@ -20,6 +20,7 @@
 //                   lower triangle its conjugate mirror (litho.cpp:510-515).
 #include "litho_internal.cuh"
 #include "tc_common.cuh"
+#include "tcc_tiles.hpp"
 
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -234,23 +235,10 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   const int Kp = ((2 * ns + 63) / 64) * 64;
   const size_t op = (size_t)Kp * sizeof(__nv_bfloat16);
   const int ldc = (n + 3) & ~3;  // 16-byte rows for the epilogue's vector stores
-  // C = A A_top^T with A = [X; Y] (2n rows): rows < n hold X X^T (the real part,
-  // symmetric), rows >= n hold Y X^T (the imaginary part, antisymmetric).  The TCC
-  // reads C[a][b] with a <= b and C[n + a][b] with a < b, so only the tiles that
-  // hold such entries are computed (about half), in 12 x 12 blocks of tiles that
-  // share their A and B panels in L2.
-  const int MT = (2 * n + 127) / 128, NT = (n + 127) / 128;
-  std::vector<int2> tiles;
-  for (int mb = 0; mb < MT; mb += 12)
-    for (int nb = 0; nb < NT; nb += 12)
-      for (int mt = mb; mt < std::min(MT, mb + 12); ++mt)
-        for (int nt = nb; nt < std::min(NT, nb + 12); ++nt) {
-          const int r0 = mt * 128, r1 = std::min(r0 + 128, 2 * n);
-          const int cmax = std::min(nt * 128 + 127, n - 1);
-          const bool top = r0 < n && r0 <= cmax;
-          const bool bottom = r1 > n && std::max(r0, n) - n < cmax;
-          if (top || bottom) tiles.push_back(make_int2(mt, nt));
-        }
+  // only the output tiles the TCC assembly reads (about half), in L2-friendly blocks
+  const std::vector<TileMN> need = tcc_needed_tiles(n);
+  std::vector<int2> tiles(need.size());
+  for (size_t i = 0; i < need.size(); ++i) tiles[i] = make_int2(need[i].m, need[i].n);
   // A: 2n rows (hi, lo); B is A's first n rows; C: 2n x ldc fp32; the tile list
   const size_t cbytes = (size_t)2 * n * ldc * sizeof(float);
   LITHO_RET(ctx->mx_c.ensure(ctx, op * 4 * (size_t)n + cbytes + tiles.size() * sizeof(int2) + 4096));
