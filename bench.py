@@ -70,6 +70,9 @@ def parse():
     p.add_argument("--profile-tcc", action="store_true",
                    help="the large-TCC workload's GPU stages only (split-BF16 TCC twice, FP64 TCC, top-48 FP64 "
                         "eigensolve), for ncu captures")
+    p.add_argument("--profile-surrogate", action="store_true",
+                   help="the surrogate's kernels only (forward passes, predictions with the error estimate and "
+                        "Adam steps on seeded 256^2 masks, --batch masks), for ncu captures")
     p.add_argument("--profile", action="store_true",
                    help="warm-up + timed steps of both forms only (no clock sampling, e2e, CPU or surrogate legs)")
     p.add_argument("--surrogate-epochs", type=int, default=10)
@@ -100,11 +103,33 @@ def job_images_per_s(world, batch, steps, seconds):
     return world * batch * steps / seconds
 
 
+def load_synth():
+    """The seeded mask and source generators (litho_gb300/synth.py, numpy only), loaded by
+    file path so that the package's __init__ -- which maps liblitho_gb300.so -- does not run:
+    the reference arm must not load the product library."""
+    import importlib.util
+    path = os.path.join(ROOT, "fpga-litho-accel_gb300", "litho_gb300", "synth.py")
+    spec = importlib.util.spec_from_file_location("litho_bench_synth", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def make_masks(n, seed0=100):
     import numpy as np
-    from litho_gb300 import synth
+    synth = load_synth()
     base = [synth.manhattan_mask(L_SIZE, seed=seed0 + i) for i in range(min(n, 8))]
     return np.stack([base[i % len(base)] for i in range(n)])
+
+
+def bench_config(nx, npts, batch, form):
+    """The workload's config, identical in both arms' lines."""
+    gib = batch * 4 * L_SIZE * L_SIZE / 2 ** 30
+    return {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "source_points": npts,
+            "batch_per_step": batch, "form": form,
+            "forms": "mixed = split-BF16 tcgen05 TCC + FP64 eigensolve + split-TF32 tcgen05 DFTs; "
+                     "plain = FP64 TCC + FP64 eigensolve + FP32 CUDA-core DFTs; both FP32 FFTs",
+            "l2": f"inputs larger than L2 ({gib:g} GiB in + {gib:g} GiB out per step), no flush"}
 
 
 class Clocks:
@@ -211,13 +236,17 @@ def cpu_leg(setup, masks_h, gpu_images, budget):
 
 
 def run_reference(args, ws, rank):
-    """The reference CPU algorithm on the host cores, one bounded sample per step."""
+    """The reference CPU algorithm on the host cores, one bounded sample per step.
+
+    The path is litho.cpp's Modules 3 + 7 (FT_r2c_padded + calcSOCS + FI) restated
+    in FP64 with scipy.fft on all host cores (oracle/cpu_socs.py); the reference's own
+    build cannot travel to the GPU host.  The kernels come from the FP64 oracle of
+    calcTCC + calcKernels for the same quasar source.  Only rank 0 works."""
     if rank != 0:
         return
-    import numpy as np
-    from litho_gb300 import synth
     from oracle import np_ref as R
     from oracle import cpu_socs
+    synth = load_synth()
     src, S, npts = synth.quasar_source(2000)
     sig = R.get_outer_sigma(src)
     nx = R.optics_nx(NA, L_SIZE, sig, WAVELENGTH)
@@ -235,14 +264,16 @@ def run_reference(args, ws, rank):
             cpu_socs.socs_image(m, krn, scales, nx, nx, workers=cores)
     el = time.perf_counter() - t0
     v = per_step * args.steps / el
+    head = "plain" if args.precision == "fp32" else "mixed"
     line = {"metric": METRIC, "value": v, "unit": "images/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "per_step_images": per_step},
+            "config": bench_config(nx, npts, args.batch, head),
             "cpu_baseline": {"value": v, "unit": "images/s", "cores": cores, "kind": "port",
-                             "sample": f"{per_step} masks per step x {args.steps} steps: FT_r2c_padded + calcSOCS "
-                                       f"(128^2 conv grid, embed 94) + FI in FP64, scipy.fft workers={cores}"},
+                             "sample": f"{per_step} masks of the workload per step x {args.steps} steps: "
+                                       "FT_r2c_padded (r2c + half-spectrum rebuild) + calcSOCS (128^2 conv grid, "
+                                       f"embed 94) + FI in FP64, scipy.fft workers={cores}"},
             "e2e": {"value": v, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -324,6 +355,32 @@ def profile_tcc(device):
     ctx.calc_kernels(tcc, 48)
     ctx.close()
     print(json.dumps({"profile_tcc": True, "tcc": int(tcc.shape[0]), "K": 48}), flush=True)
+
+
+def profile_surrogate(device, batch, steps):
+    """The launch sequence an ncu capture of the surrogate kernels needs: forward passes,
+    predictions with the error estimate and Adam steps of a 256^2 FNO on seeded masks."""
+    import torch
+    import litho_gb300 as LG
+    from litho_gb300 import surrogate as S
+    ctx = LG.Context(device)
+    ks, _ = S.c5_kernel_set(ctx, 256)
+    model = S.Surrogate(ctx, L=256, seed=1)
+    m = S.rect_masks(ctx, 1, 0, batch, 256)
+    out = torch.empty_like(m)
+    for _ in range(steps):
+        model.forward(m, out)
+    for _ in range(steps):
+        model.predict(ks, m, out)
+    tb = min(32, batch)
+    mt, tt = m[:tb].contiguous(), torch.rand_like(m[:tb])
+    for _ in range(steps):
+        model.train_step(mt, tt, 1e-4, want_loss=False)
+    torch.cuda.synchronize()
+    model.close()
+    ks.close()
+    ctx.close()
+    print(json.dumps({"profile_surrogate": True, "batch": batch, "steps": steps}), flush=True)
 
 
 def large_tcc_leg(ctx):
@@ -449,6 +506,8 @@ def main():
         return run_reference(args, ws, rank)
     if args.profile_tcc:
         return profile_tcc(local)
+    if args.profile_surrogate:
+        return profile_surrogate(local, args.batch, args.steps)
     import numpy as np
     import torch
     import litho_gb300 as L
@@ -568,11 +627,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "tf32x3/f32" if head == "mixed" else "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "L": L_SIZE, "K": K_KERNELS, "Nx": nx, "source_points": npts,
-                       "batch_per_step": B, "form": head,
-                       "forms": "mixed = split-BF16 tcgen05 TCC + FP64 eigensolve + split-TF32 tcgen05 DFTs; "
-                                "plain = FP64 TCC + FP64 eigensolve + FP32 CUDA-core DFTs; both FP32 FFTs",
-                       "l2": "inputs larger than L2 (256 MB in + 256 MB out per step)"},
+            "config": bench_config(nx, npts, B, head),
             "gpu_launches": int(launches),
             "forms": forms,
             "mixed_over_plain": forms["mixed"]["images_per_s"] / forms["plain"]["images_per_s"],

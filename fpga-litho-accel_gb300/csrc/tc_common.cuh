@@ -10,9 +10,10 @@
 // CU_TENSOR_MAP_SWIZZLE_128B with a 128-byte inner box, and one MMA's K slice
 // (32 bytes) is selected by advancing the descriptor start address.
 //
-// Every wait is bounded: mbar_wait gives up after `limit` polls (~0.5 s with
-// the nanosleep back-off) and returns false; callers set an error flag, drain
-// what they issued and return instead of spinning forever.
+// Every wait is bounded: mbar_wait polls mbarrier.try_wait (no suspend-time
+// hint) until the phase completes or `limit` milliseconds of %globaltimer have
+// passed (1000 ms by default), and then returns false; callers set an error
+// flag, drain what they issued and return instead of spinning forever.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>

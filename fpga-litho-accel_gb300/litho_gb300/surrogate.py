@@ -210,38 +210,3 @@ def rel_l2_per_image(a, b):
     import torch
     d = torch.linalg.vector_norm((a - b).reshape(a.shape[0], -1), dim=1)
     return d / torch.linalg.vector_norm(b.reshape(b.shape[0], -1), dim=1)
-
-
-def _profile_main(argv=None):
-    """python -m litho_gb300.surrogate [--L 256] [--batch 64] [--steps 3]: forward passes,
-    predictions with the estimate and Adam steps on seeded masks -- the launch sequence
-    that kernel profiles of the surrogate are taken on."""
-    import argparse
-    import torch
-    from . import Context
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--L", type=int, default=256)
-    ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--train-batch", type=int, default=32)
-    ap.add_argument("--steps", type=int, default=3)
-    a = ap.parse_args(argv)
-    ctx = Context(0)
-    ks, _ = c5_kernel_set(ctx, a.L)
-    model = Surrogate(ctx, L=a.L, seed=1)
-    m = rect_masks(ctx, 1, 0, a.batch, a.L)
-    out = torch.empty_like(m)
-    for _ in range(a.steps):
-        model.forward(m, out)
-    for _ in range(a.steps):
-        model.predict(ks, m, out)
-    tb = min(a.train_batch, a.batch)
-    mt, tt = m[:tb].contiguous(), torch.rand_like(m[:tb])
-    for _ in range(a.steps):
-        model.train_step(mt, tt, 1e-4, want_loss=False)
-    torch.cuda.synchronize()
-    print("surrogate profile run done", flush=True)
-    ctx.close()
-
-
-if __name__ == "__main__":
-    _profile_main()

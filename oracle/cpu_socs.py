@@ -7,7 +7,8 @@ on the host cores), never by the product.
 For one mask it runs, in FP64 exactly as the reference orders the work:
 
 * ``FT_r2c_padded`` (litho.cpp:242-318): centre-pad, roll, r2c over the full
-  F x F grid, rebuild the centred spectrum;
+  F x F grid (half spectrum [F][F/2+1]), rebuild the centred full spectrum from
+  it by Hermitian symmetry (``rebuild_centred``), divide by F^2;
 * ``calcSOCS`` (litho.cpp:795-1006): for each of the K kernels, embed K_k*M in a
   128 x 128 grid at offset 94, unnormalised backward c2c, accumulate
   s_k |E|^2; fftshift;
@@ -29,6 +30,25 @@ import scipy.fft as sfft
 from . import np_ref as R
 
 
+def rebuild_centred(half: np.ndarray, Fx: int, Fy: int) -> np.ndarray:
+    """The full centred spectrum from an r2c half spectrum, as litho.cpp:264-312 does:
+    R = the half spectrum with its rows rolled so DC lands at row Fy/2; the left half
+    mirrors R by Hermitian symmetry; the right half is R itself from column Fx/2 on."""
+    wt = Fx // 2 + 1
+    ay = (Fy + 1) // 2
+    r = np.concatenate([half[ay:], half[:ay]], axis=0)
+    left = np.empty_like(r)
+    if Fy % 2 == 0:
+        left[0] = np.conj(r[0, ::-1])
+        left[1:] = np.conj(r[:0:-1, ::-1])
+    else:
+        left[:] = np.conj(r[::-1, ::-1])
+    out = np.empty((Fy, Fx), np.complex128)
+    out[:, :wt] = left
+    out[:, Fx // 2:] = r[:, :Fx - Fx // 2]
+    return out
+
+
 def socs_image(mask: np.ndarray, krns: np.ndarray, scales: np.ndarray, Nx: int, Ny: int,
                conv_n: int = 128, embed: int = 94, workers: int | None = None) -> np.ndarray:
     workers = workers or os.cpu_count() or 1
@@ -36,8 +56,8 @@ def socs_image(mask: np.ndarray, krns: np.ndarray, scales: np.ndarray, Nx: int, 
     Fx, Fy = R.next_pow2(Lx), R.next_pow2(Ly)
     padded = R.pad_centered(mask.astype(np.float32), Fx, Fy)
     shifted = R.my_shift(padded, False, False).astype(np.float64)
-    spec = sfft.fft2(shifted, workers=workers)            # == rebuilt half spectrum (even F)
-    mskf = np.fft.fftshift(spec) / (Fx * Fy)
+    half = sfft.rfft2(shifted, workers=workers)
+    mskf = rebuild_centred(half, Fx, Fy) / (Fx * Fy)
     K = len(scales)
     kx_, ky_ = 2 * Nx + 1, 2 * Ny + 1
     win = mskf[Fy // 2 - Ny:Fy // 2 + Ny + 1, Fx // 2 - Nx:Fx // 2 + Nx + 1]
