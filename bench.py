@@ -434,6 +434,7 @@ def large_tcc_leg(ctx):
         i = j
     err["kernel_projector"] = proj
     res["split_bf16_vs_fp64"] = err
+    res["gemm_tuning"] = [t for t in ctx.tcc_gemm_tuning() if t["n"] == (2 * nx + 1) ** 2]
     return res
 
 

@@ -168,6 +168,13 @@ int litho_ctx_enable_timing(litho_ctx* ctx, int enable) {
   return LITHO_OK;
 }
 
+int litho_ctx_set_test_stall(litho_ctx* ctx, int chunk) {
+  if (ctx == nullptr) return LITHO_ERR_ARG;
+  LITHO_ARG_CHECK(ctx, chunk >= -1, "chunk must be >= -1 (-1 turns the hook off)");
+  ctx->test_stall_chunk = chunk;
+  return LITHO_OK;
+}
+
 int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int reset) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

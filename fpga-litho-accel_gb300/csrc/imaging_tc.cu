@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
                                                                    int rows, int batch, int ncs, int S,
                                                                    const float2* __restrict__ ytab,
                                                                    float2* __restrict__ win_part, int part_stride,
-                                                                   int* __restrict__ err) {
+                                                                   int* __restrict__ err, int stall_at) {
   using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -245,6 +245,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         int img, rb, cs, c0, c1;
         decode(t, img, rb, cs, c0, c1);
         for (int c = c0; c < c1; ++c, ++q) {
+          if (q == stall_at) {  // error-path test hook: the producer is lost here
+            ok = false;
+            break;
+          }
           if (q >= S && !mbar_wait_ab(&empty[s], ph ^ 1u, abort)) {
             *abort = 1;
             ok = false;
@@ -866,7 +870,7 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, rows,
                                                                   p.batch, ncs, S,
                                                                   reinterpret_cast<const float2*>(yt), win_part,
-                                                                  p.part_stride, err);
+                                                                  p.part_stride, err, ctx->test_stall_chunk);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }

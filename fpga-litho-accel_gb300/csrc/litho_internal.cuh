@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <string>
 #include <map>
+#include <memory>
 #include <tuple>
 #include <vector>
 
@@ -86,6 +87,18 @@ __device__ __forceinline__ float2 sum_strided(const float2* __restrict__ p, size
                      ((a[0].y + a[1].y) + (a[2].y + a[3].y)) + ((a[4].y + a[5].y) + (a[6].y + a[7].y)));
 }
 
+// Autotuned shape of the split-BF16 TCC GEMM for one (n, Kp): column tile width,
+// schedule (0 = whole tiles only, 1 = last tiles split along K) and every
+// candidate's measured time.
+struct TccTune {
+  struct Cand {
+    int bn, split;
+    float ms;
+  };
+  int bn = 128, split = 0;
+  std::vector<Cand> cands;
+};
+
 inline int next_pow2(int x) {
   int p = 1;
   while (p < x) p <<= 1;
@@ -124,6 +137,14 @@ struct litho_ctx {
   struct Pending { int stage; cudaEvent_t a, b; };
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> event_pool;
+  // split-BF16 TCC GEMM: tuned shape per (n, Kp) and device schedule tables per
+  // (n, K slices, BN, split)
+  std::map<std::pair<int, int>, litho::TccTune> tcc_tune;
+  std::map<std::tuple<int, int, int, int>, std::shared_ptr<void>> gemm_tables;
+  int tcc_force_bn = 0, tcc_force_split = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
+  // error-path test hook (litho_ctx_set_test_stall): >= 0 stops the mixed window
+  // DFT's TMA producer at that chunk of every CTA's work; -1 = off
+  int test_stall_chunk = -1;
 };
 
 struct litho_kernel_set {

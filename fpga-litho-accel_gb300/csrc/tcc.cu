@@ -212,6 +212,8 @@ int build_pupil(litho_ctx* ctx, const std::vector<SrcPt>& pts, const PupilParams
 }
 
 int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int ns, int ldp, double2* tcc);
+cudaError_t launch_nonfinite(cudaStream_t s, const double* x, size_t n, int* flag, int sms);
+int tc_err_flag_public(litho_ctx* ctx, int** flag);
 
 }  // namespace litho
 
@@ -273,15 +275,24 @@ int litho::calc_tcc_impl(litho_ctx* ctx, const float* src, int srcSize, float ou
     }
   }
   if (mem == LITHO_MEM_HOST) {
+    // finiteness is checked on the device while the result is still there
+    int* flag = nullptr;
+    LITHO_RET(tc_err_flag_public(ctx, &flag));
+    flag += 32;  // past the tensor-core kernels' timeout flag
+    LITHO_CUDA_TRY(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+    LITHO_CUDA_TRY(ctx, launch_nonfinite(ctx->stream, reinterpret_cast<const double*>(out), (size_t)2 * n * n, flag,
+                                         ctx->sm_count));
+    int bad = 0;
+    LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(tcc, out, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    for (size_t i = 0; i < (size_t)2 * n * n; ++i)
-      if (!std::isfinite(tcc[i])) {
-        set_error(ctx, LITHO_ERR_NAN,
-                  "non-finite TCC entry (NA > n_medium makes the pupil phase NaN, litho.cpp:463; "
-                  "litho_calc_tcc_medium takes an immersion index)");
-        return LITHO_ERR_NAN;
-      }
+    if (tccPrecision == LITHO_TCC_SPLIT_BF16) LITHO_RET(tc_check_flag(ctx));
+    if (bad) {
+      set_error(ctx, LITHO_ERR_NAN,
+                "non-finite TCC entry (NA > n_medium makes the pupil phase NaN, litho.cpp:463; "
+                "litho_calc_tcc_medium takes an immersion index)");
+      return LITHO_ERR_NAN;
+    }
   }
   return LITHO_OK;
 }

@@ -11,11 +11,15 @@
 // split_kernel      P (complex float), J -> Ah/Al = [X; Y], BF16, K-major rows
 //                   padded to Kp (multiple of 64); the B operand X is A's first
 //                   n rows (tensor maps over the same memory).
-// gemm_bf16x3_kernel  128 x 128 output tile per CTA (only the tiles the TCC
-//                   reads), K streamed in 64-wide (128-byte) slices through a
-//                   3-stage TMA/mbarrier ring; a producer lane refills the ring
-//                   while the MMA lane issues 12 MMAs per slice; epilogue
-//                   tcgen05.ld -> FP32 C.
+// gemm_bf16x3_kernel  persistent, one CTA per SM over the 128 x BN output tiles
+//                   the TCC reads (BN = 64, 128 or 256), K streamed in 64-wide
+//                   (128-byte) slices through a TMA/mbarrier ring; whole tiles in
+//                   data-parallel rounds and, optionally, the last tiles split
+//                   along K over all CTAs (gemm_schedule); a double-buffered TMEM
+//                   accumulator lets the epilogue warps drain one piece while the
+//                   next one's MMAs run.  gemm_fixup_kernel adds the partial sums
+//                   of split tiles in K order.  BN and the schedule are chosen per
+//                   (n, Kp) by timing every candidate on the device (gemm_tune).
 // assemble_kernel   C -> interleaved complex128 TCC: upper triangle from C, the
 //                   lower triangle its conjugate mirror (litho.cpp:510-515).
 #include "litho_internal.cuh"
@@ -26,6 +30,9 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
 #include <vector>
 
 namespace litho {
@@ -66,124 +73,234 @@ __global__ void split_kernel(const float2* __restrict__ P, const float* __restri
   *reinterpret_cast<uint4*>(Al + (size_t)(n + i) * Kp + k0) = *reinterpret_cast<const uint4*>(yl);
 }
 
-constexpr int GB_STAGES = 3;
-constexpr uint32_t GB_TILE = 128 * 128;          // 128 rows x 64 bf16
-constexpr uint32_t GB_STAGE_B = 4 * GB_TILE;     // Ah, Al, Bh, Bl
-constexpr size_t GB_SMEM = 1024 + (size_t)GB_STAGES * GB_STAGE_B + 256;
+// Persistent split-BF16 GEMM C = A B^T over a list of 128 x BN output tiles.  One CTA
+// per SM runs the pieces (GemmSeg: a tile and a range of its 64-wide K slices) the
+// host schedule gives it.  Roles (192 threads):
+//   warp 0 lane 0 : TMA producer, streams [Ah | Al | Bh | Bl] K slices through an
+//                   NS-stage ring (full[s] / empty[s])
+//   warp 1 lane 0 : MMA issuer, hi*hi + hi*lo + lo*hi per 16-wide K step into one
+//                   of two TMEM accumulators (accfull / accempty), so a piece's
+//                   epilogue overlaps the next piece's main loop
+//   warps 2-5     : epilogue, one TMEM lane quarter per warp (warp % 4): 32 columns
+//                   per tcgen05.ld, 16-byte stores to C (whole tiles) or to the
+//                   piece's partial slot (split tiles, added by gemm_fixup_kernel)
+// Every wait is bounded; a role whose wait gives up sets the abort flag and the
+// others' waits then return at once, the producer's issued loads are waited for,
+// TMEM is freed and the error flag is raised.
+template <int BN>
+struct GemmCfg {
+  static constexpr uint32_t A_T = 128 * 128;          // 128 rows x 64 bf16 (SWIZZLE_128B)
+  static constexpr uint32_t B_T = BN * 128;           // BN rows x 64 bf16
+  static constexpr uint32_t STAGE = 2 * A_T + 2 * B_T;  // Ah, Al, Bh, Bl
+  static constexpr int NS = (int)((192u * 1024u) / STAGE);  // 4, 3, 2 stages at BN = 64, 128, 256
+  static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 512;
+  static constexpr uint32_t TCOLS = 2 * BN;           // two accumulators
+};
+constexpr int GB_THREADS = 192;
 
-// One 128 x 128 tile of C = A B^T per CTA, the tile taken from a list (only the
-// tiles the TCC reads, in blocks that share operand panels in L2).  Warp 0 lane 0
-// streams the K slices through the TMA ring, warp 1 lane 0 issues the MMAs as the
-// slices land (so the tensor pipe is not idle while a stage is refilled), then all
-// four warps drain TMEM with 16-byte stores (ldc a multiple of 4).
-__global__ void __launch_bounds__(128, 1) gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tAh,
-                                                             const __grid_constant__ CUtensorMap tAl,
-                                                             const __grid_constant__ CUtensorMap tBh,
-                                                             const __grid_constant__ CUtensorMap tBl,
-                                                             const int2* __restrict__ tiles, int M, int N,
-                                                             int Kp, float* __restrict__ C, int ldc,
-                                                             int* __restrict__ err) {
+template <int BN>
+__global__ void __launch_bounds__(GB_THREADS, 1) gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tAh,
+                                                                    const __grid_constant__ CUtensorMap tAl,
+                                                                    const __grid_constant__ CUtensorMap tBh,
+                                                                    const __grid_constant__ CUtensorMap tBl,
+                                                                    const int4* __restrict__ segs,
+                                                                    const int* __restrict__ seg_begin,
+                                                                    const int2* __restrict__ tiles, int M, int N,
+                                                                    float* __restrict__ C, int ldc,
+                                                                    float* __restrict__ part,
+                                                                    int* __restrict__ err) {
+  using P = GemmCfg<BN>;
+  constexpr int NS = P::NS;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sm + GB_STAGES * GB_STAGE_B);
-  uint64_t* empty = full + GB_STAGES;
-  uint64_t* done = empty + GB_STAGES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)NS * P::STAGE);
+  uint64_t* empty = full + NS;
+  uint64_t* accfull = empty + NS;   // [2]
+  uint64_t* accempty = accfull + 2;  // [2]
+  uint64_t* done = accempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-  int* s_bad = reinterpret_cast<int*>(tslot + 1);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [NS]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int2 tl = tiles[blockIdx.x];
-  const int m0 = tl.x * 128, n0 = tl.y * 128;
-  const int nch = Kp / 64;
+  const int sb = seg_begin[blockIdx.x], se = seg_begin[blockIdx.x + 1];
 
-  if (warp == 0) tmem_alloc(tslot, 128);
+  if (warp == 0) tmem_alloc(tslot, P::TCOLS);
   if (tid == 0) {
-    for (int s = 0; s < GB_STAGES; ++s) {
+    for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+      last_issued[s] = -1;
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], 4);  // one arrival per epilogue warp
     }
     mbar_init(done, 1);
-    *s_bad = 0;
+    *abort = 0;
     fence_mbar_init();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  auto tile = [&](int s, int q) { return sm + (size_t)s * GB_STAGE_B + (size_t)q * GB_TILE; };
-  volatile int* bad = s_bad;
-  if (tid == 0) {  // TMA producer
-    int issued = 0;
-    for (; issued < nch; ++issued) {
-      const int s = issued % GB_STAGES;
-      if (issued >= GB_STAGES &&
-          !mbar_wait_ab(&empty[s], (uint32_t)(issued / GB_STAGES - 1) & 1u, bad))
-        break;
-      mbar_arrive_expect_tx(&full[s], GB_STAGE_B);
-      tma_load_2d(tile(s, 0), &tAh, &full[s], 64 * issued, m0);
-      tma_load_2d(tile(s, 1), &tAl, &full[s], 64 * issued, m0);
-      tma_load_2d(tile(s, 2), &tBh, &full[s], 64 * issued, n0);
-      tma_load_2d(tile(s, 3), &tBl, &full[s], 64 * issued, n0);
-    }
-    if (issued < nch) {
-      *bad = 1;
-      // wait (bounded) for the loads still in flight before the CTA leaves
-      for (int k = (issued > GB_STAGES ? issued - GB_STAGES : 0); k < issued; ++k)
-        mbar_wait(&full[k % GB_STAGES], (uint32_t)(k / GB_STAGES) & 1u, 200u);
-    }
-  } else if (tid == 32) {  // MMA issuer
-    constexpr uint32_t IDESC = idesc_bf16(128, 128);
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % GB_STAGES;
-      if (!mbar_wait_ab(&full[s], (uint32_t)(c / GB_STAGES) & 1u, bad)) {
-        *bad = 1;
-        break;
+  auto tile = [&](int s, int q) {  // q: 0 Ah, 1 Al, 2 Bh, 3 Bl
+    return sm + (size_t)s * P::STAGE + (q < 2 ? (size_t)q * P::A_T : 2 * (size_t)P::A_T + (size_t)(q - 2) * P::B_T);
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      int q = 0, s = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      for (int i = sb; i < se && ok; ++i) {
+        const int4 g = segs[i];
+        const int2 t = tiles[g.x];
+        const int m0 = 128 * t.x, n0 = BN * t.y;
+        for (int k = g.y; k < g.z; ++k, ++q) {
+          if (q >= NS && !mbar_wait_ab(&empty[s], ph ^ 1u, abort)) {
+            *abort = 1;
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], P::STAGE);
+          tma_load_2d(tile(s, 0), &tAh, &full[s], 64 * k, m0);
+          tma_load_2d(tile(s, 1), &tAl, &full[s], 64 * k, m0);
+          tma_load_2d(tile(s, 2), &tBh, &full[s], 64 * k, n0);
+          tma_load_2d(tile(s, 3), &tBl, &full[s], 64 * k, n0);
+          last_issued[s] = q;
+          if (++s == NS) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
       }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      constexpr uint32_t IDESC = idesc_bf16(128, BN);
+      int s = 0, tl = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      for (int i = sb; i < se && ok; ++i, ++tl) {
+        const int4 g = segs[i];
+        const int buf = tl & 1;
+        if (tl >= 2 && !mbar_wait_ab(&accempty[buf], (uint32_t)((tl - 2) >> 1) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(buf * BN);
+        for (int k = g.y; k < g.z; ++k) {
+          if (!mbar_wait_ab(&full[s], ph, abort)) {
+            *abort = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t dah = desc_sw128(tile(s, 0)), dal = desc_sw128(tile(s, 1));
+          const uint64_t dbh = desc_sw128(tile(s, 2)), dbl = desc_sw128(tile(s, 3));
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint32_t off = kk * 32;  // 16 bf16 per MMA
+            mma_bf16(acc, desc_add(dah, off), desc_add(dbh, off), IDESC, (k != g.y || kk != 0) ? 1u : 0u);
+            mma_bf16(acc, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
+            mma_bf16(acc, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
+          }
+          mma_commit(&empty[s]);
+          if (++s == NS) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (ok) mma_commit(&accfull[buf]);  // arrives when this piece's MMAs have completed
+      }
+      mma_commit(done);  // arrives once everything issued above has completed
+      // bounded, and it starts after the last MMA was issued; the other threads meet
+      // this lane at the block barrier below instead of timing the whole kernel
+      if (!mbar_wait(done, 0)) *abort = 1;
+    }
+  } else {  // warps 2-5: epilogue
+    const int quarter = warp & 3;
+    const int r = 32 * quarter + lane;  // this thread's row of the tile (its TMEM lane)
+    int tl = 0;
+    for (int i = sb; i < se; ++i, ++tl) {
+      const int4 g = segs[i];
+      const int2 t = tiles[g.x];
+      const int buf = tl & 1;
+      // on a wait that gives up: flag it and carry on (later waits return at once)
+      if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) *abort = 1;
       tc_fence_after();
-      const uint64_t dah = desc_sw128(tile(s, 0)), dal = desc_sw128(tile(s, 1));
-      const uint64_t dbh = desc_sw128(tile(s, 2)), dbl = desc_sw128(tile(s, 3));
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        const uint32_t off = kk * 32;  // 16 bf16 per MMA
-        mma_bf16(tmem, desc_add(dah, off), desc_add(dbh, off), IDESC, (c | kk) != 0 ? 1u : 0u);
-        mma_bf16(tmem, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
-        mma_bf16(tmem, desc_add(dal, off), desc_add(dbh, off), IDESC, 1u);
-      }
-      mma_commit(&empty[s]);
-    }
-    mma_commit(done);  // arrives once everything issued above has completed
-  }
-  __syncwarp();
-  if (!mbar_wait(done, 0)) *bad = 1;
-  if (__syncthreads_or(*bad)) {
-    if (tid == 0) atomicExch(err, 1);
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 128);
-    return;
-  }
-  tc_fence_after();
-  const int row = m0 + 32 * warp + lane;
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+      const uint32_t trow = tmem + (uint32_t)(buf * BN) + ((uint32_t)(32 * quarter) << 16);
+      const int row = 128 * t.x + r, n0 = BN * t.y;
 #pragma unroll 1
-  for (int slab = 0; slab < 4; ++slab) {
-    float v[32];
-    tmem_ld32(trow + (uint32_t)(slab * 32), v);
-    const int c0 = n0 + slab * 32;
-    if (row < M && c0 < N) {
-      float* out = C + (size_t)row * ldc + c0;
-      if (c0 + 32 <= ldc) {
+      for (int slab = 0; slab < BN / 32; ++slab) {
+        float v[32];
+        tmem_ld32(trow + (uint32_t)(slab * 32), v);
+        const int c0 = slab * 32;
+        if (g.w >= 0) {  // partial slot: the whole 128 x BN tile, row-major
+          float* out = part + ((size_t)g.w * 128 + r) * BN + c0;
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(out + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-      } else {
+          for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4*>(out + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        } else if (row < M && n0 + c0 < N) {
+          float* out = C + (size_t)row * ldc + n0 + c0;
+          if (n0 + c0 + 32 <= ldc) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (c0 + j < N) out[j] = v[j];
+            for (int j = 0; j < 32; j += 4)
+              *reinterpret_cast<float4*>(out + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (n0 + c0 + j < N) out[j] = v[j];
+          }
+        }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
+    }
+  }
+  __syncthreads();  // the MMA lane has seen `done`: the tensor cores have drained
+  if (*abort) {
+    if (tid == 0) {  // the producer lane: wait for the last load of every stage
+      for (int s = 0; s < NS; ++s)
+        if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / NS) & 1u, 200u);
+      atomicExch(err, 1);
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 128);
+  if (warp == 0) tmem_dealloc(tmem, P::TCOLS);
+}
+
+// Split tiles: C tile = the sum of its partial slots in K order (fixed order, so the
+// result is reproducible).  One CTA per (split tile, 1024 elements), four per thread.
+__global__ void gemm_fixup_kernel(const float* __restrict__ part, const int* __restrict__ fix_tile,
+                                  const int* __restrict__ fix_begin, const int* __restrict__ fix_slot,
+                                  const int2* __restrict__ tiles, int BN, int M, int N, float* __restrict__ C,
+                                  int ldc) {
+  const int f = blockIdx.x;
+  const int e = 4 * (blockIdx.y * blockDim.x + threadIdx.x);
+  if (e >= 128 * BN) return;
+  const int r = e / BN, c = e - r * BN;
+  const int2 t = tiles[fix_tile[f]];
+  const int row = 128 * t.x + r, col = BN * t.y + c;
+  if (row >= M || col >= N) return;
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j = fix_begin[f]; j < fix_begin[f + 1]; ++j) {
+    const float4 v = *reinterpret_cast<const float4*>(part + (size_t)fix_slot[j] * 128 * BN + e);
+    a.x += v.x;
+    a.y += v.y;
+    a.z += v.z;
+    a.w += v.w;
+  }
+  float* out = C + (size_t)row * ldc + col;
+  if (col + 4 <= ldc) {
+    *reinterpret_cast<float4*>(out) = a;
+  } else {
+    const float w[4] = {a.x, a.y, a.z, a.w};
+    for (int j = 0; j < 4 && col + j < N; ++j) out[j] = w[j];
+  }
 }
 
 __global__ void assemble_kernel(const float* __restrict__ C, int n, int ldc, double2* __restrict__ tcc) {
@@ -209,7 +326,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn_bf16() {
   return fn;
 }
 
-static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t cols, uint64_t rows) {
+static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t cols, uint64_t rows,
+                    uint32_t box_rows) {
   auto fn = encode_fn_bf16();
   if (fn == nullptr) {
     set_error(ctx, LITHO_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
@@ -217,7 +335,7 @@ static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t c
   }
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {64, 128};
+  cuuint32_t box[2] = {64, box_rows};
   cuuint32_t es[2] = {1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -231,17 +349,174 @@ static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t c
 
 int tc_err_flag_public(litho_ctx* ctx, int** flag);
 
+// Device copy of one GEMM schedule: the tile list, the CTAs' pieces and the fix-up
+// lists, plus the partial-slot workspace, cached per (n, Kp, BN, split).
+struct GemmTables {
+  ~GemmTables() {
+    buf.release();
+    part.release();
+  }
+  DevBuf buf, part;
+  int ctas = 0, ntiles = 0, nfix = 0, nslots = 0;
+  int2* tiles = nullptr;
+  int4* segs = nullptr;
+  int* seg_begin = nullptr;
+  int *fix_tile = nullptr, *fix_begin = nullptr, *fix_slot = nullptr;
+};
+
+static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, bool split, GemmTables** out) {
+  const auto key = std::make_tuple(n, nk, bn, split ? 1 : 0);
+  auto it = ctx->gemm_tables.find(key);
+  if (it != ctx->gemm_tables.end()) {
+    *out = static_cast<GemmTables*>(it->second.get());
+    return LITHO_OK;
+  }
+  const std::vector<TileMN> need = tcc_needed_tiles(n, bn);
+  const int T = (int)need.size();
+  const int ctas = split ? ctx->sm_count : std::min(ctx->sm_count, T);
+  const GemmSchedule sc = gemm_schedule(T, nk, ctas, split);
+  // one host image of all tables, uploaded once
+  std::vector<int> h;
+  auto put = [&](size_t n_ints) {
+    const size_t off = h.size();
+    h.resize(off + ((n_ints + 3) & ~size_t(3)), 0);  // 16-byte aligned sub-arrays
+    return off;
+  };
+  const size_t o_tiles = put(2 * (size_t)T), o_segs = put(4 * sc.segs.size()), o_beg = put(sc.begin.size()),
+               o_ft = put(sc.fix_tile.size()), o_fb = put(sc.fix_begin.size()), o_fs = put(sc.fix_slot.size());
+  for (int i = 0; i < T; ++i) {
+    h[o_tiles + 2 * i] = need[i].m;
+    h[o_tiles + 2 * i + 1] = need[i].n;
+  }
+  for (size_t i = 0; i < sc.segs.size(); ++i) {
+    h[o_segs + 4 * i] = sc.segs[i].tile;
+    h[o_segs + 4 * i + 1] = sc.segs[i].k0;
+    h[o_segs + 4 * i + 2] = sc.segs[i].k1;
+    h[o_segs + 4 * i + 3] = sc.segs[i].slot;
+  }
+  std::copy(sc.begin.begin(), sc.begin.end(), h.begin() + o_beg);
+  std::copy(sc.fix_tile.begin(), sc.fix_tile.end(), h.begin() + o_ft);
+  std::copy(sc.fix_begin.begin(), sc.fix_begin.end(), h.begin() + o_fb);
+  std::copy(sc.fix_slot.begin(), sc.fix_slot.end(), h.begin() + o_fs);
+  auto t = std::make_shared<GemmTables>();
+  LITHO_RET(t->buf.ensure(ctx, h.size() * sizeof(int) + 16));
+  LITHO_CUDA_TRY(ctx, cudaMemcpy(t->buf.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+  int* d = t->buf.as<int>();
+  t->tiles = reinterpret_cast<int2*>(d + o_tiles);
+  t->segs = reinterpret_cast<int4*>(d + o_segs);
+  t->seg_begin = d + o_beg;
+  t->fix_tile = d + o_ft;
+  t->fix_begin = d + o_fb;
+  t->fix_slot = d + o_fs;
+  t->ctas = ctas;
+  t->ntiles = T;
+  t->nfix = (int)sc.fix_tile.size();
+  t->nslots = sc.nslots;
+  if (sc.nslots > 0) LITHO_RET(t->part.ensure(ctx, (size_t)sc.nslots * 128 * bn * sizeof(float)));
+  ctx->gemm_tables[key] = t;
+  *out = t.get();
+  return LITHO_OK;
+}
+
+// One persistent GEMM of the given shape and schedule (plus the fix-up of split tiles).
+template <int BN>
+static int run_gemm(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16* Al, int n, int Kp, float* C,
+                    int ldc, bool split, int* err) {
+  using P = GemmCfg<BN>;
+  GemmTables* t = nullptr;
+  LITHO_RET(gemm_tables(ctx, n, Kp / 64, BN, split, &t));
+  CUtensorMap mAh, mAl, mBh, mBl;
+  LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n, 128));
+  LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n, 128));
+  LITHO_RET(map_bf16(ctx, &mBh, Ah, Kp, n, BN));  // B = A's first n rows
+  LITHO_RET(map_bf16(ctx, &mBl, Al, Kp, n, BN));
+  static_assert(P::SMEM <= 227 * 1024, "GEMM stages exceed the shared memory of one CTA");
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_bf16x3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)P::SMEM));
+  gemm_bf16x3_kernel<BN><<<t->ctas, GB_THREADS, P::SMEM, ctx->stream>>>(
+      mAh, mAl, mBh, mBl, t->segs, t->seg_begin, t->tiles, 2 * n, n, C, ldc, t->part.as<float>(), err);
+  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  if (t->nfix > 0) {
+    gemm_fixup_kernel<<<dim3(t->nfix, (128 * BN / 4 + 255) / 256), 256, 0, ctx->stream>>>(
+        t->part.as<float>(), t->fix_tile, t->fix_begin, t->fix_slot, t->tiles, BN, 2 * n, n, C, ldc);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  }
+  return LITHO_OK;
+}
+
+static int run_gemm_shape(litho_ctx* ctx, int bn, bool split, const __nv_bfloat16* Ah, const __nv_bfloat16* Al,
+                          int n, int Kp, float* C, int ldc, int* err) {
+  switch (bn) {
+    case 64: return run_gemm<64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    case 128: return run_gemm<128>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    default: return run_gemm<256>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+  }
+}
+
+// The GEMM's column tile width and schedule, chosen on the device the first time a
+// (n, Kp) is seen: every candidate is run once to warm up and then timed twice with
+// CUDA events on the context's stream; the fastest is cached with the timings.
+static int gemm_tune(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16* Al, int n, int Kp, float* C,
+                     int ldc, int* err, TccTune** out) {
+  const auto key = std::make_pair(n, Kp);
+  auto it = ctx->tcc_tune.find(key);
+  if (it != ctx->tcc_tune.end()) {
+    *out = &it->second;
+    return LITHO_OK;
+  }
+  TccTune tu;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LITHO_CUDA_TRY(ctx, cudaEventCreate(&a));
+  LITHO_CUDA_TRY(ctx, cudaEventCreate(&b));
+  int rc = LITHO_OK;
+  float best = 0.f;
+  for (int bn : {64, 128, 256}) {
+    for (int split = 0; split < 2 && rc == LITHO_OK; ++split) {
+      rc = run_gemm_shape(ctx, bn, split != 0, Ah, Al, n, Kp, C, ldc, err);
+      if (rc == LITHO_OK && cudaEventRecord(a, ctx->stream) != cudaSuccess) rc = LITHO_ERR_CUDA;
+      for (int r = 0; r < 2 && rc == LITHO_OK; ++r) rc = run_gemm_shape(ctx, bn, split != 0, Ah, Al, n, Kp, C, ldc, err);
+      float ms = 0.f;
+      if (rc == LITHO_OK && (cudaEventRecord(b, ctx->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                             cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
+        rc = LITHO_ERR_CUDA;
+      if (rc != LITHO_OK) break;
+      ms *= 0.5f;
+      tu.cands.push_back({bn, split, ms});
+      if (tu.cands.size() == 1 || ms < best) {
+        best = ms;
+        tu.bn = bn;
+        tu.split = split;
+      }
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc == LITHO_ERR_CUDA) set_error(ctx, LITHO_ERR_CUDA, "timing the TCC GEMM candidates failed");
+  if (rc != LITHO_OK) return rc;
+  *out = &(ctx->tcc_tune[key] = tu);
+  return LITHO_OK;
+}
+
+// any non-finite entry of n doubles sets *flag (NA > n_medium makes the pupil phase NaN)
+__global__ void nonfinite_kernel(const double* __restrict__ x, size_t n, int* __restrict__ flag) {
+  bool bad = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(x[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+cudaError_t launch_nonfinite(cudaStream_t s, const double* x, size_t n, int* flag, int sms) {
+  nonfinite_kernel<<<2 * sms, 256, 0, s>>>(x, n, flag);
+  return cudaGetLastError();
+}
+
 int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int ns, int ldp, double2* tcc) {
   const int Kp = ((2 * ns + 63) / 64) * 64;
   const size_t op = (size_t)Kp * sizeof(__nv_bfloat16);
   const int ldc = (n + 3) & ~3;  // 16-byte rows for the epilogue's vector stores
-  // only the output tiles the TCC assembly reads (about half), in L2-friendly blocks
-  const std::vector<TileMN> need = tcc_needed_tiles(n);
-  std::vector<int2> tiles(need.size());
-  for (size_t i = 0; i < need.size(); ++i) tiles[i] = make_int2(need[i].m, need[i].n);
-  // A: 2n rows (hi, lo); B is A's first n rows; C: 2n x ldc fp32; the tile list
+  // A: 2n rows (hi, lo); B is A's first n rows; C: 2n x ldc fp32
   const size_t cbytes = (size_t)2 * n * ldc * sizeof(float);
-  LITHO_RET(ctx->mx_c.ensure(ctx, op * 4 * (size_t)n + cbytes + tiles.size() * sizeof(int2) + 4096));
+  LITHO_RET(ctx->mx_c.ensure(ctx, op * 4 * (size_t)n + cbytes + 4096));
   char* base = ctx->mx_c.as<char>();
   auto take = [&](size_t b) {
     char* p = base;
@@ -251,26 +526,55 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   __nv_bfloat16* Ah = reinterpret_cast<__nv_bfloat16*>(take(op * 2 * n));
   __nv_bfloat16* Al = reinterpret_cast<__nv_bfloat16*>(take(op * 2 * n));
   float* C = reinterpret_cast<float*>(take(cbytes));
-  int2* dtiles = reinterpret_cast<int2*>(take(tiles.size() * sizeof(int2)));
-  LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
-                                      ctx->stream));
   split_kernel<<<dim3((Kp / 8 + 127) / 128, n), 128, 0, ctx->stream>>>(P, J, n, ns, ldp, Kp, Ah, Al);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
-  CUtensorMap mAh, mAl, mBh, mBl;
-  LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n));
-  LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n));
-  LITHO_RET(map_bf16(ctx, &mBh, Ah, Kp, n));
-  LITHO_RET(map_bf16(ctx, &mBl, Al, Kp, n));
   int* err = nullptr;
   LITHO_RET(tc_err_flag_public(ctx, &err));
-  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)GB_SMEM));
-  gemm_bf16x3_kernel<<<(unsigned)tiles.size(), 128, GB_SMEM, ctx->stream>>>(mAh, mAl, mBh, mBl, dtiles, 2 * n, n, Kp,
-                                                                             C, ldc, err);
-  LITHO_CUDA_TRY(ctx, cudaGetLastError());
+  if (ctx->tcc_force_bn > 0) {
+    LITHO_RET(run_gemm_shape(ctx, ctx->tcc_force_bn, ctx->tcc_force_split != 0, Ah, Al, n, Kp, C, ldc, err));
+  } else {
+    TccTune* tu = nullptr;
+    LITHO_RET(gemm_tune(ctx, Ah, Al, n, Kp, C, ldc, err, &tu));
+    LITHO_RET(run_gemm_shape(ctx, tu->bn, tu->split != 0, Ah, Al, n, Kp, C, ldc, err));
+  }
   assemble_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(C, n, ldc, tcc);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
 
 }  // namespace litho
+
+using namespace litho;
+
+extern "C" int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int split_tail) {
+  if (ctx == nullptr) return LITHO_ERR_ARG;
+  LITHO_ARG_CHECK(ctx, bn == 0 || bn == 64 || bn == 128 || bn == 256, "bn must be 0, 64, 128 or 256 (got %d)", bn);
+  ctx->tcc_force_bn = bn;
+  ctx->tcc_force_split = split_tail != 0;
+  return LITHO_OK;
+}
+
+extern "C" int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap) {
+  if (ctx == nullptr || buf == nullptr || cap <= 0) return 0;
+  std::string o = "[";
+  bool first = true;
+  char t[160];
+  for (const auto& kv : ctx->tcc_tune) {
+    snprintf(t, sizeof t, "%s{\"n\": %d, \"Kp\": %d, \"bn\": %d, \"split_tail\": %d, \"candidates\": [",
+             first ? "" : ", ", kv.first.first, kv.first.second, kv.second.bn, kv.second.split);
+    o += t;
+    first = false;
+    for (size_t i = 0; i < kv.second.cands.size(); ++i) {
+      const auto& c = kv.second.cands[i];
+      snprintf(t, sizeof t, "%s{\"bn\": %d, \"split_tail\": %d, \"ms\": %.4f}", i ? ", " : "", c.bn, c.split,
+               c.ms);
+      o += t;
+    }
+    o += "]}";
+  }
+  o += "]";
+  const int n = (int)std::min<size_t>(o.size(), (size_t)cap - 1);
+  memcpy(buf, o.data(), n);
+  buf[n] = 0;
+  return n;
+}

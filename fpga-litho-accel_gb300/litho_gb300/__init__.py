@@ -72,6 +72,9 @@ _SIGS = {
     "litho_calc_image": (_i, [_p, _p, _p, _i, _i, _p, _i, _i, _i, _i, _i, _p, _i]),
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
+    "litho_ctx_set_test_stall": (_i, [_p, _i]),
+    "litho_tcc_gemm_shape": (_i, [_p, _i, _i]),
+    "litho_tcc_gemm_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
     "litho_batch_plan_mask": (_p, [_p, _i]),
     "litho_batch_plan_image": (_p, [_p, _i]),
@@ -301,6 +304,11 @@ class Context:
     def enable_timing(self, on: bool = True):
         self._check(_lib.litho_ctx_enable_timing(self.h, 1 if on else 0))
 
+    def set_test_stall(self, chunk: int):
+        """Error-path test hook (litho_ctx_set_test_stall): chunk >= 0 makes the mixed window
+        DFT's TMA producer stop at that chunk, so the call returns LITHO_ERR_TIMEOUT; -1 = off."""
+        self._check(_lib.litho_ctx_set_test_stall(self.h, int(chunk)))
+
     def stage_times(self, reset: bool = True):
         """{stage: (device ms, kernel launches)} since the last reset (synchronises the stream)."""
         ms = (C.c_double * len(STAGES))()
@@ -403,6 +411,18 @@ class Context:
             self._check(_lib.litho_calc_tcc_medium(self.h, _ptr(s), int(s.shape[0]), outer_sigma_, wavelength, NA,
                                                    defocus, n_medium, Lx, Ly, Nx, Ny, _ptr(out), precision, MEM_HOST))
         return out
+
+    def tcc_gemm_shape(self, bn: int = 0, split_tail: bool = False):
+        """Fix the split-BF16 TCC GEMM's column tile width (64, 128, 256) and schedule; bn = 0
+        restores the on-device autotuner (litho_tcc_gemm_shape)."""
+        self._check(_lib.litho_tcc_gemm_shape(self.h, int(bn), 1 if split_tail else 0))
+
+    def tcc_gemm_tuning(self) -> list:
+        """The autotuner's cached choices with every candidate's time (litho_tcc_gemm_describe)."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        _lib.litho_tcc_gemm_describe(self.h, buf, len(buf))
+        return json.loads(buf.value.decode())
 
     # -- calcKernels -----------------------------------------------------------
     def calc_kernels(self, tcc: np.ndarray, nk: int):

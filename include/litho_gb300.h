@@ -106,6 +106,20 @@ int litho_ctx_enable_timing(litho_ctx* ctx, int enable);
  * output may be NULL.  reset != 0 clears the counters afterwards. */
 int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int reset);
 
+/* ---- error-path test hook for the bounded device-side waits ----------------
+ * No counterpart in the reference, whose failure handling is assert and exit
+ * (common/file_io.cpp:137-150, litho.cpp:246-248).  chunk >= 0 makes the TMA
+ * producer of the mixed-precision window DFT (LITHO_PREC_MIXED imaging) stop
+ * issuing loads at that 64-column chunk of every CTA's share of the work, as if
+ * it had been lost.  The consumers' waits then give up after their limit (about
+ * one second), every role of the kernel leaves, the kernel frees its tensor
+ * memory, and the call (or the next litho_ctx_synchronize, for device pointers)
+ * returns LITHO_ERR_TIMEOUT; the images of that call are undefined.  -1, the
+ * default, turns the hook off.  The value is read when a window DFT is launched
+ * (and baked into a batch plan's graph when the plan is created).  For tests of
+ * the error path only. */
+int litho_ctx_set_test_stall(litho_ctx* ctx, int chunk);
+
 /* ---- optics helpers (litho.cpp:414-426, 1297-1302) --------------------- */
 /* getOuterSigma: max lit-pixel radius / ((srcSize-1)/2), clamped to 1 as
  * litho.cpp:1298 does.  Host pointer. */
@@ -294,6 +308,18 @@ int   litho_surrogate_image(litho_fno* f, const litho_kernel_set* ks, const floa
 int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSigma,
                    float wavelength, float NA, float defocus, int Lx, int Ly, int Nx, int Ny,
                    double* tcc, int tccPrecision, int mem);
+
+/* Shape of the split-BF16 TCC GEMM (no reference counterpart: the reference
+ * accumulates the TCC in scalar loops, litho.cpp:477-515).  By default the
+ * column tile width (64, 128 or 256 columns of 128-row tiles) and the schedule
+ * (whole tiles only, or the last tiles split along K over all SMs) are chosen
+ * per (tccSize, padded source count) by timing every candidate on the device
+ * the first time that size is seen, and cached on the context.
+ * litho_tcc_gemm_shape fixes them instead (bn = 0 restores the tuner);
+ * litho_tcc_gemm_describe writes the cached choices and every candidate's
+ * time as JSON and returns the length written. */
+int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int split_tail);
+int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap);
 
 /* Immersion extension (no reference counterpart): the pupil phase is
  * dz k sqrt(n_medium^2 - rho^2 NA^2) instead of litho.cpp:463's sqrt(1 - rho^2 NA^2),

@@ -60,6 +60,31 @@ def test_tcc_3025(setup):
     setup["t64"], setup["tbf"] = t64, tbf
 
 
+@pytest.mark.parametrize("bn", [64, 128, 256])
+@pytest.mark.parametrize("split_tail", [False, True])
+def test_tcc_3025_every_gemm_shape(setup, bn, split_tail):
+    """Every candidate the GEMM autotuner may pick gives the same split-BF16 TCC."""
+    LG, ctx, ref, nx = setup["LG"], setup["ctx"], setup["ref"], setup["nx"]
+    ctx.tcc_gemm_shape(bn, split_tail)
+    try:
+        tbf = ctx.calc_tcc(setup["src"], setup["sig"], LAM, NA, 0.0, L, L, nx, nx, precision=LG.TCC_SPLIT_BF16,
+                           n_medium=NMED)
+    finally:
+        ctx.tcc_gemm_shape(0)
+    assert _rel(tbf, ref) < 5e-5
+    assert np.array_equal(tbf, tbf.conj().T)
+
+
+def test_tcc_3025_tuning_record(setup):
+    tun = [t for t in setup["ctx"].tcc_gemm_tuning() if t["n"] == 3025]
+    assert len(tun) == 1
+    t = tun[0]
+    assert len(t["candidates"]) == 6
+    best = min(t["candidates"], key=lambda c: c["ms"])
+    assert (best["bn"], best["split_tail"]) == (t["bn"], t["split_tail"])
+    print("tcc 3025 GEMM tuning:", t)
+
+
 def test_top48_eigenpairs(setup):
     from scipy.linalg import eigh
     ctx, ref = setup["ctx"], setup["ref"]

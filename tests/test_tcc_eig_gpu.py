@@ -147,6 +147,37 @@ def test_tcc_split_bf16_close_to_fp64(ctx, L, case):
     assert np.array_equal(tcc, tcc.conj().T)
 
 
+@pytest.mark.parametrize("bn", [64, 128, 256])
+@pytest.mark.parametrize("split_tail", [False, True])
+@pytest.mark.parametrize("case", ["annular21_512", "quasar_1024"])
+def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, bn, split_tail):
+    """Every shape the GEMM autotuner may pick (column tile width, whole tiles or a K-split
+    tail) gives the split-BF16 TCC within the same bar, at tcc 81 and 289 (fewer tiles than SMs:
+    the K-split schedule spreads one tile over many CTAs and sums their partial slots)."""
+    from litho_gb300 import synth
+    src, L_ = (synth.annular_source(21, 0.6, 0.9), 512) if case == "annular21_512" else \
+        (synth.quasar_source(2000)[0], 1024)
+    sig = R.get_outer_sigma(src)
+    nx = R.optics_nx(0.8, L_, sig, 193.0)
+    ref = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx)
+    ctx.tcc_gemm_shape(bn, split_tail)
+    try:
+        tcc = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
+        again = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
+    finally:
+        ctx.tcc_gemm_shape(0)
+    err = np.linalg.norm(tcc - ref) / np.linalg.norm(ref)
+    assert err < 5e-5, err
+    assert np.array_equal(tcc, tcc.conj().T)
+    assert np.array_equal(tcc, again)  # fixed summation order: reproducible
+
+
+def test_tcc_gemm_shape_rejects_bad_width(ctx, L):
+    with pytest.raises(L.LithoError) as e:
+        ctx.tcc_gemm_shape(96)
+    assert e.value.status == L.LITHO_ERR_ARG
+
+
 def test_mixed_chain_config2_vs_fp64(ctx, L):
     """Split-BF16 TCC -> FP64 eigensolve -> split-TF32 imaging, vs the all-FP64 oracle: <= 1e-4."""
     from litho_gb300 import synth
