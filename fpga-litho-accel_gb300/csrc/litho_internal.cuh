@@ -87,15 +87,15 @@ __device__ __forceinline__ float2 sum_strided(const float2* __restrict__ p, size
                      ((a[0].y + a[1].y) + (a[2].y + a[3].y)) + ((a[4].y + a[5].y) + (a[6].y + a[7].y)));
 }
 
-// Autotuned shape of the split-BF16 TCC GEMM for one (n, Kp): column tile width,
-// schedule (0 = whole tiles only, 1 = last tiles split along K) and every
+// Autotuned shape of the split-BF16 TCC GEMM for one (n, Kp): column tile width, K
+// slice, schedule (0 = whole tiles only, 1 = last tiles split along K) and every
 // candidate's measured time.
 struct TccTune {
   struct Cand {
-    int bn, split;
+    int bn, bk, split;
     float ms;
   };
-  int bn = 128, split = 0;
+  int bn = 128, bk = 64, split = 0;
   std::vector<Cand> cands;
 };
 
@@ -141,7 +141,7 @@ struct litho_ctx {
   // (n, K slices, BN, split)
   std::map<std::pair<int, int>, litho::TccTune> tcc_tune;
   std::map<std::tuple<int, int, int, int>, std::shared_ptr<void>> gemm_tables;
-  int tcc_force_bn = 0, tcc_force_split = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
+  int tcc_force_bn = 0, tcc_force_bk = 64, tcc_force_split = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
   // error-path test hook (litho_ctx_set_test_stall): >= 0 stops the mixed window
   // DFT's TMA producer at that chunk of every CTA's work; -1 = off
   int test_stall_chunk = -1;

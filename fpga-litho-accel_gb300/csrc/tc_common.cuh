@@ -140,6 +140,18 @@ __device__ __forceinline__ uint64_t desc_sw128(const void* smem_tile) {
   d |= (uint64_t)2 << 61;
   return d;
 }
+// K-major, SWIZZLE_64B (rows of 64 bytes = 32 bf16), 8-row groups 512 B apart (SBO),
+// LBO unused (1); layout type 4 is the 64-byte swizzle
+__device__ __forceinline__ uint64_t desc_sw64(const void* smem_tile) {
+  const uint32_t a = smem_u32(smem_tile);
+  uint64_t d = 0;
+  d |= (uint64_t)((a & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(512u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)4 << 61;
+  return d;
+}
 // advance the start address by `bytes` (a multiple of 16) inside the swizzle atom
 __device__ __forceinline__ uint64_t desc_add(uint64_t d, uint32_t bytes) { return d + (uint64_t)(bytes >> 4); }
 

@@ -87,18 +87,20 @@ __global__ void split_kernel(const float2* __restrict__ P, const float* __restri
 // Every wait is bounded; a role whose wait gives up sets the abort flag and the
 // others' waits then return at once, the producer's issued loads are waited for,
 // TMEM is freed and the error flag is raised.
-template <int BN>
+template <int BN, int BK>
 struct GemmCfg {
-  static constexpr uint32_t A_T = 128 * 128;          // 128 rows x 64 bf16 (SWIZZLE_128B)
-  static constexpr uint32_t B_T = BN * 128;           // BN rows x 64 bf16
+  static_assert(BK == 64 || BK == 32, "K slices of 64 (128-byte swizzle) or 32 (64-byte swizzle) bf16");
+  static constexpr uint32_t A_T = 128 * BK * 2;       // 128 rows x BK bf16
+  static constexpr uint32_t B_T = BN * BK * 2;        // BN rows x BK bf16
   static constexpr uint32_t STAGE = 2 * A_T + 2 * B_T;  // Ah, Al, Bh, Bl
-  static constexpr int NS = (int)((192u * 1024u) / STAGE);  // 4, 3, 2 stages at BN = 64, 128, 256
+  static constexpr int NS0 = (int)((192u * 1024u) / STAGE);
+  static constexpr int NS = NS0 > 8 ? 8 : NS0;         // BK = 64: 4, 3, 2 at BN = 64, 128, 256; BK = 32: 6, 4 at 128, 256
   static constexpr size_t SMEM = 1024 + (size_t)NS * STAGE + 512;
   static constexpr uint32_t TCOLS = 2 * BN;           // two accumulators
 };
 constexpr int GB_THREADS = 192;
 
-template <int BN>
+template <int BN, int BK>
 __global__ void __launch_bounds__(GB_THREADS, 1) gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tAh,
                                                                     const __grid_constant__ CUtensorMap tAl,
                                                                     const __grid_constant__ CUtensorMap tBh,
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(GB_THREADS, 1) gemm_bf16x3_kernel(const __grid
                                                                     float* __restrict__ C, int ldc,
                                                                     float* __restrict__ part,
                                                                     int* __restrict__ err) {
-  using P = GemmCfg<BN>;
+  using P = GemmCfg<BN, BK>;
   constexpr int NS = P::NS;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -163,10 +165,10 @@ __global__ void __launch_bounds__(GB_THREADS, 1) gemm_bf16x3_kernel(const __grid
             break;
           }
           mbar_arrive_expect_tx(&full[s], P::STAGE);
-          tma_load_2d(tile(s, 0), &tAh, &full[s], 64 * k, m0);
-          tma_load_2d(tile(s, 1), &tAl, &full[s], 64 * k, m0);
-          tma_load_2d(tile(s, 2), &tBh, &full[s], 64 * k, n0);
-          tma_load_2d(tile(s, 3), &tBl, &full[s], 64 * k, n0);
+          tma_load_2d(tile(s, 0), &tAh, &full[s], BK * k, m0);
+          tma_load_2d(tile(s, 1), &tAl, &full[s], BK * k, m0);
+          tma_load_2d(tile(s, 2), &tBh, &full[s], BK * k, n0);
+          tma_load_2d(tile(s, 3), &tBl, &full[s], BK * k, n0);
           last_issued[s] = q;
           if (++s == NS) {
             s = 0;
@@ -197,10 +199,11 @@ __global__ void __launch_bounds__(GB_THREADS, 1) gemm_bf16x3_kernel(const __grid
             break;
           }
           tc_fence_after();
-          const uint64_t dah = desc_sw128(tile(s, 0)), dal = desc_sw128(tile(s, 1));
-          const uint64_t dbh = desc_sw128(tile(s, 2)), dbl = desc_sw128(tile(s, 3));
+          auto desc = [](const void* t) { return BK == 64 ? desc_sw128(t) : desc_sw64(t); };
+          const uint64_t dah = desc(tile(s, 0)), dal = desc(tile(s, 1));
+          const uint64_t dbh = desc(tile(s, 2)), dbl = desc(tile(s, 3));
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
+          for (int kk = 0; kk < BK / 16; ++kk) {
             const uint32_t off = kk * 32;  // 16 bf16 per MMA
             mma_bf16(acc, desc_add(dah, off), desc_add(dbh, off), IDESC, (k != g.y || kk != 0) ? 1u : 0u);
             mma_bf16(acc, desc_add(dah, off), desc_add(dbl, off), IDESC, 1u);
@@ -327,7 +330,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn_bf16() {
 }
 
 static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t cols, uint64_t rows,
-                    uint32_t box_rows) {
+                    uint32_t box_rows, int bk) {
   auto fn = encode_fn_bf16();
   if (fn == nullptr) {
     set_error(ctx, LITHO_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
@@ -335,11 +338,11 @@ static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t c
   }
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)bk, box_rows};
   cuuint32_t es[2] = {1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error(ctx, LITHO_ERR_CUDA, "cuTensorMapEncodeTiled (bf16) failed (%d)", (int)r);
     return LITHO_ERR_CUDA;
@@ -419,21 +422,21 @@ static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, bool split, GemmTa
 }
 
 // One persistent GEMM of the given shape and schedule (plus the fix-up of split tiles).
-template <int BN>
+template <int BN, int BK>
 static int run_gemm(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16* Al, int n, int Kp, float* C,
                     int ldc, bool split, int* err) {
-  using P = GemmCfg<BN>;
+  using P = GemmCfg<BN, BK>;
   GemmTables* t = nullptr;
-  LITHO_RET(gemm_tables(ctx, n, Kp / 64, BN, split, &t));
+  LITHO_RET(gemm_tables(ctx, n, Kp / BK, BN, split, &t));
   CUtensorMap mAh, mAl, mBh, mBl;
-  LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n, 128));
-  LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n, 128));
-  LITHO_RET(map_bf16(ctx, &mBh, Ah, Kp, n, BN));  // B = A's first n rows
-  LITHO_RET(map_bf16(ctx, &mBl, Al, Kp, n, BN));
+  LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n, 128, BK));
+  LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n, 128, BK));
+  LITHO_RET(map_bf16(ctx, &mBh, Ah, Kp, n, BN, BK));  // B = A's first n rows
+  LITHO_RET(map_bf16(ctx, &mBl, Al, Kp, n, BN, BK));
   static_assert(P::SMEM <= 227 * 1024, "GEMM stages exceed the shared memory of one CTA");
-  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_bf16x3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_bf16x3_kernel<BN, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)P::SMEM));
-  gemm_bf16x3_kernel<BN><<<t->ctas, GB_THREADS, P::SMEM, ctx->stream>>>(
+  gemm_bf16x3_kernel<BN, BK><<<t->ctas, GB_THREADS, P::SMEM, ctx->stream>>>(
       mAh, mAl, mBh, mBl, t->segs, t->seg_begin, t->tiles, 2 * n, n, C, ldc, t->part.as<float>(), err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   if (t->nfix > 0) {
@@ -444,18 +447,25 @@ static int run_gemm(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16
   return LITHO_OK;
 }
 
-static int run_gemm_shape(litho_ctx* ctx, int bn, bool split, const __nv_bfloat16* Ah, const __nv_bfloat16* Al,
-                          int n, int Kp, float* C, int ldc, int* err) {
+// the GEMM shapes the tuner chooses from: (column tile width, K slice)
+static const int kGemmShapes[][2] = {{64, 64}, {128, 64}, {256, 64}, {128, 32}, {256, 32}};
+
+static int run_gemm_shape(litho_ctx* ctx, int bn, int bk, bool split, const __nv_bfloat16* Ah,
+                          const __nv_bfloat16* Al, int n, int Kp, float* C, int ldc, int* err) {
+  if (bk == 32) {
+    if (bn == 128) return run_gemm<128, 32>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    return run_gemm<256, 32>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+  }
   switch (bn) {
-    case 64: return run_gemm<64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
-    case 128: return run_gemm<128>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
-    default: return run_gemm<256>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    case 64: return run_gemm<64, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    case 128: return run_gemm<128, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    default: return run_gemm<256, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
   }
 }
 
-// The GEMM's column tile width and schedule, chosen on the device the first time a
-// (n, Kp) is seen: every candidate is run once to warm up and then timed twice with
-// CUDA events on the context's stream; the fastest is cached with the timings.
+// The GEMM's column tile width, K slice and schedule, chosen on the device the first
+// time a (n, Kp) is seen: every candidate is run once to warm up and then timed twice
+// with CUDA events on the context's stream; the fastest is cached with the timings.
 static int gemm_tune(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16* Al, int n, int Kp, float* C,
                      int ldc, int* err, TccTune** out) {
   const auto key = std::make_pair(n, Kp);
@@ -470,24 +480,28 @@ static int gemm_tune(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat1
   LITHO_CUDA_TRY(ctx, cudaEventCreate(&b));
   int rc = LITHO_OK;
   float best = 0.f;
-  for (int bn : {64, 128, 256}) {
+  for (const auto& sh : kGemmShapes) {
+    const int bn = sh[0], bk = sh[1];
     for (int split = 0; split < 2 && rc == LITHO_OK; ++split) {
-      rc = run_gemm_shape(ctx, bn, split != 0, Ah, Al, n, Kp, C, ldc, err);
+      rc = run_gemm_shape(ctx, bn, bk, split != 0, Ah, Al, n, Kp, C, ldc, err);
       if (rc == LITHO_OK && cudaEventRecord(a, ctx->stream) != cudaSuccess) rc = LITHO_ERR_CUDA;
-      for (int r = 0; r < 2 && rc == LITHO_OK; ++r) rc = run_gemm_shape(ctx, bn, split != 0, Ah, Al, n, Kp, C, ldc, err);
+      for (int r = 0; r < 2 && rc == LITHO_OK; ++r)
+        rc = run_gemm_shape(ctx, bn, bk, split != 0, Ah, Al, n, Kp, C, ldc, err);
       float ms = 0.f;
       if (rc == LITHO_OK && (cudaEventRecord(b, ctx->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
                              cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
         rc = LITHO_ERR_CUDA;
       if (rc != LITHO_OK) break;
       ms *= 0.5f;
-      tu.cands.push_back({bn, split, ms});
+      tu.cands.push_back({bn, bk, split, ms});
       if (tu.cands.size() == 1 || ms < best) {
         best = ms;
         tu.bn = bn;
+        tu.bk = bk;
         tu.split = split;
       }
     }
+    if (rc != LITHO_OK) break;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -531,11 +545,12 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   int* err = nullptr;
   LITHO_RET(tc_err_flag_public(ctx, &err));
   if (ctx->tcc_force_bn > 0) {
-    LITHO_RET(run_gemm_shape(ctx, ctx->tcc_force_bn, ctx->tcc_force_split != 0, Ah, Al, n, Kp, C, ldc, err));
+    LITHO_RET(run_gemm_shape(ctx, ctx->tcc_force_bn, ctx->tcc_force_bk, ctx->tcc_force_split != 0, Ah, Al, n, Kp,
+                             C, ldc, err));
   } else {
     TccTune* tu = nullptr;
     LITHO_RET(gemm_tune(ctx, Ah, Al, n, Kp, C, ldc, err, &tu));
-    LITHO_RET(run_gemm_shape(ctx, tu->bn, tu->split != 0, Ah, Al, n, Kp, C, ldc, err));
+    LITHO_RET(run_gemm_shape(ctx, tu->bn, tu->bk, tu->split != 0, Ah, Al, n, Kp, C, ldc, err));
   }
   assemble_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(C, n, ldc, tcc);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
@@ -546,10 +561,13 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
 
 using namespace litho;
 
-extern "C" int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int split_tail) {
+extern "C" int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int split_tail) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
-  LITHO_ARG_CHECK(ctx, bn == 0 || bn == 64 || bn == 128 || bn == 256, "bn must be 0, 64, 128 or 256 (got %d)", bn);
+  bool ok = bn == 0;
+  for (const auto& sh : kGemmShapes) ok = ok || (sh[0] == bn && sh[1] == bk);
+  LITHO_ARG_CHECK(ctx, ok, "no GEMM shape with %d-column tiles and %d-wide K slices", bn, bk);
   ctx->tcc_force_bn = bn;
+  ctx->tcc_force_bk = bk;
   ctx->tcc_force_split = split_tail != 0;
   return LITHO_OK;
 }
@@ -560,14 +578,15 @@ extern "C" int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap)
   bool first = true;
   char t[160];
   for (const auto& kv : ctx->tcc_tune) {
-    snprintf(t, sizeof t, "%s{\"n\": %d, \"Kp\": %d, \"bn\": %d, \"split_tail\": %d, \"candidates\": [",
-             first ? "" : ", ", kv.first.first, kv.first.second, kv.second.bn, kv.second.split);
+    snprintf(t, sizeof t,
+             "%s{\"n\": %d, \"Kp\": %d, \"bn\": %d, \"bk\": %d, \"split_tail\": %d, \"candidates\": [",
+             first ? "" : ", ", kv.first.first, kv.first.second, kv.second.bn, kv.second.bk, kv.second.split);
     o += t;
     first = false;
     for (size_t i = 0; i < kv.second.cands.size(); ++i) {
       const auto& c = kv.second.cands[i];
-      snprintf(t, sizeof t, "%s{\"bn\": %d, \"split_tail\": %d, \"ms\": %.4f}", i ? ", " : "", c.bn, c.split,
-               c.ms);
+      snprintf(t, sizeof t, "%s{\"bn\": %d, \"bk\": %d, \"split_tail\": %d, \"ms\": %.4f}", i ? ", " : "",
+               c.bn, c.bk, c.split, c.ms);
       o += t;
     }
     o += "]}";

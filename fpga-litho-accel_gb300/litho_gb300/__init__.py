@@ -73,7 +73,7 @@ _SIGS = {
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
     "litho_ctx_set_test_stall": (_i, [_p, _i]),
-    "litho_tcc_gemm_shape": (_i, [_p, _i, _i]),
+    "litho_tcc_gemm_shape": (_i, [_p, _i, _i, _i]),
     "litho_tcc_gemm_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
     "litho_batch_plan_mask": (_p, [_p, _i]),
@@ -412,10 +412,12 @@ class Context:
                                                    defocus, n_medium, Lx, Ly, Nx, Ny, _ptr(out), precision, MEM_HOST))
         return out
 
-    def tcc_gemm_shape(self, bn: int = 0, split_tail: bool = False):
-        """Fix the split-BF16 TCC GEMM's column tile width (64, 128, 256) and schedule; bn = 0
-        restores the on-device autotuner (litho_tcc_gemm_shape)."""
-        self._check(_lib.litho_tcc_gemm_shape(self.h, int(bn), 1 if split_tail else 0))
+    GEMM_SHAPES = ((64, 64), (128, 64), (256, 64), (128, 32), (256, 32))
+
+    def tcc_gemm_shape(self, bn: int = 0, bk: int = 64, split_tail: bool = False):
+        """Fix the split-BF16 TCC GEMM's column tile width bn and K slice bk (one of GEMM_SHAPES)
+        and its schedule; bn = 0 restores the on-device autotuner (litho_tcc_gemm_shape)."""
+        self._check(_lib.litho_tcc_gemm_shape(self.h, int(bn), int(bk), 1 if split_tail else 0))
 
     def tcc_gemm_tuning(self) -> list:
         """The autotuner's cached choices with every candidate's time (litho_tcc_gemm_describe)."""

@@ -311,14 +311,15 @@ int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSig
 
 /* Shape of the split-BF16 TCC GEMM (no reference counterpart: the reference
  * accumulates the TCC in scalar loops, litho.cpp:477-515).  By default the
- * column tile width (64, 128 or 256 columns of 128-row tiles) and the schedule
- * (whole tiles only, or the last tiles split along K over all SMs) are chosen
- * per (tccSize, padded source count) by timing every candidate on the device
- * the first time that size is seen, and cached on the context.
- * litho_tcc_gemm_shape fixes them instead (bn = 0 restores the tuner);
- * litho_tcc_gemm_describe writes the cached choices and every candidate's
- * time as JSON and returns the length written. */
-int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int split_tail);
+ * shape is chosen per (tccSize, padded source count) by timing every candidate
+ * on the device the first time that size is seen, and cached on the context:
+ * the column tile width bn of the 128-row output tiles and the K slice bk of
+ * one pipeline stage, (bn, bk) in {(64, 64), (128, 64), (256, 64), (128, 32),
+ * (256, 32)}, and the schedule (whole tiles only, or the last tiles split along
+ * K over all SMs).  litho_tcc_gemm_shape fixes them instead (bn = 0 restores
+ * the tuner); litho_tcc_gemm_describe writes the cached choices and every
+ * candidate's time as JSON and returns the length written. */
+int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int split_tail);
 int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap);
 
 /* Immersion extension (no reference counterpart): the pupil phase is

@@ -60,12 +60,15 @@ def test_tcc_3025(setup):
     setup["t64"], setup["tbf"] = t64, tbf
 
 
-@pytest.mark.parametrize("bn", [64, 128, 256])
+SHAPES = [(64, 64), (128, 64), (256, 64), (128, 32), (256, 32)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("split_tail", [False, True])
-def test_tcc_3025_every_gemm_shape(setup, bn, split_tail):
+def test_tcc_3025_every_gemm_shape(setup, shape, split_tail):
     """Every candidate the GEMM autotuner may pick gives the same split-BF16 TCC."""
     LG, ctx, ref, nx = setup["LG"], setup["ctx"], setup["ref"], setup["nx"]
-    ctx.tcc_gemm_shape(bn, split_tail)
+    ctx.tcc_gemm_shape(shape[0], shape[1], split_tail)
     try:
         tbf = ctx.calc_tcc(setup["src"], setup["sig"], LAM, NA, 0.0, L, L, nx, nx, precision=LG.TCC_SPLIT_BF16,
                            n_medium=NMED)
@@ -79,9 +82,9 @@ def test_tcc_3025_tuning_record(setup):
     tun = [t for t in setup["ctx"].tcc_gemm_tuning() if t["n"] == 3025]
     assert len(tun) == 1
     t = tun[0]
-    assert len(t["candidates"]) == 6
+    assert len(t["candidates"]) == 2 * len(SHAPES)
     best = min(t["candidates"], key=lambda c: c["ms"])
-    assert (best["bn"], best["split_tail"]) == (t["bn"], t["split_tail"])
+    assert (best["bn"], best["bk"], best["split_tail"]) == (t["bn"], t["bk"], t["split_tail"])
     print("tcc 3025 GEMM tuning:", t)
 
 

@@ -147,10 +147,10 @@ def test_tcc_split_bf16_close_to_fp64(ctx, L, case):
     assert np.array_equal(tcc, tcc.conj().T)
 
 
-@pytest.mark.parametrize("bn", [64, 128, 256])
+@pytest.mark.parametrize("shape", [(64, 64), (128, 64), (256, 64), (128, 32), (256, 32)])
 @pytest.mark.parametrize("split_tail", [False, True])
 @pytest.mark.parametrize("case", ["annular21_512", "quasar_1024"])
-def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, bn, split_tail):
+def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, shape, split_tail):
     """Every shape the GEMM autotuner may pick (column tile width, whole tiles or a K-split
     tail) gives the split-BF16 TCC within the same bar, at tcc 81 and 289 (fewer tiles than SMs:
     the K-split schedule spreads one tile over many CTAs and sums their partial slots)."""
@@ -160,7 +160,7 @@ def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, bn, split_tail):
     sig = R.get_outer_sigma(src)
     nx = R.optics_nx(0.8, L_, sig, 193.0)
     ref = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx)
-    ctx.tcc_gemm_shape(bn, split_tail)
+    ctx.tcc_gemm_shape(shape[0], shape[1], split_tail)
     try:
         tcc = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
         again = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
@@ -173,9 +173,10 @@ def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, bn, split_tail):
 
 
 def test_tcc_gemm_shape_rejects_bad_width(ctx, L):
-    with pytest.raises(L.LithoError) as e:
-        ctx.tcc_gemm_shape(96)
-    assert e.value.status == L.LITHO_ERR_ARG
+    for bn, bk in ((96, 64), (64, 32), (128, 16)):
+        with pytest.raises(L.LithoError) as e:
+            ctx.tcc_gemm_shape(bn, bk)
+        assert e.value.status == L.LITHO_ERR_ARG
 
 
 def test_mixed_chain_config2_vs_fp64(ctx, L):
