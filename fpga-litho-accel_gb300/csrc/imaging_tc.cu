@@ -161,14 +161,19 @@ constexpr int WP_CONS = 256;     // consumer threads
 constexpr int WP_RSR = 132;      // sR rows (fp32)
 constexpr int WP_RST = 130;      // sRT rows (float2)
 constexpr int WP_MAX_STAGES = 12;
+constexpr int WP_TQ = 8;         // tile ring: tiles the producer may publish ahead of the slowest role
 constexpr size_t WP_SMEM_CAP = 227 * 1024;
 
 // epilogue buffers: sR [NBH][RSR] fp32 + sRT [Ny+1][RST] float2
 static inline size_t win_epi_bytes(int NBH, int Ny) {
   return (size_t)NBH * WP_RSR * 4 + (size_t)(Ny + 1) * WP_RST * 8;
 }
-// mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES)
-static inline size_t win_bar_bytes(int S) { return (size_t)(5 * S + 5) * 8 + 16 + 8 * (size_t)S; }
+// mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES): 5 per stage, 5 more,
+// two per tile-ring slot; the TMEM slot, abort flag, per-stage ints, tile ring and the two
+// groups' current tiles
+static inline size_t win_bar_bytes(int S) {
+  return (size_t)(5 * S + 5 + 2 * WP_TQ) * 8 + 16 + 8 * (size_t)S + 4 * WP_TQ + 8;
+}
 
 template <int NBH>
 __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
@@ -177,7 +182,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
                                                                    int rows, int batch, int ncs, int S,
                                                                    const float2* __restrict__ ytab,
                                                                    float2* __restrict__ win_part, int part_stride,
-                                                                   int* __restrict__ err, int stall_at) {
+                                                                   int* __restrict__ err, int stall_at,
+                                                                   int* __restrict__ ctr) {
   using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -192,10 +198,14 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   uint64_t* accfull = empty + S;
   uint64_t* accempty = accfull + 2;
   uint64_t* done = accempty + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* tqf = done + 1;       // [WP_TQ] tile-ring slot published (producer)
+  uint64_t* tqe = tqf + WP_TQ;    // [WP_TQ] slot read by all three reading roles
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tqe + WP_TQ);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [S]
   int* nzflag = last_issued + S;                          // [S]
+  volatile int* tq = nzflag + S;                          // [WP_TQ] tile index, -1 = no more tiles
+  volatile int* gtile = tq + WP_TQ;                       // [2] consumers' / epilogue's current tile
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nch = (Lx + 32 * P::KB - 1) / (32 * P::KB);  // chunks of 32 KB columns
   const int T = rows * batch * ncs;
@@ -216,6 +226,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       mbar_init(&accempty[b], 128);
     }
     mbar_init(done, 1);
+    for (int j = 0; j < WP_TQ; ++j) {
+      mbar_init(&tqf[j], 1);
+      mbar_init(&tqe[j], 3);  // the consumers' leader, the MMA lane, the epilogue's leader
+    }
     *abort = 0;
     fence_mbar_init();
   }
@@ -223,6 +237,23 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
+
+  // Tiles come through a ring of WP_TQ slots: the producer takes the next tile (from the
+  // global counter ctr[0] when ctr is given, so CTAs that start late take fewer tiles;
+  // else blockIdx.x + k gridDim.x) and publishes it; the MMA lane and one leader thread
+  // of the consumer and epilogue groups read it (a named barrier hands the leader's copy
+  // to its group, so a group never splits at a barrier) and release the slot.
+  auto ring_read = [&](int seq, int& t) {  // false: the wait gave up (abort is set)
+    const int j = seq & (WP_TQ - 1);
+    if (!mbar_wait_ab(&tqf[j], (uint32_t)(seq / WP_TQ) & 1u, abort)) {
+      *abort = 1;
+      t = -1;
+      return false;
+    }
+    t = tq[j];
+    mbar_arrive(&tqe[j]);
+    return true;
+  };
 
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
   auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };  // [Bh; Bl], 2 NBH rows
@@ -241,7 +272,17 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       int q = 0, s = 0;
       uint32_t ph = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < T && ok; t += gridDim.x) {
+      for (int seq = 0; ok; ++seq) {
+        const int j = seq & (WP_TQ - 1);
+        if (seq >= WP_TQ && !mbar_wait_ab(&tqe[j], (uint32_t)(seq / WP_TQ - 1) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        int t = ctr != nullptr ? atomicAdd(ctr, 1) : (int)blockIdx.x + seq * (int)gridDim.x;
+        if (t >= T) t = -1;
+        tq[j] = t;
+        mbar_arrive(&tqf[j]);  // release: the slot's tile index is visible to the readers
+        if (t < 0) break;
         int img, rb, cs, c0, c1;
         decode(t, img, rb, cs, c0, c1);
         for (int c = c0; c < c1; ++c, ++q) {
@@ -278,7 +319,9 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       int tl = 0, s = 0;
       uint32_t ph = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < T && ok; t += gridDim.x, ++tl) {
+      for (int seq = 0; ok; ++seq, ++tl) {
+        int t;
+        if (!ring_read(seq, t) || t < 0) break;
         int img, rb, cs, c0, c1;
         decode(t, img, rb, cs, c0, c1);
         const int buf = tl & 1;
@@ -341,7 +384,16 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
     // a wait that gives up flags the error and the thread carries on through the
     // named barriers with the others (later waits return at once): a thread that
     // left alone would strand the rest at the next barrier
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+    for (int seq = 0;; ++seq) {
+      if (tid == 0) {
+        int t;
+        ring_read(seq, t);
+        gtile[0] = t;
+      }
+      named_bar(1, WP_CONS);
+      const int t = gtile[0];
+      named_bar(1, WP_CONS);  // every consumer holds t before the leader may overwrite it
+      if (t < 0) break;
       int img, rb, cs, c0, c1;
       decode(t, img, rb, cs, c0, c1);
       for (int c = c0; c < c1; ++c) {
@@ -392,7 +444,16 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
     const int KY = 2 * Ny + 1, NU = Nx + 1;
     const float inv_ff = 1.0f / ((float)Fx * (float)Fy);
     int tl = 0;
-    for (int t = blockIdx.x; t < T; t += gridDim.x, ++tl) {
+    for (int seq = 0;; ++seq, ++tl) {
+      if (etid == 0) {
+        int t;
+        ring_read(seq, t);
+        gtile[1] = t;
+      }
+      named_bar(2, 128);
+      const int t = gtile[1];
+      named_bar(2, 128);  // every epilogue thread holds t before the leader may overwrite it
+      if (t < 0) break;
       int img, rb, cs, c0, c1;
       decode(t, img, rb, cs, c0, c1);
       const int buf = tl & 1;
@@ -478,6 +539,16 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       for (int s = 0; s < S; ++s)
         if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / S) & 1u, 200u);
     if (tid == 0) atomicExch(err, 1);
+  }
+  if (ctr != nullptr && tid == 0) {
+    // the last CTA to finish resets the tile counter for the next launch: every CTA's
+    // fetches precede its count (the fence orders them)
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
+      ctr[0] = 0;
+      ctr[1] = 0;
+      __threadfence();
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -830,7 +901,8 @@ static int cached_table(litho_ctx* ctx, std::tuple<int, int, int, int> key, size
 }
 
 template <int NBH>
-static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
+static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err,
+                         int* ctr, int grid_cap) {
   const ImgGeom& g = p.g;
   bool fresh = false;
   float* tw = nullptr;
@@ -865,25 +937,26 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
                                            (int)smem));
   const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
   const int tiles = rows * p.batch * ncs;
-  const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
+  // persistent: one CTA per SM (at most grid_cap SMs when given)
+  const int grid = std::min(tiles, grid_cap > 0 ? std::min(grid_cap, ctx->sm_count) : ctx->sm_count);
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
   win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, rows,
                                                                   p.batch, ncs, S,
                                                                   reinterpret_cast<const float2*>(yt), win_part,
-                                                                  p.part_stride, err, ctx->test_stall_chunk);
+                                                                  p.part_stride, err, ctx->test_stall_chunk, ctr);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
 
-int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* ctr, int grid_cap) {
   int* err = nullptr;
   LITHO_RET(tc_err_flag(ctx, &err));
   switch (nb_for(p.g.Nx)) {
-    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err);
-    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err);
-    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err);
-    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err);
-    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err);
+    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err, ctr, grid_cap);
+    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err, ctr, grid_cap);
+    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err, ctr, grid_cap);
+    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err, ctr, grid_cap);
+    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err, ctr, grid_cap);
     default:
       set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT supports Nx <= 16");
       return LITHO_ERR_UNSUPPORTED;

@@ -88,14 +88,13 @@ __device__ __forceinline__ float2 sum_strided(const float2* __restrict__ p, size
 }
 
 // Autotuned shape of the split-BF16 TCC GEMM for one (n, Kp): column tile width, K
-// slice, schedule (0 = whole tiles only, 1 = last tiles split along K) and every
-// candidate's measured time.
+// slice, schedule (gemm_schedule's sched) and every candidate's measured time.
 struct TccTune {
   struct Cand {
-    int bn, bk, split;
+    int bn, bk, sched;
     float ms;
   };
-  int bn = 128, bk = 64, split = 0;
+  int bn = 128, bk = 64, sched = 0;
   std::vector<Cand> cands;
 };
 
@@ -141,7 +140,7 @@ struct litho_ctx {
   // (n, K slices, BN, split)
   std::map<std::pair<int, int>, litho::TccTune> tcc_tune;
   std::map<std::tuple<int, int, int, int>, std::shared_ptr<void>> gemm_tables;
-  int tcc_force_bn = 0, tcc_force_bk = 64, tcc_force_split = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
+  int tcc_force_bn = 0, tcc_force_bk = 64, tcc_force_sched = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
   // error-path test hook (litho_ctx_set_test_stall): >= 0 stops the mixed window
   // DFT's TMA producer at that chunk of every CTA's work; -1 = off
   int test_stall_chunk = -1;
@@ -226,7 +225,11 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
                    const float2* krn, const float* scales, float* images, int precision);
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
-int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+// ctr: a pair of zeroed ints (the persistent kernel's tile counter; the kernel leaves it
+// zeroed) for dynamic tile fetching, or nullptr for a static tile order; grid_cap > 0
+// limits the persistent grid to that many SMs
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* ctr = nullptr,
+                   int grid_cap = 0);
 int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images);
 size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch);
 bool tc_supported(const ImgGeom& g);

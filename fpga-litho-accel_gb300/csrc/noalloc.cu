@@ -16,6 +16,10 @@
 // stand-in, not a device address, so the address is looked up once per device
 // with cudaGetSymbolAddress while that device is current; the first call on a
 // device does this set-up, so make that first call before any stream capture.
+// The looked-up address stays valid for the life of the device's context: a
+// process that destroys the context between calls (cudaDeviceReset) must not
+// call this entry point again on that device, since the cached address would
+// then name memory of a context that no longer exists.
 // All calls on a device share the array and it keeps the previous call's
 // contents: every region is fully written before it is read in a call, so
 // nothing has to start at zero, but calls whose work overlaps on the GPU

@@ -13,9 +13,10 @@
 //                   n rows (tensor maps over the same memory).
 // gemm_bf16x3_kernel  persistent, one CTA per SM over the 128 x BN output tiles
 //                   the TCC reads (BN = 64, 128 or 256), K streamed in 64-wide
-//                   (128-byte) slices through a TMA/mbarrier ring; whole tiles in
-//                   data-parallel rounds and, optionally, the last tiles split
-//                   along K over all CTAs (gemm_schedule); a double-buffered TMEM
+//                   (128-byte) or 32-wide (64-byte swizzle) slices through a
+//                   TMA/mbarrier ring; whole tiles in data-parallel rounds and,
+//                   optionally, the last one or two rounds' tiles split along K
+//                   over all CTAs (gemm_schedule); a double-buffered TMEM
 //                   accumulator lets the epilogue warps drain one piece while the
 //                   next one's MMAs run.  gemm_fixup_kernel adds the partial sums
 //                   of split tiles in K order.  BN and the schedule are chosen per
@@ -353,7 +354,7 @@ static int map_bf16(litho_ctx* ctx, CUtensorMap* m, const void* base, uint64_t c
 int tc_err_flag_public(litho_ctx* ctx, int** flag);
 
 // Device copy of one GEMM schedule: the tile list, the CTAs' pieces and the fix-up
-// lists, plus the partial-slot workspace, cached per (n, Kp, BN, split).
+// lists, plus the partial-slot workspace, cached per (n, K slices, BN, schedule).
 struct GemmTables {
   ~GemmTables() {
     buf.release();
@@ -367,8 +368,8 @@ struct GemmTables {
   int *fix_tile = nullptr, *fix_begin = nullptr, *fix_slot = nullptr;
 };
 
-static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, bool split, GemmTables** out) {
-  const auto key = std::make_tuple(n, nk, bn, split ? 1 : 0);
+static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, int sched, GemmTables** out) {
+  const auto key = std::make_tuple(n, nk, bn, sched);
   auto it = ctx->gemm_tables.find(key);
   if (it != ctx->gemm_tables.end()) {
     *out = static_cast<GemmTables*>(it->second.get());
@@ -376,8 +377,8 @@ static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, bool split, GemmTa
   }
   const std::vector<TileMN> need = tcc_needed_tiles(n, bn);
   const int T = (int)need.size();
-  const int ctas = split ? ctx->sm_count : std::min(ctx->sm_count, T);
-  const GemmSchedule sc = gemm_schedule(T, nk, ctas, split);
+  const int ctas = sched != GEMM_WHOLE_TILES ? ctx->sm_count : std::min(ctx->sm_count, T);
+  const GemmSchedule sc = gemm_schedule(T, nk, ctas, sched);
   // one host image of all tables, uploaded once
   std::vector<int> h;
   auto put = [&](size_t n_ints) {
@@ -424,10 +425,10 @@ static int gemm_tables(litho_ctx* ctx, int n, int nk, int bn, bool split, GemmTa
 // One persistent GEMM of the given shape and schedule (plus the fix-up of split tiles).
 template <int BN, int BK>
 static int run_gemm(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16* Al, int n, int Kp, float* C,
-                    int ldc, bool split, int* err) {
+                    int ldc, int sched, int* err) {
   using P = GemmCfg<BN, BK>;
   GemmTables* t = nullptr;
-  LITHO_RET(gemm_tables(ctx, n, Kp / BK, BN, split, &t));
+  LITHO_RET(gemm_tables(ctx, n, Kp / BK, BN, sched, &t));
   CUtensorMap mAh, mAl, mBh, mBl;
   LITHO_RET(map_bf16(ctx, &mAh, Ah, Kp, 2 * n, 128, BK));
   LITHO_RET(map_bf16(ctx, &mAl, Al, Kp, 2 * n, 128, BK));
@@ -450,16 +451,16 @@ static int run_gemm(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat16
 // the GEMM shapes the tuner chooses from: (column tile width, K slice)
 static const int kGemmShapes[][2] = {{64, 64}, {128, 64}, {256, 64}, {128, 32}, {256, 32}};
 
-static int run_gemm_shape(litho_ctx* ctx, int bn, int bk, bool split, const __nv_bfloat16* Ah,
+static int run_gemm_shape(litho_ctx* ctx, int bn, int bk, int sched, const __nv_bfloat16* Ah,
                           const __nv_bfloat16* Al, int n, int Kp, float* C, int ldc, int* err) {
   if (bk == 32) {
-    if (bn == 128) return run_gemm<128, 32>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
-    return run_gemm<256, 32>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    if (bn == 128) return run_gemm<128, 32>(ctx, Ah, Al, n, Kp, C, ldc, sched, err);
+    return run_gemm<256, 32>(ctx, Ah, Al, n, Kp, C, ldc, sched, err);
   }
   switch (bn) {
-    case 64: return run_gemm<64, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
-    case 128: return run_gemm<128, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
-    default: return run_gemm<256, 64>(ctx, Ah, Al, n, Kp, C, ldc, split, err);
+    case 64: return run_gemm<64, 64>(ctx, Ah, Al, n, Kp, C, ldc, sched, err);
+    case 128: return run_gemm<128, 64>(ctx, Ah, Al, n, Kp, C, ldc, sched, err);
+    default: return run_gemm<256, 64>(ctx, Ah, Al, n, Kp, C, ldc, sched, err);
   }
 }
 
@@ -482,23 +483,22 @@ static int gemm_tune(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat1
   float best = 0.f;
   for (const auto& sh : kGemmShapes) {
     const int bn = sh[0], bk = sh[1];
-    for (int split = 0; split < 2 && rc == LITHO_OK; ++split) {
-      rc = run_gemm_shape(ctx, bn, bk, split != 0, Ah, Al, n, Kp, C, ldc, err);
+    for (int sched = 0; sched < 3 && rc == LITHO_OK; ++sched) {
+      rc = run_gemm_shape(ctx, bn, bk, sched, Ah, Al, n, Kp, C, ldc, err);
       if (rc == LITHO_OK && cudaEventRecord(a, ctx->stream) != cudaSuccess) rc = LITHO_ERR_CUDA;
-      for (int r = 0; r < 2 && rc == LITHO_OK; ++r)
-        rc = run_gemm_shape(ctx, bn, bk, split != 0, Ah, Al, n, Kp, C, ldc, err);
+      for (int r = 0; r < 2 && rc == LITHO_OK; ++r) rc = run_gemm_shape(ctx, bn, bk, sched, Ah, Al, n, Kp, C, ldc, err);
       float ms = 0.f;
       if (rc == LITHO_OK && (cudaEventRecord(b, ctx->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
                              cudaEventElapsedTime(&ms, a, b) != cudaSuccess))
         rc = LITHO_ERR_CUDA;
       if (rc != LITHO_OK) break;
       ms *= 0.5f;
-      tu.cands.push_back({bn, bk, split, ms});
+      tu.cands.push_back({bn, bk, sched, ms});
       if (tu.cands.size() == 1 || ms < best) {
         best = ms;
         tu.bn = bn;
         tu.bk = bk;
-        tu.split = split;
+        tu.sched = sched;
       }
     }
     if (rc != LITHO_OK) break;
@@ -545,12 +545,12 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
   int* err = nullptr;
   LITHO_RET(tc_err_flag_public(ctx, &err));
   if (ctx->tcc_force_bn > 0) {
-    LITHO_RET(run_gemm_shape(ctx, ctx->tcc_force_bn, ctx->tcc_force_bk, ctx->tcc_force_split != 0, Ah, Al, n, Kp,
-                             C, ldc, err));
+    LITHO_RET(run_gemm_shape(ctx, ctx->tcc_force_bn, ctx->tcc_force_bk, ctx->tcc_force_sched, Ah, Al, n, Kp, C, ldc,
+                             err));
   } else {
     TccTune* tu = nullptr;
     LITHO_RET(gemm_tune(ctx, Ah, Al, n, Kp, C, ldc, err, &tu));
-    LITHO_RET(run_gemm_shape(ctx, tu->bn, tu->bk, tu->split != 0, Ah, Al, n, Kp, C, ldc, err));
+    LITHO_RET(run_gemm_shape(ctx, tu->bn, tu->bk, tu->sched, Ah, Al, n, Kp, C, ldc, err));
   }
   assemble_kernel<<<dim3((n + 127) / 128, n), 128, 0, ctx->stream>>>(C, n, ldc, tcc);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
@@ -561,14 +561,15 @@ int tcc_split_bf16(litho_ctx* ctx, const float2* P, const float* J, int n, int n
 
 using namespace litho;
 
-extern "C" int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int split_tail) {
+extern "C" int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int sched) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   bool ok = bn == 0;
   for (const auto& sh : kGemmShapes) ok = ok || (sh[0] == bn && sh[1] == bk);
   LITHO_ARG_CHECK(ctx, ok, "no GEMM shape with %d-column tiles and %d-wide K slices", bn, bk);
+  LITHO_ARG_CHECK(ctx, sched >= 0 && sched <= 2, "schedule %d not in {0, 1, 2}", sched);
   ctx->tcc_force_bn = bn;
   ctx->tcc_force_bk = bk;
-  ctx->tcc_force_split = split_tail != 0;
+  ctx->tcc_force_sched = sched;
   return LITHO_OK;
 }
 
@@ -579,14 +580,14 @@ extern "C" int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap)
   char t[160];
   for (const auto& kv : ctx->tcc_tune) {
     snprintf(t, sizeof t,
-             "%s{\"n\": %d, \"Kp\": %d, \"bn\": %d, \"bk\": %d, \"split_tail\": %d, \"candidates\": [",
-             first ? "" : ", ", kv.first.first, kv.first.second, kv.second.bn, kv.second.bk, kv.second.split);
+             "%s{\"n\": %d, \"Kp\": %d, \"bn\": %d, \"bk\": %d, \"sched\": %d, \"candidates\": [",
+             first ? "" : ", ", kv.first.first, kv.first.second, kv.second.bn, kv.second.bk, kv.second.sched);
     o += t;
     first = false;
     for (size_t i = 0; i < kv.second.cands.size(); ++i) {
       const auto& c = kv.second.cands[i];
-      snprintf(t, sizeof t, "%s{\"bn\": %d, \"bk\": %d, \"split_tail\": %d, \"ms\": %.4f}", i ? ", " : "",
-               c.bn, c.bk, c.split, c.ms);
+      snprintf(t, sizeof t, "%s{\"bn\": %d, \"bk\": %d, \"sched\": %d, \"ms\": %.4f}", i ? ", " : "", c.bn,
+               c.bk, c.sched, c.ms);
       o += t;
     }
     o += "]}";

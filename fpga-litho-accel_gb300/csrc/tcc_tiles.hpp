@@ -50,18 +50,26 @@ struct GemmSchedule {
 };
 
 // ntiles tiles of nk K slices each on `ctas` persistent CTAs (ctas >= 1, nk >= 1).
-// split_tail == false: data-parallel rounds, tile t on CTA t % ctas.
-// split_tail == true: the first ntiles / ctas - 1 rounds (if any) as whole tiles,
-// tile r * ctas + b on CTA b, so the tiles running at one time are neighbours in the
-// list (L2 reuse); the K slices of the remaining tiles (between one and two rounds'
-// worth) are dealt out contiguously and evenly, so every CTA ends within one slice
-// of the others and the last round has no idle SMs.  A tile whose slices are shared
-// by several CTAs is summed from their partial slots by the fix-up.
-inline GemmSchedule gemm_schedule(int ntiles, int nk, int ctas, bool split_tail) {
+// sched 0 (GEMM_WHOLE_TILES): data-parallel rounds, tile t on CTA t % ctas.
+// sched 1 (GEMM_SPLIT_LAST_ROUNDS): the first ntiles / ctas - 1 rounds (if any) as whole
+//   tiles, tile r * ctas + b on CTA b, so the tiles running at one time are neighbours in
+//   the list (L2 reuse); the K slices of the remaining tiles (between one and two rounds'
+//   worth) are dealt out contiguously and evenly (stream-K).
+// sched 2 (GEMM_SPLIT_LAST_ROUND): every full round as whole tiles and only the last,
+//   partial round's tiles dealt out along K: the split tiles are few, so the CTAs sharing
+//   them read the same operand panels at the same time.
+// With sched 1 or 2 every CTA ends within one K slice of the others and the last round
+// has no idle SMs.  A tile whose slices are shared by several CTAs is summed from their
+// partial slots by the fix-up.
+enum { GEMM_WHOLE_TILES = 0, GEMM_SPLIT_LAST_ROUNDS = 1, GEMM_SPLIT_LAST_ROUND = 2 };
+
+inline GemmSchedule gemm_schedule(int ntiles, int nk, int ctas, int sched) {
   GemmSchedule s;
   s.begin.assign(1, 0);
   std::vector<std::vector<int>> parts(ntiles);  // partial slots per tile, in K order
-  const int dp_rounds = split_tail ? std::max(0, ntiles / ctas - 1) : (ntiles + ctas - 1) / ctas;
+  const int dp_rounds = sched == GEMM_SPLIT_LAST_ROUNDS ? std::max(0, ntiles / ctas - 1)
+                        : sched == GEMM_SPLIT_LAST_ROUND ? ntiles / ctas
+                                                         : (ntiles + ctas - 1) / ctas;
   const int dp_tiles = std::min(ntiles, dp_rounds * ctas);
   const long long iters = (long long)(ntiles - dp_tiles) * nk;
   for (int b = 0; b < ctas; ++b) {

@@ -414,10 +414,11 @@ class Context:
 
     GEMM_SHAPES = ((64, 64), (128, 64), (256, 64), (128, 32), (256, 32))
 
-    def tcc_gemm_shape(self, bn: int = 0, bk: int = 64, split_tail: bool = False):
+    def tcc_gemm_shape(self, bn: int = 0, bk: int = 64, sched: int = 0):
         """Fix the split-BF16 TCC GEMM's column tile width bn and K slice bk (one of GEMM_SHAPES)
-        and its schedule; bn = 0 restores the on-device autotuner (litho_tcc_gemm_shape)."""
-        self._check(_lib.litho_tcc_gemm_shape(self.h, int(bn), int(bk), 1 if split_tail else 0))
+        and its schedule (0 whole tiles, 1 last one or two rounds split along K, 2 last partial
+        round split); bn = 0 restores the on-device autotuner (litho_tcc_gemm_shape)."""
+        self._check(_lib.litho_tcc_gemm_shape(self.h, int(bn), int(bk), int(sched)))
 
     def tcc_gemm_tuning(self) -> list:
         """The autotuner's cached choices with every candidate's time (litho_tcc_gemm_describe)."""

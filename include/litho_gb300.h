@@ -237,7 +237,8 @@ int litho_batch_plan_destroy(litho_batch_plan* plan);
  * returns without synchronising.  Limits: 2 <= Lx, Ly <= 4096, Nx, Ny <= 16,
  * 1 <= nk <= 64; anything beyond returns LITHO_ERR_ARG.  The first call on a
  * device looks up the array's device address (make it before any stream
- * capture).  Calls share the array: calls whose work overlaps on the GPU race
+ * capture); the address is kept for the life of the process, so do not reset
+ * the device (cudaDeviceReset) between calls.  Calls share the array: calls whose work overlaps on the GPU race
  * and must be serialised by the caller. */
 int litho_image_noalloc(const float* mask, int Lx, int Ly, const float* krn_r, const float* krn_i,
                         const float* scales, int nk, int Nx, int Ny, float* image, void* stream);
@@ -315,11 +316,13 @@ int litho_calc_tcc(litho_ctx* ctx, const float* src, int srcSize, float outerSig
  * on the device the first time that size is seen, and cached on the context:
  * the column tile width bn of the 128-row output tiles and the K slice bk of
  * one pipeline stage, (bn, bk) in {(64, 64), (128, 64), (256, 64), (128, 32),
- * (256, 32)}, and the schedule (whole tiles only, or the last tiles split along
- * K over all SMs).  litho_tcc_gemm_shape fixes them instead (bn = 0 restores
- * the tuner); litho_tcc_gemm_describe writes the cached choices and every
- * candidate's time as JSON and returns the length written. */
-int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int split_tail);
+ * (256, 32)}, and the schedule of the persistent CTAs: 0 = whole tiles only;
+ * 1 = whole tiles for all but the last one or two rounds, whose tiles are split
+ * along K over all SMs; 2 = whole tiles for every full round, only the last
+ * partial round split along K.  litho_tcc_gemm_shape fixes them instead
+ * (bn = 0 restores the tuner); litho_tcc_gemm_describe writes the cached
+ * choices and every candidate's time as JSON and returns the length written. */
+int litho_tcc_gemm_shape(litho_ctx* ctx, int bn, int bk, int sched);
 int litho_tcc_gemm_describe(const litho_ctx* ctx, char* buf, int cap);
 
 /* Immersion extension (no reference counterpart): the pupil phase is

@@ -64,11 +64,11 @@ SHAPES = [(64, 64), (128, 64), (256, 64), (128, 32), (256, 32)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-@pytest.mark.parametrize("split_tail", [False, True])
-def test_tcc_3025_every_gemm_shape(setup, shape, split_tail):
+@pytest.mark.parametrize("sched", [0, 1, 2])
+def test_tcc_3025_every_gemm_shape(setup, shape, sched):
     """Every candidate the GEMM autotuner may pick gives the same split-BF16 TCC."""
     LG, ctx, ref, nx = setup["LG"], setup["ctx"], setup["ref"], setup["nx"]
-    ctx.tcc_gemm_shape(shape[0], shape[1], split_tail)
+    ctx.tcc_gemm_shape(shape[0], shape[1], sched)
     try:
         tbf = ctx.calc_tcc(setup["src"], setup["sig"], LAM, NA, 0.0, L, L, nx, nx, precision=LG.TCC_SPLIT_BF16,
                            n_medium=NMED)
@@ -82,9 +82,9 @@ def test_tcc_3025_tuning_record(setup):
     tun = [t for t in setup["ctx"].tcc_gemm_tuning() if t["n"] == 3025]
     assert len(tun) == 1
     t = tun[0]
-    assert len(t["candidates"]) == 2 * len(SHAPES)
+    assert len(t["candidates"]) == 3 * len(SHAPES)
     best = min(t["candidates"], key=lambda c: c["ms"])
-    assert (best["bn"], best["bk"], best["split_tail"]) == (t["bn"], t["bk"], t["split_tail"])
+    assert (best["bn"], best["bk"], best["sched"]) == (t["bn"], t["bk"], t["sched"])
     print("tcc 3025 GEMM tuning:", t)
 
 

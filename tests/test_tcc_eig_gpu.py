@@ -148,19 +148,19 @@ def test_tcc_split_bf16_close_to_fp64(ctx, L, case):
 
 
 @pytest.mark.parametrize("shape", [(64, 64), (128, 64), (256, 64), (128, 32), (256, 32)])
-@pytest.mark.parametrize("split_tail", [False, True])
+@pytest.mark.parametrize("sched", [0, 1, 2])
 @pytest.mark.parametrize("case", ["annular21_512", "quasar_1024"])
-def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, shape, split_tail):
-    """Every shape the GEMM autotuner may pick (column tile width, whole tiles or a K-split
-    tail) gives the split-BF16 TCC within the same bar, at tcc 81 and 289 (fewer tiles than SMs:
-    the K-split schedule spreads one tile over many CTAs and sums their partial slots)."""
+def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, shape, sched):
+    """Every shape the GEMM autotuner may pick (column tile width, K slice, schedule) gives the
+    split-BF16 TCC within the same bar, at tcc 81 and 289 (fewer tiles than SMs: the K-split
+    schedules spread one tile over many CTAs and sum their partial slots)."""
     from litho_gb300 import synth
     src, L_ = (synth.annular_source(21, 0.6, 0.9), 512) if case == "annular21_512" else \
         (synth.quasar_source(2000)[0], 1024)
     sig = R.get_outer_sigma(src)
     nx = R.optics_nx(0.8, L_, sig, 193.0)
     ref = R.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx)
-    ctx.tcc_gemm_shape(shape[0], shape[1], split_tail)
+    ctx.tcc_gemm_shape(shape[0], shape[1], sched)
     try:
         tcc = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
         again = ctx.calc_tcc(src, sig, 193.0, 0.8, 0.0, L_, L_, nx, nx, precision=L.TCC_SPLIT_BF16)
@@ -173,9 +173,9 @@ def test_tcc_split_bf16_every_gemm_shape(ctx, L, case, shape, split_tail):
 
 
 def test_tcc_gemm_shape_rejects_bad_width(ctx, L):
-    for bn, bk in ((96, 64), (64, 32), (128, 16)):
+    for bn, bk, sched in ((96, 64, 0), (64, 32, 0), (128, 16, 0), (128, 64, 3)):
         with pytest.raises(L.LithoError) as e:
-            ctx.tcc_gemm_shape(bn, bk)
+            ctx.tcc_gemm_shape(bn, bk, sched)
         assert e.value.status == L.LITHO_ERR_ARG
 
 

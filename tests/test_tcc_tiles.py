@@ -7,8 +7,9 @@ part).  The list must hold exactly the tiles that contain such an entry, once ea
 blocks; at n = 3025 (Nx = 27) and bn = 128 that is 623 of 1,152.
 
 The schedule hands every (tile, K slice) to exactly one persistent CTA: whole tiles in
-data-parallel rounds, and with the split tail the remaining tiles' K slices dealt out
-evenly; a tile shared by several CTAs is summed from partial slots listed in K order."""
+data-parallel rounds, and with a split schedule (1: the last one or two rounds, 2: the last
+partial round) the remaining tiles' K slices dealt out evenly; a tile shared by several CTAs
+is summed from partial slots listed in K order."""
 import os
 import shutil
 import subprocess
@@ -40,7 +41,7 @@ SCHED_DRIVER = r"""
 int main() {
   int T, nk, ctas, split;
   while (std::scanf("%d %d %d %d", &T, &nk, &ctas, &split) == 4) {
-    const litho::GemmSchedule s = litho::gemm_schedule(T, nk, ctas, split != 0);
+    const litho::GemmSchedule s = litho::gemm_schedule(T, nk, ctas, split);
     std::printf("%d %zu %zu %zu", s.nslots, s.begin.size(), s.segs.size(), s.fix_tile.size());
     for (int v : s.begin) std::printf(" %d", v);
     for (const litho::GemmSeg& g : s.segs) std::printf(" %d %d %d %d", g.tile, g.k0, g.k1, g.slot);
@@ -128,7 +129,7 @@ SCHED_CASES = [(623, 127, 152), (1241, 127, 152), (317, 127, 152), (10, 62, 152)
 @pytest.fixture(scope="module")
 def schedules(tmp_path_factory):
     exe = _build(tmp_path_factory, "gemm_sched", SCHED_DRIVER)
-    cases = [(T, nk, c, sp) for T, nk, c in SCHED_CASES for sp in (0, 1)]
+    cases = [(T, nk, c, sp) for T, nk, c in SCHED_CASES for sp in (0, 1, 2)]
     out = subprocess.run([str(exe)], input="".join(f"{T} {nk} {c} {sp}\n" for T, nk, c, sp in cases),
                          capture_output=True, text=True, check=True).stdout.splitlines()
     assert len(out) == len(cases)
@@ -197,7 +198,7 @@ def test_schedule_data_parallel_rounds_come_first(schedules):
     for (T, nk, ctas, sp), s in schedules.items():
         if not sp:
             continue
-        rounds = max(0, T // ctas - 1)
+        rounds = max(0, T // ctas - 1) if sp == 1 else T // ctas
         for b in range(ctas):
             segs = s["segs"][s["begin"][b]:s["begin"][b + 1]]
             whole = [g[0] for g in segs[:rounds]]
