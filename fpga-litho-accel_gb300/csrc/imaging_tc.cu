@@ -574,6 +574,7 @@ struct FiTC {
   static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
 constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
+constexpr int FI_TQ = 8;         // tile ring slots
 
 // Persistent FI contraction: one CTA per SM takes a contiguous range of output
 // tiles ordered (row band, image, column tile), so the Cy operand (A, the row
@@ -598,7 +599,8 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
                                                               const __grid_constant__ CUtensorMap tmTl,
                                                               const __grid_constant__ CUtensorMap tmOut, int Lx,
                                                               int batch, int ntile, int ntiles,
-                                                              const float* __restrict__ t0g, int* __restrict__ err) {
+                                                              const float* __restrict__ t0g, int* __restrict__ err,
+                                                              int* __restrict__ ctr) {
   using P = FiTC<KBLK, BN>;
   constexpr int NS = P::NS, NOUT = P::NOUT;
   extern __shared__ unsigned char smraw[];
@@ -615,9 +617,14 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   uint64_t* accFull = emptyB + NS;       // [2]
   uint64_t* accEmpty = accFull + 2;      // [2]
   uint64_t* drain = accEmpty + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
+  uint64_t* tqf = drain + 1;             // [FI_TQ] tile-ring slot published (producer)
+  uint64_t* tqe = tqf + FI_TQ;           // [FI_TQ] slot read by the MMA lane and both epilogue groups
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tqe + FI_TQ);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [NS], then the last A generation
+  volatile int* tq = last_issued + NS + 1;               // [FI_TQ] tile index, -1 = no more tiles
+  volatile int* gtile = tq + FI_TQ;                      // [2] each epilogue group's current tile
+  volatile int* gnext = gtile + 2;                       // [2] ... and its next one, when already published
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int i1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
@@ -645,6 +652,10 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       mbar_init(&accEmpty[b], 256);
     }
     mbar_init(drain, 1);
+    for (int j = 0; j < FI_TQ; ++j) {
+      mbar_init(&tqf[j], 1);
+      mbar_init(&tqe[j], 3);  // the MMA lane and the two epilogue groups' leaders
+    }
     *abort = 0;
     fence_mbar_init();
   }
@@ -652,6 +663,21 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
+  // Tiles come through a ring of FI_TQ slots, as in the window kernel: the producer takes
+  // the next tile (from the global counter ctr[0] when given, so CTAs that start late take
+  // fewer tiles; else the next of its contiguous range [i0, i1)) and publishes it; the MMA
+  // lane and one leader per epilogue group read it and release the slot.
+  auto ring_read = [&](int seq, int& t) {  // false: the wait gave up (abort is set)
+    const int j = seq & (FI_TQ - 1);
+    if (!mbar_wait_ab(&tqf[j], (uint32_t)(seq / FI_TQ) & 1u, abort)) {
+      *abort = 1;
+      t = -1;
+      return false;
+    }
+    t = tq[j];
+    mbar_arrive(&tqe[j]);
+    return true;
+  };
   // the hi and lo tiles of one K block sit back to back, so Ah x [Bh; Bl] is one N = 2 BN MMA
   auto Bh = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb) * P::B_KB; };
   auto Bl = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb + 1) * P::B_KB; };
@@ -659,7 +685,17 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   if (warp == 8) {
     if (lane == 0) {  // TMA producer
       int cur = -1, gen = 0;
-      for (int i = i0; i < i1; ++i) {
+      for (int seq = 0;; ++seq) {
+        const int j = seq & (FI_TQ - 1);
+        if (seq >= FI_TQ && !mbar_wait_ab(&tqe[j], (uint32_t)(seq / FI_TQ - 1) & 1u, abort)) {
+          *abort = 1;
+          break;
+        }
+        int i = ctr != nullptr ? atomicAdd(ctr, 1) : i0 + seq;
+        if (i >= (ctr != nullptr ? ntiles : i1)) i = -1;
+        tq[j] = i;
+        mbar_arrive(&tqf[j]);  // release: the slot's tile index is visible to the readers
+        if (i < 0) break;
         int yb, img, xt;
         decode(i, yb, img, xt);
         if (yb != cur) {  // (re)load the row band's Cy tiles once the MMAs on the previous ones are done
@@ -676,7 +712,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
           ++gen;
           cur = yb;
         }
-        const int q = i - i0, s = q % NS;
+        const int q = seq, s = q % NS;
         if (q >= NS && !mbar_wait_ab(&emptyB[s], (uint32_t)((q - NS) / NS) & 1u, abort)) {
           *abort = 1;
           break;
@@ -695,10 +731,18 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       constexpr uint32_t IDESC1 = idesc_tf32(128, BN);      // Al x Bh
       int cur = -1, gen = 0;
       bool ok = true;
-      for (int i = i0; ok && i < i1; ++i) {
-        const int q = i - i0, s = q % NS, b = q & 1;
+      for (int seq = 0; ok; ++seq) {
+        int i;
+        if (!ring_read(seq, i)) {
+          ok = false;
+          break;
+        }
+        if (i < 0) break;
+        const int q = seq, s = q % NS, b = q & 1;
         const int yb = band_of(i);
         if (yb != cur) {
+          // every MMA on the previous band's A tiles is issued: they may be replaced once those complete
+          if (cur >= 0) mma_commit(emptyA);
           if (!mbar_wait_ab(fullA, (uint32_t)gen & 1u, abort)) {
             ok = false;
             break;
@@ -726,7 +770,6 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
         }
         mma_commit(&emptyB[s]);
         mma_commit(&accFull[b]);
-        if (i + 1 == i1 || band_of(i + 1) != yb) mma_commit(emptyA);  // the A tiles may be replaced
       }
       if (!ok) *abort = 1;
     }
@@ -744,14 +787,35 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       const int X = xt * BN + gtid;
       return (gtid < BN && X < Lx) ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
     };
-    float t0n = i0 < i1 ? t0_of(i0) : 0.f;
-    for (int i = i0; i < i1; ++i) {
-      const int q = i - i0, b = q & 1;
+    float t0n = 0.f;  // DC row values of tile tn, fetched one tile ahead when the ring holds it
+    int tn = -1;
+    for (int seq = 0;; ++seq) {
+      if (gtid == 0) {
+        int i, nx = -1;
+        ring_read(seq, i);
+        if (i >= 0) {  // peek: is the next tile published already?
+          const int j1 = (seq + 1) & (FI_TQ - 1);
+          if (mbar_poll(&tqf[j1], (uint32_t)((seq + 1) / FI_TQ) & 1u)) nx = tq[j1];
+        }
+        gtile[grp] = i;
+        gnext[grp] = nx;
+      }
+      named_bar(1 + grp, 128);
+      const int i = gtile[grp], nx = gnext[grp];
+      named_bar(1 + grp, 128);  // every thread of the group holds i before the leader may overwrite it
+      if (i < 0) break;
+      const int q = seq, b = q & 1;
       int yb, img, xt;
       decode(i, yb, img, xt);
-      // every reader of the previous tile's DC row has passed its last slab's second barrier
-      if (gtid < BN) t0s[gtid] = t0n;
-      if (i + 1 < i1) t0n = t0_of(i + 1);
+      // every reader of the previous tile's DC row has passed the barriers above
+      const float t0c = tn == i ? t0n : t0_of(i);
+      if (gtid < BN) t0s[gtid] = t0c;
+      if (nx >= 0) {
+        t0n = t0_of(nx);
+        tn = nx;
+      } else {
+        tn = -1;
+      }
       // a wait that gives up flags the error and carries on with the rest of the
       // group (later waits return at once): a thread that left the loop alone
       // would strand the others at the next named barrier
@@ -806,6 +870,15 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
         if (last_issued[s] >= 0) mbar_wait(&fullB[s], (uint32_t)(last_issued[s] / NS) & 1u, 200u);
     }
     if (tid == 0) atomicExch(err, 1);
+  }
+  if (ctr != nullptr && tid == 0) {
+    // the last CTA to finish resets the tile counter for the next launch
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
+      ctr[0] = 0;
+      ctr[1] = 0;
+      __threadfence();
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -965,7 +1038,7 @@ int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2*
 
 template <int KBLK, int BN>
 static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, const float* cyl, const float* tmh,
-                        const float* tml, const float* t0, float* images, int* err) {
+                        const float* tml, const float* t0, float* images, int* err, int* ctr, int grid_cap) {
   const ImgGeom& g = p.g;
   const int KP = 32 * KBLK;
   CUtensorMap mCh, mCl, mTh, mTl, mO;
@@ -981,10 +1054,10 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   // persistent: one CTA per SM over all (row band, image, column tile) tiles
   const int ntile = (g.Lx + BN - 1) / BN, rows = (g.Ly + 127) / 128;
   const int ntiles = rows * p.batch * ntile;
-  const int grid = std::min(ntiles, ctx->sm_count);
+  const int grid = std::min(ntiles, grid_cap > 0 ? std::min(grid_cap, ctx->sm_count) : ctx->sm_count);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);
   fi_tc_kernel<KBLK, BN><<<grid, FI_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, p.batch, ntile,
-                                                                  ntiles, t0, err);
+                                                                  ntiles, t0, err, ctr);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
@@ -994,9 +1067,31 @@ size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch) {
   return (size_t)2 * batch * g.Lx * 32 * kblk_for(g.Ny) * sizeof(float) + (size_t)batch * g.Lx * sizeof(float);
 }
 
-// tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
-// nullptr to use the context's grow-only buffer.
-int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images) {
+// Pointers of one run of images inside the FI workspace of a batch of `total` images:
+// hi rows [total][Lx][KP], lo rows likewise, then the DC rows [total][Lx].
+FiTcBufs fi_tc_bufs(float* base, const ImgGeom& g, int total, int first) {
+  const size_t KP = 32 * (size_t)kblk_for(g.Ny), plane = (size_t)total * g.Lx * KP;
+  FiTcBufs b;
+  b.tmh = base + (size_t)first * g.Lx * KP;
+  b.tml = base + plane + (size_t)first * g.Lx * KP;
+  b.t0 = base + 2 * plane + (size_t)first * g.Lx;
+  return b;
+}
+
+// FI step 1 on the tensor-core layout: the band's interpolation rows as K-major hi/lo
+// TF32 splits and the DC row, on the context's stream.
+int run_fi_rows_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, const FiTcBufs& b) {
+  const ImgGeom& g = p.g;
+  const int KP = 32 * kblk_for(g.Ny);
+  const float2* twF = nullptr;
+  LITHO_RET(fi_twiddles(ctx, g, &twF));
+  StageScope sc(ctx, LITHO_STAGE_FI_PREP);
+  LITHO_CUDA_TRY(ctx, launch_fi_rows(ctx->stream, p, band_part, twF, KP, nullptr, b.tmh, b.tml, b.t0));
+  return LITHO_OK;
+}
+
+// FI step 2: the tensor-core contraction writing the images, on the context's stream.
+int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* images, int* ctr, int grid_cap) {
   const ImgGeom& g = p.g;
   const int KBLK = kblk_for(g.Ny);
   const int KP = 32 * KBLK;
@@ -1014,23 +1109,22 @@ int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* 
     cyT_init_kernel<<<dim3((g.Ly + 127) / 128, KP), 128, 0, ctx->stream>>>(cyh, cyl, g.Ly, g.Fy, g.Ny, KP);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  // TmT hi/lo: [batch][Lx][KP], then T0
-  float* tmh = tmT;
-  if (tmh == nullptr) {
-    LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(g, p.batch)));
-    tmh = ctx->mx_b.as<float>();
-  }
-  float* tml = tmh + (size_t)p.batch * g.Lx * KP;
-  float* t0 = tml + (size_t)p.batch * g.Lx * KP;
-  {
-    const float2* twF = nullptr;
-    LITHO_RET(fi_twiddles(ctx, g, &twF));
-    StageScope sc(ctx, LITHO_STAGE_FI_PREP);
-    LITHO_CUDA_TRY(ctx, launch_fi_rows(ctx->stream, p, band_part, twF, KP, nullptr, tmh, tml, t0));
-  }
-  if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
+  if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err, ctr, grid_cap);
   // K = 64: 64-column tiles keep three B stages and two staging tiles per group
-  return launch_fi_tc<2, 64>(ctx, p, cyh, cyl, tmh, tml, t0, images, err);
+  return launch_fi_tc<2, 64>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err, ctr, grid_cap);
+}
+
+// tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
+// nullptr to use the context's grow-only buffer.
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images, int* ctr,
+              int grid_cap) {
+  if (tmT == nullptr) {
+    LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(p.g, p.batch)));
+    tmT = ctx->mx_b.as<float>();
+  }
+  const FiTcBufs b = fi_tc_bufs(tmT, p.g, p.batch, 0);
+  LITHO_RET(run_fi_rows_tc(ctx, p, band_part, b));
+  return run_fi_out_tc(ctx, p, b, images, ctr, grid_cap);
 }
 
 }  // namespace litho
