@@ -5,11 +5,11 @@ Workload (one "step"): a batch of B seeded 1024x1024 float32 Manhattan masks
 (line/space gratings and contact arrays, ~50 % density) imaged with K=24 fixed
 SOCS kernels.  The kernels come from this library's own GPU TCC + FP64
 eigensolver for a quasar source (4 poles at 45/135/225/315 deg, sigma 0.7-0.9,
-~2000 lit points), NA 0.8, lambda 193 nm, defocus 0.  B=256 masks (the size of
-the batched workload) are 1 GiB in and 1 GiB out per step, far larger than the
-129 MB L2, so no flush is needed.  Smaller steps pay a fixed per-step cost (the
-previous step's image writes still dirty in L2, kernel tails and launch gaps)
-over fewer masks: 64 masks per step run at ~0.83 of the 256-mask throughput.
+~2000 lit points), NA 0.8, lambda 193 nm, defocus 0.  B=1024 masks are 4 GiB in
+and 4 GiB out per step, far larger than the 129 MB L2, so no flush is needed.
+Smaller steps pay a fixed per-step cost (the previous step's image writes still
+dirty in L2, kernel ramps, tails and launch gaps) over fewer masks: 256 masks per
+step run at ~0.9 of the 1024-mask throughput, 64 masks at ~0.75.
 
   value : images/s with masks resident in HBM (litho_image_batch on device
           pointers), timed with CUDA events over K steps on the library's stream.
@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--batch", type=int, default=256)
+    p.add_argument("--batch", type=int, default=1024)
     p.add_argument("--cpu-budget-s", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--precision", default="auto", choices=["auto", "fp32", "mixed"])

@@ -16,7 +16,8 @@
 //   window column splits in {1, 2}
 // with CUDA events on the context's stream and keeps the fastest; results are
 // cached on the context by (L, Nx, nk, images, precision).  The plan then
-// captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH).
+// captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH), the size
+// classes as parallel branches.
 #include "litho_internal.cuh"
 
 #include <algorithm>
@@ -63,6 +64,12 @@ struct litho_batch_plan {
   std::vector<litho::ClassRun> classes;
   std::vector<float*> item_mask, item_image;
   litho::DevBuf mask_pool, image_pool;
+  // size classes run as parallel branches: one stream per class after the first, fork
+  // and join events, and per class a pair of tile counters for the persistent
+  // tensor-core kernels (window DFT, FI contraction)
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> branch_ev;
+  litho::DevBuf ctrs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -78,11 +85,15 @@ static int default_conv(int Nx, int Ny) {
   return n < 32 ? 32 : n;
 }
 
-// enqueue one class: windows of its sub-batches, SOCS, interpolation
+// enqueue one class on the context's stream: windows of its sub-batches, SOCS,
+// interpolation.  The tensor-core kernels take their tiles from the class's counters, so
+// a class running beside another one adapts to the SMs it gets.
 static int run_class(litho_batch_plan* bp, int ci) {
   litho_ctx* ctx = bp->ctx;
   ClassRun& c = bp->classes[ci];
   const bool tc = bp->precision == LITHO_PREC_MIXED;
+  int* ctrW = bp->ctrs.as<int>() + 32 * ci;
+  int* ctrF = ctrW + 16;
   const int Nx = c.ks->Nx, Ny = c.ks->Ny, KY = 2 * Ny + 1;
   LITHO_CUDA_TRY(ctx, cudaMemsetAsync(c.win.p, 0, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2),
                                       ctx->stream));
@@ -93,7 +104,7 @@ static int run_class(litho_batch_plan* bp, int ci) {
     pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 63) / 64 / 2 : (s.mLx + 63) / 64));
     pw.part_stride = c.part_stride;
     float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
-    if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));
+    if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp, ctrW));
     else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
   }
   ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
@@ -103,13 +114,40 @@ static int run_class(litho_batch_plan* bp, int ci) {
   w.part = c.win.as<float2>();
   w.nparts = c.part_stride;
   LITHO_RET(run_socs(ctx, p, w, c.ks->krn, c.ks->scales, c.band.as<float2>(), nullptr));
-  if (tc) return run_fi_tc(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
+  if (tc) return run_fi_tc(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images, ctrF);
   return run_fi(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
 }
 
+// Switch the context's launch stream for a scope (the stage timers follow it).
+struct BranchStream {
+  litho_ctx* ctx;
+  cudaStream_t saved;
+  BranchStream(litho_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+  ~BranchStream() { ctx->stream = saved; }
+};
+
+// Every class with masks, the first on the context's stream and the others on their own
+// streams forked from it and joined back into it: the classes' stages overlap (one
+// class's SOCS and interpolation rows run while another's masks stream in).  Under
+// stream capture the fork and join become parallel branches of the graph.
 static int run_all(litho_batch_plan* bp) {
+  litho_ctx* ctx = bp->ctx;
+  std::vector<int> act;
   for (int ci = 0; ci < (int)bp->classes.size(); ++ci)
-    if (bp->classes[ci].count > 0) LITHO_RET(run_class(bp, ci));
+    if (bp->classes[ci].count > 0) act.push_back(ci);
+  if (act.size() <= 1) {
+    for (int ci : act) LITHO_RET(run_class(bp, ci));
+    return LITHO_OK;
+  }
+  cudaEvent_t fork = bp->branch_ev[0];
+  LITHO_CUDA_TRY(ctx, cudaEventRecord(fork, ctx->stream));
+  for (size_t k = 1; k < act.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(bp->branch[k - 1], fork, 0));
+  for (size_t k = 0; k < act.size(); ++k) {
+    BranchStream bs(ctx, k == 0 ? ctx->stream : bp->branch[k - 1]);
+    LITHO_RET(run_class(bp, act[k]));
+    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->branch_ev[k], ctx->stream));
+  }
+  for (size_t k = 1; k < act.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->branch_ev[k], 0));
   return LITHO_OK;
 }
 
@@ -244,6 +282,18 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
   for (auto& c : bp->classes) image_floats += (size_t)c.count * c.L * c.L;
   int rc = bp->mask_pool.ensure(ctx, mask_floats * sizeof(float));
   if (rc == LITHO_OK) rc = bp->image_pool.ensure(ctx, image_floats * sizeof(float));
+  if (rc == LITHO_OK) rc = bp->ctrs.ensure(ctx, (size_t)nsets * 32 * sizeof(int));
+  if (rc == LITHO_OK && cudaMemset(bp->ctrs.p, 0, (size_t)nsets * 32 * sizeof(int)) != cudaSuccess) rc = LITHO_ERR_CUDA;
+  for (int k = 0; rc == LITHO_OK && k < nsets; ++k) {  // nsets - 1 branch streams, nsets events
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LITHO_ERR_CUDA;
+    else bp->branch_ev.push_back(e);
+    if (rc == LITHO_OK && k > 0) {
+      cudaStream_t st = nullptr;
+      if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = LITHO_ERR_CUDA;
+      else bp->branch.push_back(st);
+    }
+  }
   if (rc != LITHO_OK) {
     litho_batch_plan_destroy(bp);
     return rc;
@@ -390,6 +440,12 @@ int litho_batch_plan_destroy(litho_batch_plan* bp) {
     c.band.release();
     c.tmbuf.release();
   }
+  for (cudaStream_t st : bp->branch) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  for (cudaEvent_t e : bp->branch_ev) cudaEventDestroy(e);
+  bp->ctrs.release();
   bp->mask_pool.release();
   bp->image_pool.release();
   delete bp;

@@ -126,7 +126,7 @@ int litho_ctx_destroy(litho_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->win_part, &ctx->band_part, &ctx->tm,     &ctx->stage_in, &ctx->stage_out,
                     &ctx->stage_k,  &ctx->stage_s,   &ctx->stage_x, &ctx->tcc_a,   &ctx->tcc_b,
                     &ctx->tcc_c,    &ctx->tcc_pq,  &ctx->eig_w,     &ctx->eig_v,   &ctx->eig_work, &ctx->eig_info,
-                    &ctx->mx_b,     &ctx->mx_c,      &ctx->mx_d,    &ctx->tile_ctr};
+                    &ctx->mx_b,     &ctx->mx_c,      &ctx->mx_d};
   for (DevBuf* b : bufs) b->release();
   for (auto& kv : ctx->twx_tables) kv.second.release();
   for (auto& p : ctx->pending) {
@@ -134,12 +134,6 @@ int litho_ctx_destroy(litho_ctx* ctx) {
     cudaEventDestroy(p.b);
   }
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
-  for (cudaEvent_t e : ctx->pipe_events) cudaEventDestroy(e);
-  for (cudaStream_t st : {ctx->pipe_hi, ctx->pipe_lo})
-    if (st) {
-      cudaStreamSynchronize(st);
-      cudaStreamDestroy(st);
-    }
   for (cudaStream_t st : {ctx->copy_in, ctx->copy_out})
     if (st) {
       cudaStreamSynchronize(st);
@@ -171,16 +165,6 @@ int litho_ctx_synchronize(litho_ctx* ctx) {
 int litho_ctx_enable_timing(litho_ctx* ctx, int enable) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   ctx->timing = enable != 0;
-  return LITHO_OK;
-}
-
-int litho_ctx_set_pipeline(litho_ctx* ctx, int chunk_masks, int stream_sms) {
-  if (ctx == nullptr) return LITHO_ERR_ARG;
-  LITHO_ARG_CHECK(ctx, chunk_masks >= 0, "chunk_masks must be >= 0 (0 turns the pipeline off)");
-  LITHO_ARG_CHECK(ctx, stream_sms >= 0 && stream_sms <= ctx->sm_count, "stream_sms %d outside [0, %d]", stream_sms,
-                  ctx->sm_count);
-  ctx->pipe_chunk = chunk_masks;
-  ctx->pipe_stream_sms = stream_sms;
   return LITHO_OK;
 }
 

@@ -1324,104 +1324,10 @@ static ImgPlan mixed_plan(const ImgGeom& g, int batch, int sm_count) {
   return p;
 }
 
-// Switch the context's launch stream for a scope (the stage timers follow it).
-struct StreamSwap {
-  litho_ctx* ctx;
-  cudaStream_t saved;
-  StreamSwap(litho_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
-  ~StreamSwap() { ctx->stream = saved; }
-};
-
-static int pipe_setup(litho_ctx* ctx, int nev) {
-  if (ctx->pipe_hi == nullptr) {
-    int least = 0, greatest = 0;
-    LITHO_CUDA_TRY(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    LITHO_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->pipe_hi, cudaStreamNonBlocking, greatest));
-    LITHO_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->pipe_lo, cudaStreamNonBlocking, least));
-  }
-  while ((int)ctx->pipe_events.size() < nev) {
-    cudaEvent_t e = nullptr;
-    LITHO_CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    ctx->pipe_events.push_back(e);
-  }
-  if (ctx->tile_ctr.p == nullptr) {
-    LITHO_RET(ctx->tile_ctr.ensure(ctx, 256));
-    LITHO_CUDA_TRY(ctx, cudaMemset(ctx->tile_ctr.p, 0, 256));  // the kernels leave it zeroed
-  }
-  return LITHO_OK;
-}
-
-// Mixed form over chunks of `cb` masks, overlapping each chunk's SOCS and interpolation
-// rows (latency-bound, L2-resident) with the next chunk's window DFT and the previous
-// chunk's interpolation contraction (HBM-streaming).  The streaming kernels run on the
-// high-priority stream, persistent on at most `cap` SMs and fetching their tiles from a
-// global counter, so CTAs that start late take fewer tiles; SOCS and the rows run on the
-// low-priority stream and take the SMs left free.  Per chunk c:
-//   hi: W_c -> eW[c];  lo: wait eW[c], SOCS_c, rows_c -> eR[c];  hi: wait eR[c], FI_c
-// with FI_c issued after W_{c+1}, so the window DFT of the next chunk streams while the
-// low-priority stream works on this one.
-static int image_pipeline_chunked(litho_ctx* ctx, const ImgGeom& g, int batch, int cb, const float* masks,
-                                  const float2* krn, const float* scales, float* images) {
-  const int nc = (batch + cb - 1) / cb;
-  const int KY = 2 * g.Ny + 1, NU = g.Nx + 1, NB = 4 * g.Nx + 1;
-  const int maxparts = ((g.Ly + 127) / 128) * 4;  // row blocks x at most four column splits
-  LITHO_RET(pipe_setup(ctx, 2 * nc + 3));
-  LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * maxparts * KY * NU * sizeof(float2)));
-  LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * g.nk * KY * NB * sizeof(float2)));
-  LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(g, batch)));
-  const int cap = ctx->pipe_stream_sms > 0 ? ctx->pipe_stream_sms : std::max(1, ctx->sm_count - 16);
-  int* ctrW = ctx->tile_ctr.as<int>();
-  int* ctrF = ctrW + 16;  // separate 64-byte lines
-  cudaEvent_t* ev = ctx->pipe_events.data();
-  cudaEvent_t eFork = ev[2 * nc], eHi = ev[2 * nc + 1], eLo = ev[2 * nc + 2];
-  const size_t img = (size_t)g.Lx * g.Ly;
-  std::vector<ImgPlan> plans(nc);
-  for (int c = 0; c < nc; ++c) plans[c] = mixed_plan(g, std::min(cb, batch - c * cb), ctx->sm_count);
-  auto winp = [&](int c) { return ctx->win_part.as<float2>() + (size_t)c * cb * maxparts * KY * NU; };
-  auto bandp = [&](int c) { return ctx->band_part.as<float2>() + (size_t)c * cb * g.nk * KY * NB; };
-  auto fi_out = [&](int c) -> int {
-    StreamSwap sw(ctx, ctx->pipe_hi);
-    LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->pipe_hi, ev[2 * c + 1], 0));
-    return run_fi_out_tc(ctx, plans[c], fi_tc_bufs(ctx->mx_b.as<float>(), g, batch, c * cb),
-                         images + (size_t)c * cb * img, ctrF, cap);
-  };
-  LITHO_CUDA_TRY(ctx, cudaEventRecord(eFork, ctx->stream));
-  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->pipe_hi, eFork, 0));
-  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->pipe_lo, eFork, 0));
-  for (int c = 0; c < nc; ++c) {
-    {
-      StreamSwap sw(ctx, ctx->pipe_hi);
-      LITHO_RET(run_win_dft_tc(ctx, plans[c], masks + (size_t)c * cb * img, winp(c), ctrW, cap));
-      LITHO_CUDA_TRY(ctx, cudaEventRecord(ev[2 * c], ctx->pipe_hi));
-    }
-    {
-      StreamSwap sw(ctx, ctx->pipe_lo);
-      LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->pipe_lo, ev[2 * c], 0));
-      WindowSrc w;
-      w.part = winp(c);
-      w.nparts = plans[c].nparts();
-      LITHO_RET(run_socs(ctx, plans[c], w, krn, scales, bandp(c), nullptr));
-      LITHO_RET(run_fi_rows_tc(ctx, plans[c], bandp(c), fi_tc_bufs(ctx->mx_b.as<float>(), g, batch, c * cb)));
-      LITHO_CUDA_TRY(ctx, cudaEventRecord(ev[2 * c + 1], ctx->pipe_lo));
-    }
-    if (c >= 1) LITHO_RET(fi_out(c - 1));
-  }
-  LITHO_RET(fi_out(nc - 1));
-  LITHO_CUDA_TRY(ctx, cudaEventRecord(eHi, ctx->pipe_hi));
-  LITHO_CUDA_TRY(ctx, cudaEventRecord(eLo, ctx->pipe_lo));
-  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, eHi, 0));
-  LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, eLo, 0));
-  return LITHO_OK;
-}
-
 int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const float2* krn,
                    const float* scales, float* images, int precision) {
   const int KY = 2 * g.Ny + 1;
   const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  LITHO_CUDA_TRY(ctx, cudaStreamIsCapturing(ctx->stream, &cap));
-  if (tc && ctx->pipe_chunk > 0 && batch >= 2 * ctx->pipe_chunk && cap == cudaStreamCaptureStatusNone)
-    return image_pipeline_chunked(ctx, g, batch, ctx->pipe_chunk, masks, krn, scales, images);
   ImgPlan p = tc ? mixed_plan(g, batch, ctx->sm_count) : make_plan(g, batch, ctx->sm_count);
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));

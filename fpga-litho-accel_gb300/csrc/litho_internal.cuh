@@ -141,14 +141,6 @@ struct litho_ctx {
   std::map<std::pair<int, int>, litho::TccTune> tcc_tune;
   std::map<std::tuple<int, int, int, int>, std::shared_ptr<void>> gemm_tables;
   int tcc_force_bn = 0, tcc_force_bk = 64, tcc_force_sched = 0;  // litho_tcc_gemm_shape: bn > 0 bypasses the tuner
-  // mixed-form imaging pipeline over chunks of a batch (image_pipeline): the HBM-streaming
-  // kernels on pipe_hi (high priority), SOCS and the interpolation rows on pipe_lo (low
-  // priority), ordered by events; tile counters of the dynamic persistent kernels
-  cudaStream_t pipe_hi = nullptr, pipe_lo = nullptr;
-  std::vector<cudaEvent_t> pipe_events;
-  litho::DevBuf tile_ctr;
-  int pipe_chunk = 64;       // masks per chunk; 0 turns the pipeline off
-  int pipe_stream_sms = 0;   // SMs the streaming kernels may hold; 0 = all but 16
   // error-path test hook (litho_ctx_set_test_stall): >= 0 stops the mixed window
   // DFT's TMA producer at that chunk of every CTA's work; -1 = off
   int test_stall_chunk = -1;

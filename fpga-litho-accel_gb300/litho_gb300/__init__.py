@@ -73,7 +73,6 @@ _SIGS = {
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
     "litho_ctx_set_test_stall": (_i, [_p, _i]),
-    "litho_ctx_set_pipeline": (_i, [_p, _i, _i]),
     "litho_tcc_gemm_shape": (_i, [_p, _i, _i, _i]),
     "litho_tcc_gemm_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
@@ -304,11 +303,6 @@ class Context:
 
     def enable_timing(self, on: bool = True):
         self._check(_lib.litho_ctx_enable_timing(self.h, 1 if on else 0))
-
-    def set_pipeline(self, chunk_masks: int = 64, stream_sms: int = 0):
-        """Chunked two-stream pipeline of large mixed-precision batches (litho_ctx_set_pipeline):
-        chunk_masks per chunk (0 = off), streaming kernels on at most stream_sms SMs (0 = default)."""
-        self._check(_lib.litho_ctx_set_pipeline(self.h, int(chunk_masks), int(stream_sms)))
 
     def set_test_stall(self, chunk: int):
         """Error-path test hook (litho_ctx_set_test_stall): chunk >= 0 makes the mixed window

@@ -106,18 +106,6 @@ int litho_ctx_enable_timing(litho_ctx* ctx, int enable);
  * output may be NULL.  reset != 0 clears the counters afterwards. */
 int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int reset);
 
-/* ---- pipelined mixed-precision batches (no reference counterpart) -----------
- * A LITHO_PREC_MIXED batch of device-resident masks of at least 2 * chunk_masks
- * masks runs as a pipeline over chunks of chunk_masks masks: the HBM-streaming
- * kernels (window DFT, interpolation contraction) on a high-priority stream,
- * persistent on at most stream_sms SMs, and each chunk's SOCS and interpolation
- * rows on a low-priority stream, where they take the SMs left free while the next
- * chunk streams in.  The call's work still begins and ends on the context's
- * stream.  Defaults: chunk_masks 64, stream_sms 0 (= all SMs but 16);
- * chunk_masks 0 turns the pipeline off.  A call made while the context's stream
- * is being captured into a CUDA graph runs unpipelined. */
-int litho_ctx_set_pipeline(litho_ctx* ctx, int chunk_masks, int stream_sms);
-
 /* ---- error-path test hook for the bounded device-side waits ----------------
  * No counterpart in the reference, whose failure handling is assert and exit
  * (common/file_io.cpp:137-150, litho.cpp:246-248).  chunk >= 0 makes the TMA
