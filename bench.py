@@ -70,6 +70,9 @@ def parse():
     p.add_argument("--profile-tcc", action="store_true",
                    help="the large-TCC workload's GPU stages only (split-BF16 TCC twice, FP64 TCC, top-48 FP64 "
                         "eigensolve), for ncu captures")
+    p.add_argument("--profile-batched", action="store_true",
+                   help="the batched workload only (plan creation with its autotuning, then --steps graph launches "
+                        "per form), for ncu captures")
     p.add_argument("--profile-surrogate", action="store_true",
                    help="the surrogate's kernels only (forward passes, predictions with the error estimate and "
                         "Adam steps on seeded 256^2 masks, --batch masks), for ncu captures")
@@ -288,7 +291,7 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-def batched_leg(ctx, setup, reps=20):
+def batched_leg(ctx, setup, reps=20, forms=("plain", "mixed")):
     """The batched workload: 256 seeded masks with sides drawn from {256, 512, 768, 1024, 2048}
     and 20-60 % density (rectangles with sides L/64..L/8, count set by the drawn density),
     imaged per size class in one CUDA graph (litho_batch_plan_*, autotuned).  Masks up to 1024
@@ -320,6 +323,8 @@ def batched_leg(ctx, setup, reps=20):
     res["config"]["density_mean"] = float(np.mean([float(x.mean()) for x in masks]))
     pix = float(sum(int(m) ** 2 for m in sizes))
     for form, prec in (("plain", LG.PREC_FP32), ("mixed", LG.PREC_MIXED)):
+        if form not in forms:
+            continue
         f = setup[form]
         sets = [ctx.kernel_set(f["krn"], f["s32"], setup["nx"], setup["nx"]), ctx.kernel_set(k2, s2, nx2, nx2)]
         t0 = time.perf_counter()
@@ -519,6 +524,13 @@ def main():
         return profile_tcc(local)
     if args.profile_surrogate:
         return profile_surrogate(local, args.batch, args.steps)
+    if args.profile_batched:
+        import litho_gb300 as LG
+        ctx = LG.Context(local)
+        res = batched_leg(ctx, setup_kernels(ctx), reps=args.steps, forms=("mixed",))
+        ctx.close()
+        print(json.dumps({"profile_batched": True, "ms_per_batch": res["mixed"]["ms_per_batch"]}), flush=True)
+        return
     import numpy as np
     import torch
     import litho_gb300 as L

@@ -17,7 +17,7 @@
 // with CUDA events on the context's stream and keeps the fastest; results are
 // cached on the context by (L, Nx, nk, images, precision).  The plan then
 // captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH), the size
-// classes as parallel branches.
+// classes as staggered parallel branches (run_all).
 #include "litho_internal.cuh"
 
 #include <algorithm>
@@ -88,7 +88,7 @@ static int default_conv(int Nx, int Ny) {
 // enqueue one class on the context's stream: windows of its sub-batches, SOCS,
 // interpolation.  The tensor-core kernels take their tiles from the class's counters, so
 // a class running beside another one adapts to the SMs it gets.
-static int run_class(litho_batch_plan* bp, int ci) {
+static int run_class(litho_batch_plan* bp, int ci, cudaEvent_t after_window = nullptr) {
   litho_ctx* ctx = bp->ctx;
   ClassRun& c = bp->classes[ci];
   const bool tc = bp->precision == LITHO_PREC_MIXED;
@@ -107,6 +107,7 @@ static int run_class(litho_batch_plan* bp, int ci) {
     if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp, ctrW));
     else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
   }
+  if (after_window) LITHO_CUDA_TRY(ctx, cudaEventRecord(after_window, ctx->stream));
   ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
   p.kpg = std::min(c.kpg, c.ks->nk);
   p.ngroups = (c.ks->nk + p.kpg - 1) / p.kpg;
@@ -126,10 +127,14 @@ struct BranchStream {
   ~BranchStream() { ctx->stream = saved; }
 };
 
-// Every class with masks, the first on the context's stream and the others on their own
-// streams forked from it and joined back into it: the classes' stages overlap (one
-// class's SOCS and interpolation rows run while another's masks stream in).  Under
-// stream capture the fork and join become parallel branches of the graph.
+// Every class with masks, staggered over parallel branches: the classes go in order of
+// their tuned time (longest first; it is the one with the heaviest SOCS and interpolation
+// rows), the first on the context's stream and each later one on its own stream, starting
+// when the previous class's window DFTs have been issued ahead of it.  A class's masks then
+// stream in while the previous class runs its latency-bound SOCS and interpolation rows,
+// and its SOCS runs while the previous class writes its images.  The persistent kernels
+// take their tiles from per-class counters, so each adapts to the SMs it gets.  Under
+// stream capture the branches become parallel branches of the graph.
 static int run_all(litho_batch_plan* bp) {
   litho_ctx* ctx = bp->ctx;
   std::vector<int> act;
@@ -139,15 +144,18 @@ static int run_all(litho_batch_plan* bp) {
     for (int ci : act) LITHO_RET(run_class(bp, ci));
     return LITHO_OK;
   }
-  cudaEvent_t fork = bp->branch_ev[0];
-  LITHO_CUDA_TRY(ctx, cudaEventRecord(fork, ctx->stream));
-  for (size_t k = 1; k < act.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(bp->branch[k - 1], fork, 0));
-  for (size_t k = 0; k < act.size(); ++k) {
+  std::stable_sort(act.begin(), act.end(),
+                   [&](int a, int b) { return bp->classes[a].tuned_ms > bp->classes[b].tuned_ms; });
+  const size_t na = act.size();
+  cudaEvent_t* win_done = bp->branch_ev.data();    // [na - 1]
+  cudaEvent_t* done = bp->branch_ev.data() + na;   // [na]
+  for (size_t k = 0; k < na; ++k) {
     BranchStream bs(ctx, k == 0 ? ctx->stream : bp->branch[k - 1]);
-    LITHO_RET(run_class(bp, act[k]));
-    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->branch_ev[k], ctx->stream));
+    if (k > 0) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, win_done[k - 1], 0));
+    LITHO_RET(run_class(bp, act[k], k + 1 < na ? win_done[k] : nullptr));
+    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(done[k], ctx->stream));
   }
-  for (size_t k = 1; k < act.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->branch_ev[k], 0));
+  for (size_t k = 1; k < na; ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, done[k], 0));
   return LITHO_OK;
 }
 
@@ -284,10 +292,12 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
   if (rc == LITHO_OK) rc = bp->image_pool.ensure(ctx, image_floats * sizeof(float));
   if (rc == LITHO_OK) rc = bp->ctrs.ensure(ctx, (size_t)nsets * 32 * sizeof(int));
   if (rc == LITHO_OK && cudaMemset(bp->ctrs.p, 0, (size_t)nsets * 32 * sizeof(int)) != cudaSuccess) rc = LITHO_ERR_CUDA;
-  for (int k = 0; rc == LITHO_OK && k < nsets; ++k) {  // nsets - 1 branch streams, nsets events
-    cudaEvent_t e = nullptr;
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LITHO_ERR_CUDA;
-    else bp->branch_ev.push_back(e);
+  for (int k = 0; rc == LITHO_OK && k < nsets; ++k) {  // nsets - 1 branch streams, 2 nsets events
+    for (int j = 0; j < 2 && rc == LITHO_OK; ++j) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LITHO_ERR_CUDA;
+      else bp->branch_ev.push_back(e);
+    }
     if (rc == LITHO_OK && k > 0) {
       cudaStream_t st = nullptr;
       if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = LITHO_ERR_CUDA;

@@ -30,10 +30,16 @@ struct SrcPt {
   float J;
 };
 
+// One CTA per pupil row id, threads along the source points s: the row P[id][*] is
+// written with consecutive 8-byte stores, the padding columns s >= ns as zeros.
 __global__ void pupil_kernel(const int2* __restrict__ pq, PupilParams pp, float2* __restrict__ P, int ldp) {
-  const int s = blockIdx.y;
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= pp.ns || id >= pp.tccSize) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int id = blockIdx.y;
+  if (s >= ldp || id >= pp.tccSize) return;
+  if (s >= pp.ns) {
+    P[(size_t)id * ldp + s] = make_float2(0.f, 0.f);
+    return;
+  }
   const int2 src = pq[s];
   const int KX = 2 * pp.Nx + 1;
   const int ny = id / KX - pp.Ny, nx = id % KX - pp.Nx;
@@ -201,9 +207,7 @@ int build_pupil(litho_ctx* ctx, const std::vector<SrcPt>& pts, const PupilParams
   LITHO_RET(pqbuf.ensure(ctx, (size_t)ns * sizeof(int2)));
   LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(pqbuf.p, pq.data(), (size_t)ns * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
   LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(J_dev, J.data(), (size_t)ns * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
-  if ((size_t)ldp > (size_t)ns)
-    LITHO_CUDA_TRY(ctx, cudaMemsetAsync(P, 0, (size_t)pp.tccSize * ldp * sizeof(float2), ctx->stream));
-  dim3 grid((pp.tccSize + 127) / 128, ns);
+  dim3 grid((ldp + 127) / 128, pp.tccSize);
   pupil_kernel<<<grid, 128, 0, ctx->stream>>>(pqbuf.as<int2>(), pp, P, ldp);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   // the host vectors must outlive the async copies

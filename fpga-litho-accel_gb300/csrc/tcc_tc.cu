@@ -511,16 +511,32 @@ static int gemm_tune(litho_ctx* ctx, const __nv_bfloat16* Ah, const __nv_bfloat1
   return LITHO_OK;
 }
 
-// any non-finite entry of n doubles sets *flag (NA > n_medium makes the pupil phase NaN)
-__global__ void nonfinite_kernel(const double* __restrict__ x, size_t n, int* __restrict__ flag) {
+// any non-finite entry of n doubles sets *flag (NA > n_medium makes the pupil phase NaN):
+// 16-byte loads, four in flight per thread
+__global__ void nonfinite_kernel(const double2* __restrict__ x, size_t n2, const double* __restrict__ tail,
+                                 int ntail, int* __restrict__ flag) {
   bool bad = false;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    bad |= !isfinite(x[i]);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n2; i += 4 * stride) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = __ldcs(x + i + u * stride);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) bad |= !isfinite(v[u].x) || !isfinite(v[u].y);
+  }
+  for (; i < n2; i += stride) {
+    const double2 v = __ldcs(x + i);
+    bad |= !isfinite(v.x) || !isfinite(v.y);
+  }
+  if (blockIdx.x == 0 && (int)threadIdx.x < ntail) bad |= !isfinite(tail[threadIdx.x]);
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
 }
 
 cudaError_t launch_nonfinite(cudaStream_t s, const double* x, size_t n, int* flag, int sms) {
-  nonfinite_kernel<<<2 * sms, 256, 0, s>>>(x, n, flag);
+  // complex128 data is 16-byte aligned; an odd count leaves one double for the tail
+  nonfinite_kernel<<<8 * sms, 256, 0, s>>>(reinterpret_cast<const double2*>(x), n / 2, x + (n & ~size_t(1)),
+                                           (int)(n & 1), flag);
   return cudaGetLastError();
 }
 
