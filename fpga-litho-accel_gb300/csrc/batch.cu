@@ -16,8 +16,7 @@
 //   window column splits in {1, 2}
 // with CUDA events on the context's stream and keeps the fastest; results are
 // cached on the context by (L, Nx, nk, images, precision).  The plan then
-// captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH), the size
-// classes as staggered parallel branches (run_all).
+// captures the whole sequence in a CUDA graph (LITHO_BATCH_GRAPH).
 #include "litho_internal.cuh"
 
 #include <algorithm>
@@ -64,11 +63,8 @@ struct litho_batch_plan {
   std::vector<litho::ClassRun> classes;
   std::vector<float*> item_mask, item_image;
   litho::DevBuf mask_pool, image_pool;
-  // size classes run as parallel branches: one stream per class after the first, fork
-  // and join events, and per class a pair of tile counters for the persistent
-  // tensor-core kernels (window DFT, FI contraction)
-  std::vector<cudaStream_t> branch;
-  std::vector<cudaEvent_t> branch_ev;
+  // per class a pair of tile counters for the persistent tensor-core kernels (window
+  // DFT, FI contraction): their CTAs take tiles dynamically
   litho::DevBuf ctrs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -86,9 +82,8 @@ static int default_conv(int Nx, int Ny) {
 }
 
 // enqueue one class on the context's stream: windows of its sub-batches, SOCS,
-// interpolation.  The tensor-core kernels take their tiles from the class's counters, so
-// a class running beside another one adapts to the SMs it gets.
-static int run_class(litho_batch_plan* bp, int ci, cudaEvent_t after_window = nullptr) {
+// interpolation.  The tensor-core kernels take their tiles from the class's counters.
+static int run_class(litho_batch_plan* bp, int ci) {
   litho_ctx* ctx = bp->ctx;
   ClassRun& c = bp->classes[ci];
   const bool tc = bp->precision == LITHO_PREC_MIXED;
@@ -107,7 +102,6 @@ static int run_class(litho_batch_plan* bp, int ci, cudaEvent_t after_window = nu
     if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp, ctrW));
     else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
   }
-  if (after_window) LITHO_CUDA_TRY(ctx, cudaEventRecord(after_window, ctx->stream));
   ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
   p.kpg = std::min(c.kpg, c.ks->nk);
   p.ngroups = (c.ks->nk + p.kpg - 1) / p.kpg;
@@ -119,43 +113,15 @@ static int run_class(litho_batch_plan* bp, int ci, cudaEvent_t after_window = nu
   return run_fi(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
 }
 
-// Switch the context's launch stream for a scope (the stage timers follow it).
-struct BranchStream {
-  litho_ctx* ctx;
-  cudaStream_t saved;
-  BranchStream(litho_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
-  ~BranchStream() { ctx->stream = saved; }
-};
-
-// Every class with masks, staggered over parallel branches: the classes go in order of
-// their tuned time (longest first; it is the one with the heaviest SOCS and interpolation
-// rows), the first on the context's stream and each later one on its own stream, starting
-// when the previous class's window DFTs have been issued ahead of it.  A class's masks then
-// stream in while the previous class runs its latency-bound SOCS and interpolation rows,
-// and its SOCS runs while the previous class writes its images.  The persistent kernels
-// take their tiles from per-class counters, so each adapts to the SMs it gets.  Under
-// stream capture the branches become parallel branches of the graph.
+// Every class with masks, one after another on the context's stream.  (Running the
+// classes as parallel graph branches, plain or staggered so that one class's SOCS meets
+// another's streaming kernels, measured slower: the persistent streaming kernels hold
+// ~200 KB of shared memory per SM, so a class's latency-bound SOCS CTAs and another
+// class's streaming CTAs cannot share an SM, and whichever kernel was launched first
+// takes the SMs as they free up.)
 static int run_all(litho_batch_plan* bp) {
-  litho_ctx* ctx = bp->ctx;
-  std::vector<int> act;
   for (int ci = 0; ci < (int)bp->classes.size(); ++ci)
-    if (bp->classes[ci].count > 0) act.push_back(ci);
-  if (act.size() <= 1) {
-    for (int ci : act) LITHO_RET(run_class(bp, ci));
-    return LITHO_OK;
-  }
-  std::stable_sort(act.begin(), act.end(),
-                   [&](int a, int b) { return bp->classes[a].tuned_ms > bp->classes[b].tuned_ms; });
-  const size_t na = act.size();
-  cudaEvent_t* win_done = bp->branch_ev.data();    // [na - 1]
-  cudaEvent_t* done = bp->branch_ev.data() + na;   // [na]
-  for (size_t k = 0; k < na; ++k) {
-    BranchStream bs(ctx, k == 0 ? ctx->stream : bp->branch[k - 1]);
-    if (k > 0) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, win_done[k - 1], 0));
-    LITHO_RET(run_class(bp, act[k], k + 1 < na ? win_done[k] : nullptr));
-    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(done[k], ctx->stream));
-  }
-  for (size_t k = 1; k < na; ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, done[k], 0));
+    if (bp->classes[ci].count > 0) LITHO_RET(run_class(bp, ci));
   return LITHO_OK;
 }
 
@@ -292,18 +258,6 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
   if (rc == LITHO_OK) rc = bp->image_pool.ensure(ctx, image_floats * sizeof(float));
   if (rc == LITHO_OK) rc = bp->ctrs.ensure(ctx, (size_t)nsets * 32 * sizeof(int));
   if (rc == LITHO_OK && cudaMemset(bp->ctrs.p, 0, (size_t)nsets * 32 * sizeof(int)) != cudaSuccess) rc = LITHO_ERR_CUDA;
-  for (int k = 0; rc == LITHO_OK && k < nsets; ++k) {  // nsets - 1 branch streams, 2 nsets events
-    for (int j = 0; j < 2 && rc == LITHO_OK; ++j) {
-      cudaEvent_t e = nullptr;
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LITHO_ERR_CUDA;
-      else bp->branch_ev.push_back(e);
-    }
-    if (rc == LITHO_OK && k > 0) {
-      cudaStream_t st = nullptr;
-      if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = LITHO_ERR_CUDA;
-      else bp->branch.push_back(st);
-    }
-  }
   if (rc != LITHO_OK) {
     litho_batch_plan_destroy(bp);
     return rc;
@@ -450,11 +404,6 @@ int litho_batch_plan_destroy(litho_batch_plan* bp) {
     c.band.release();
     c.tmbuf.release();
   }
-  for (cudaStream_t st : bp->branch) {
-    cudaStreamSynchronize(st);
-    cudaStreamDestroy(st);
-  }
-  for (cudaEvent_t e : bp->branch_ev) cudaEventDestroy(e);
   bp->ctrs.release();
   bp->mask_pool.release();
   bp->image_pool.release();

@@ -570,28 +570,27 @@ struct FiTC {
   static constexpr bool WIDE_OUT = KBLK == 1 && BN == 128;  // two B stages, four staging tiles per group
   static constexpr int NS = WIDE_OUT ? 2 : (ROOMY ? 3 : 2);
   static constexpr int NOUT = WIDE_OUT ? 4 : (ROOMY ? 2 : 1);
-  static constexpr uint32_t OUT_B = 128 * 128;    // 128 rows x 32 fp32 staging
-  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 2 * NOUT * OUT_B + 2 * BN * 4 + 512;
+  static constexpr uint32_t OUT_B = 32 * 128;     // 32 rows x 32 fp32 staging tile of one warp
+  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 8 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
 constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
 constexpr int FI_TQ = 8;         // tile ring slots
 
-// Persistent FI contraction: one CTA per SM takes a contiguous range of output
-// tiles ordered (row band, image, column tile), so the Cy operand (A, the row
-// band's twiddles) is reloaded only when the range crosses a row band.  Tm tiles
-// (B) stream through an NS-stage TMA ring; the two TMEM accumulators alternate
-// between tiles.  Roles (320 threads):
+// Persistent FI contraction: one CTA per SM over output tiles ordered (row band,
+// image, column tile), taken as a contiguous range or from a global counter, so the
+// Cy operand (A, the row band's twiddles) is reloaded only when a CTA's tiles cross a
+// row band.  Tm tiles (B) stream through an NS-stage TMA ring; the two TMEM
+// accumulators alternate between tiles.  Roles (320 threads):
 //   warp 8   : TMA producer  [band change: wait emptyA] A -> fullA;
 //              [wait emptyB[s]] B -> fullB[s]
-//   warp 9   : MMA issuer    [band change: wait fullA]; wait fullB[s], accEmpty[b];
-//              Ah x [Bh; Bl] (N = 2 BN) + Al x Bh; commit emptyB[s], accFull[b];
-//              [last tile of a band: commit emptyA]
-//   warps 0-7: epilogue in two groups of four warps (one warp per TMEM lane
-//              quarter each); group g drains the 32-column slabs g, g + 2, ...:
-//              hi + lo halves + T0[X] -> swizzled staging -> TMA store, then both
-//              groups arrive on accEmpty[b].
-// The epilogue is latency-bound per slab (TMEM load, barriers, staging), so two
-// groups with their own staging tiles and barriers keep twice the slabs in flight.
+//   warp 9   : MMA issuer    [band change: commit emptyA, wait fullA]; wait fullB[s],
+//              accEmpty[b]; Ah x [Bh; Bl] (N = 2 BN) + Al x Bh; commit emptyB[s], accFull[b]
+//   warps 0-7: epilogue, each warp on its own: warp w drains TMEM lane quarter w % 4
+//              for the 32-column slabs w / 4, w / 4 + 2, ...: hi + lo halves + T0[X] ->
+//              its swizzled 32-row staging tile -> its TMA store; each warp arrives on
+//              accEmpty[b] once it has read the tile.
+// The epilogue is latency-bound per slab (TMEM load, staging, store issue); with no
+// barrier between the warps each keeps NOUT stores of its own in flight.
 template <int KBLK, int BN>
 __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_constant__ CUtensorMap tmCh,
                                                               const __grid_constant__ CUtensorMap tmCl,
@@ -608,8 +607,8 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   unsigned char* sAh = sm;
   unsigned char* sAl = sm + KBLK * P::A_KB;
   unsigned char* sB = sm + P::A_BYTES;               // [NS][kb][hi, lo]
-  unsigned char* sOut = sB + NS * P::B_BYTES;        // [2 groups][NOUT][OUT_B]
-  float* sT0 = reinterpret_cast<float*>(sOut + 2 * NOUT * P::OUT_B);  // [2 groups][BN]: the tile's DC row
+  unsigned char* sOut = sB + NS * P::B_BYTES;        // [8 epilogue warps][NOUT][OUT_B]
+  float* sT0 = reinterpret_cast<float*>(sOut + 8 * NOUT * P::OUT_B);  // [2 accumulators][BN]: the tile's DC row
   uint64_t* fullA = reinterpret_cast<uint64_t*>(sT0 + 2 * BN);
   uint64_t* emptyA = fullA + 1;
   uint64_t* fullB = fullA + 2;           // [NS]
@@ -623,8 +622,6 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   int* last_issued = reinterpret_cast<int*>(tslot + 2);  // [NS], then the last A generation
   volatile int* tq = last_issued + NS + 1;               // [FI_TQ] tile index, -1 = no more tiles
-  volatile int* gtile = tq + FI_TQ;                      // [2] each epilogue group's current tile
-  volatile int* gnext = gtile + 2;                       // [2] ... and its next one, when already published
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int i1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
@@ -649,12 +646,12 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
     last_issued[NS] = -1;
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accFull[b], 1);
-      mbar_init(&accEmpty[b], 256);
+      mbar_init(&accEmpty[b], 8);  // one arrival per epilogue warp
     }
     mbar_init(drain, 1);
     for (int j = 0; j < FI_TQ; ++j) {
       mbar_init(&tqf[j], 1);
-      mbar_init(&tqe[j], 3);  // the MMA lane and the two epilogue groups' leaders
+      mbar_init(&tqe[j], 9);  // the MMA lane and the eight epilogue warps
     }
     *abort = 0;
     fence_mbar_init();
@@ -666,7 +663,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   // Tiles come through a ring of FI_TQ slots, as in the window kernel: the producer takes
   // the next tile (from the global counter ctr[0] when given, so CTAs that start late take
   // fewer tiles; else the next of its contiguous range [i0, i1)) and publishes it; the MMA
-  // lane and one leader per epilogue group read it and release the slot.
+  // lane and every epilogue warp (its lane 0) read it and release the slot.
   auto ring_read = [&](int seq, int& t) {  // false: the wait gave up (abort is set)
     const int j = seq & (FI_TQ - 1);
     if (!mbar_wait_ab(&tqf[j], (uint32_t)(seq / FI_TQ) & 1u, abort)) {
@@ -773,90 +770,105 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       }
       if (!ok) *abort = 1;
     }
-  } else {  // warps 0-7: epilogue, group grp = warp / 4
-    const int grp = warp >> 2, gtid = tid & 127, quarter = warp & 3;
-    const int row = 32 * quarter + lane;
-    const bool leader = gtid == 0;
-    float* t0s = sT0 + grp * BN;
-    unsigned char* stg = sOut + (size_t)grp * NOUT * P::OUT_B;
+  } else {  // warps 0-7: epilogue, every warp on its own
+    // Warp w drains TMEM lane quarter w % 4 (32 image rows) for the slabs w / 4,
+    // w / 4 + 2, ... of every tile: 32 rows x 32 columns per slab, hi + lo halves + the DC
+    // row, through its own swizzled staging tiles and its own 32-row TMA stores.  No
+    // barrier joins the warps, so each keeps NOUT stores of its own in flight.
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = 32 * quarter + lane;  // this lane's image row in the tile (its TMEM lane)
+    unsigned char* stg = sOut + (size_t)warp * NOUT * P::OUT_B;
     int slab_count = 0;
-    // the DC row of the next tile is fetched one tile ahead (its latency hides behind a tile)
-    auto t0_of = [&](int i) {  // thread gtid < BN holds column gtid of the tile
+    constexpr int NSL = BN / 64;  // slabs per warp per tile (1 or 2)
+    // the DC row values this lane writes into the shared row of its slabs: column
+    // slab * 32 + lane of tile i
+    auto t0_of = [&](int i, float (&t)[NSL]) {
       int yb, img, xt;
       decode(i, yb, img, xt);
-      const int X = xt * BN + gtid;
-      return (gtid < BN && X < Lx) ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
+#pragma unroll
+      for (int k = 0; k < NSL; ++k) {
+        const int X = xt * BN + (half + 2 * k) * 32 + lane;
+        t[k] = X < Lx ? __ldg(t0g + (size_t)img * Lx + X) : 0.f;
+      }
     };
-    float t0n = 0.f;  // DC row values of tile tn, fetched one tile ahead when the ring holds it
+    float t0n[NSL];  // DC row values of tile tn, fetched one tile ahead when the ring holds it
     int tn = -1;
     for (int seq = 0;; ++seq) {
-      if (gtid == 0) {
-        int i, nx = -1;
+      int i = -1, nx = -1;
+      if (lane == 0) {
         ring_read(seq, i);
         if (i >= 0) {  // peek: is the next tile published already?
           const int j1 = (seq + 1) & (FI_TQ - 1);
           if (mbar_poll(&tqf[j1], (uint32_t)((seq + 1) / FI_TQ) & 1u)) nx = tq[j1];
         }
-        gtile[grp] = i;
-        gnext[grp] = nx;
       }
-      named_bar(1 + grp, 128);
-      const int i = gtile[grp], nx = gnext[grp];
-      named_bar(1 + grp, 128);  // every thread of the group holds i before the leader may overwrite it
+      i = __shfl_sync(0xffffffffu, i, 0);
+      nx = __shfl_sync(0xffffffffu, nx, 0);
       if (i < 0) break;
       const int q = seq, b = q & 1;
       int yb, img, xt;
       decode(i, yb, img, xt);
-      // every reader of the previous tile's DC row has passed the barriers above
-      const float t0c = tn == i ? t0n : t0_of(i);
-      if (gtid < BN) t0s[gtid] = t0c;
+      float t0c[NSL];
+      if (tn == i) {
+#pragma unroll
+        for (int k = 0; k < NSL; ++k) t0c[k] = t0n[k];
+      } else {
+        t0_of(i, t0c);
+      }
+      // the shared DC row of accumulator buffer b: this warp writes and then reads only its
+      // own slabs' columns (warps of the other quarters write the same values), and no warp
+      // is ever more than one tile ahead of another (the MMA lane refills buffer b only after
+      // every warp has released it)
+      float* t0s = sT0 + b * BN;
+#pragma unroll
+      for (int k = 0; k < NSL; ++k) t0s[(half + 2 * k) * 32 + lane] = t0c[k];
+      __syncwarp();
       if (nx >= 0) {
-        t0n = t0_of(nx);
+        t0_of(nx, t0n);
         tn = nx;
       } else {
         tn = -1;
       }
-      // a wait that gives up flags the error and carries on with the rest of the
-      // group (later waits return at once): a thread that left the loop alone
-      // would strand the others at the next named barrier
+      // a wait that gives up flags the error and carries on (later waits return at once)
       if (!mbar_wait_ab(&accFull[b], (uint32_t)(q >> 1) & 1u, abort)) *abort = 1;
       tc_fence_after();
       const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(b * 2 * BN);
 #pragma unroll 1
-      for (int slab = grp; slab < BN / 32; slab += 2, ++slab_count) {
+      for (int slab = half; slab < BN / 32; slab += 2, ++slab_count) {
         uint32_t v[32], w[32];
         tmem_ld32_async(trow + (uint32_t)(slab * 32), v);
         tmem_ld32_async(trow + (uint32_t)(BN + slab * 32), w);
         tmem_ld_wait();
         unsigned char* st = stg + (size_t)(slab_count % NOUT) * P::OUT_B;
-        if (leader) bulk_wait_read<NOUT - 1>();  // the store that used this staging tile has read it
-        named_bar(1 + grp, 128);  // ... and t0s holds this tile's DC row
+        if (lane == 0) bulk_wait_read<NOUT - 1>();  // the store that used this staging tile has read it
+        __syncwarp();
         const float4* t04 = reinterpret_cast<const float4*>(t0s + slab * 32);
         float4 d[8];
 #pragma unroll
         for (int q4 = 0; q4 < 8; ++q4) d[q4] = t04[q4];
-        float4* rowp = reinterpret_cast<float4*>(st + (size_t)row * 128);
+        float4* rowp = reinterpret_cast<float4*>(st + (size_t)lane * 128);
 #pragma unroll
         for (int q4 = 0; q4 < 8; ++q4) {
           const int j = 4 * q4;
-          rowp[q4 ^ (row & 7)] = make_float4(__uint_as_float(v[j]) + (__uint_as_float(w[j]) + d[q4].x),
-                                             __uint_as_float(v[j + 1]) + (__uint_as_float(w[j + 1]) + d[q4].y),
-                                             __uint_as_float(v[j + 2]) + (__uint_as_float(w[j + 2]) + d[q4].z),
-                                             __uint_as_float(v[j + 3]) + (__uint_as_float(w[j + 3]) + d[q4].w));
+          rowp[q4 ^ (lane & 7)] = make_float4(__uint_as_float(v[j]) + (__uint_as_float(w[j]) + d[q4].x),
+                                              __uint_as_float(v[j + 1]) + (__uint_as_float(w[j + 1]) + d[q4].y),
+                                              __uint_as_float(v[j + 2]) + (__uint_as_float(w[j + 2]) + d[q4].z),
+                                              __uint_as_float(v[j + 3]) + (__uint_as_float(w[j + 3]) + d[q4].w));
         }
         fence_proxy_async();
-        named_bar(1 + grp, 128);
-        if (leader) {
+        __syncwarp();
+        if (lane == 0) {
           // evict-first: the images are not read again here, and keeping them from
           // displacing the T tiles and twiddles in L2 measured 52 -> 46.5 us per 64 images
-          tma_store_3d_hint(&tmOut, st, xt * BN + slab * 32, 128 * yb, img, policy_evict_first());
+          tma_store_3d_hint(&tmOut, st, xt * BN + slab * 32, 128 * yb + 32 * quarter, img, policy_evict_first());
           bulk_commit();
         }
       }
       tc_fence_before();
-      mbar_arrive(&accEmpty[b]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accEmpty[b]);
     }
-    if (leader) bulk_wait0();
+    if (lane == 0) bulk_wait0();
   }
   __syncthreads();
   if (*abort) {
@@ -1046,7 +1058,7 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   LITHO_RET(make_map(ctx, &mCl, cyl, 2, KP, g.Ly, 1, 128));
   LITHO_RET(make_map(ctx, &mTh, tmh, 3, KP, g.Lx, p.batch, BN));
   LITHO_RET(make_map(ctx, &mTl, tml, 3, KP, g.Lx, p.batch, BN));
-  LITHO_RET(make_map(ctx, &mO, images, 3, g.Lx, g.Ly, p.batch, 128));
+  LITHO_RET(make_map(ctx, &mO, images, 3, g.Lx, g.Ly, p.batch, 32));  // one warp's 32-row store
   static_assert(FiTC<KBLK, BN>::SMEM <= 227 * 1024, "FI tiles exceed the shared memory of one CTA");
   const size_t smem = FiTC<KBLK, BN>::SMEM;
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_tc_kernel<KBLK, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
