@@ -63,9 +63,6 @@ struct litho_batch_plan {
   std::vector<litho::ClassRun> classes;
   std::vector<float*> item_mask, item_image;
   litho::DevBuf mask_pool, image_pool;
-  // per class a pair of tile counters for the persistent tensor-core kernels (window
-  // DFT, FI contraction): their CTAs take tiles dynamically
-  litho::DevBuf ctrs;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -82,13 +79,11 @@ static int default_conv(int Nx, int Ny) {
 }
 
 // enqueue one class on the context's stream: windows of its sub-batches, SOCS,
-// interpolation.  The tensor-core kernels take their tiles from the class's counters.
+// interpolation
 static int run_class(litho_batch_plan* bp, int ci) {
   litho_ctx* ctx = bp->ctx;
   ClassRun& c = bp->classes[ci];
   const bool tc = bp->precision == LITHO_PREC_MIXED;
-  int* ctrW = bp->ctrs.as<int>() + 32 * ci;
-  int* ctrF = ctrW + 16;
   const int Nx = c.ks->Nx, Ny = c.ks->Ny, KY = 2 * Ny + 1;
   LITHO_CUDA_TRY(ctx, cudaMemsetAsync(c.win.p, 0, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2),
                                       ctx->stream));
@@ -99,7 +94,7 @@ static int run_class(litho_batch_plan* bp, int ci) {
     pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 63) / 64 / 2 : (s.mLx + 63) / 64));
     pw.part_stride = c.part_stride;
     float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
-    if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp, ctrW));
+    if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));
     else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
   }
   ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
@@ -109,16 +104,16 @@ static int run_class(litho_batch_plan* bp, int ci) {
   w.part = c.win.as<float2>();
   w.nparts = c.part_stride;
   LITHO_RET(run_socs(ctx, p, w, c.ks->krn, c.ks->scales, c.band.as<float2>(), nullptr));
-  if (tc) return run_fi_tc(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images, ctrF);
+  if (tc) return run_fi_tc(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
   return run_fi(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
 }
 
 // Every class with masks, one after another on the context's stream.  (Running the
 // classes as parallel graph branches, plain or staggered so that one class's SOCS meets
-// another's streaming kernels, measured slower: the persistent streaming kernels hold
-// ~200 KB of shared memory per SM, so a class's latency-bound SOCS CTAs and another
-// class's streaming CTAs cannot share an SM, and whichever kernel was launched first
-// takes the SMs as they free up.)
+// another's streaming kernels, with the persistent kernels taking tiles from per-class
+// counters, measured slower: the streaming kernels hold ~200 KB of shared memory per
+// SM, so a class's latency-bound SOCS CTAs and another class's streaming CTAs cannot
+// share an SM, and whichever kernel was launched first takes the SMs as they free up.)
 static int run_all(litho_batch_plan* bp) {
   for (int ci = 0; ci < (int)bp->classes.size(); ++ci)
     if (bp->classes[ci].count > 0) LITHO_RET(run_class(bp, ci));
@@ -256,8 +251,6 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
   for (auto& c : bp->classes) image_floats += (size_t)c.count * c.L * c.L;
   int rc = bp->mask_pool.ensure(ctx, mask_floats * sizeof(float));
   if (rc == LITHO_OK) rc = bp->image_pool.ensure(ctx, image_floats * sizeof(float));
-  if (rc == LITHO_OK) rc = bp->ctrs.ensure(ctx, (size_t)nsets * 32 * sizeof(int));
-  if (rc == LITHO_OK && cudaMemset(bp->ctrs.p, 0, (size_t)nsets * 32 * sizeof(int)) != cudaSuccess) rc = LITHO_ERR_CUDA;
   if (rc != LITHO_OK) {
     litho_batch_plan_destroy(bp);
     return rc;
@@ -404,7 +397,6 @@ int litho_batch_plan_destroy(litho_batch_plan* bp) {
     c.band.release();
     c.tmbuf.release();
   }
-  bp->ctrs.release();
   bp->mask_pool.release();
   bp->image_pool.release();
   delete bp;

@@ -182,8 +182,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
                                                                    int rows, int batch, int ncs, int S,
                                                                    const float2* __restrict__ ytab,
                                                                    float2* __restrict__ win_part, int part_stride,
-                                                                   int* __restrict__ err, int stall_at,
-                                                                   int* __restrict__ ctr) {
+                                                                   int* __restrict__ err, int stall_at) {
   using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
@@ -238,11 +237,12 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   tc_fence_after();
   const uint32_t tmem = *tslot;
 
-  // Tiles come through a ring of WP_TQ slots: the producer takes the next tile (from the
-  // global counter ctr[0] when ctr is given, so CTAs that start late take fewer tiles;
-  // else blockIdx.x + k gridDim.x) and publishes it; the MMA lane and one leader thread
-  // of the consumer and epilogue groups read it (a named barrier hands the leader's copy
-  // to its group, so a group never splits at a barrier) and release the slot.
+  // Tiles come through a ring of WP_TQ slots: the producer takes the next tile of its
+  // sequence (blockIdx.x + k gridDim.x) and publishes it; the MMA lane and one leader
+  // thread of the consumer and epilogue groups read it (a named barrier hands the
+  // leader's copy to its group, so a group never splits at a barrier) and release the
+  // slot.  The end of the sequence is published as -1, so every role stops on the same
+  // tile.
   auto ring_read = [&](int seq, int& t) {  // false: the wait gave up (abort is set)
     const int j = seq & (WP_TQ - 1);
     if (!mbar_wait_ab(&tqf[j], (uint32_t)(seq / WP_TQ) & 1u, abort)) {
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           *abort = 1;
           break;
         }
-        int t = ctr != nullptr ? atomicAdd(ctr, 1) : (int)blockIdx.x + seq * (int)gridDim.x;
+        int t = (int)blockIdx.x + seq * (int)gridDim.x;
         if (t >= T) t = -1;
         tq[j] = t;
         mbar_arrive(&tqf[j]);  // release: the slot's tile index is visible to the readers
@@ -540,16 +540,6 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         if (last_issued[s] >= 0) mbar_wait(&full[s], (uint32_t)(last_issued[s] / S) & 1u, 200u);
     if (tid == 0) atomicExch(err, 1);
   }
-  if (ctr != nullptr && tid == 0) {
-    // the last CTA to finish resets the tile counter for the next launch: every CTA's
-    // fetches precede its count (the fence orders them)
-    __threadfence();
-    if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
-      ctr[0] = 0;
-      ctr[1] = 0;
-      __threadfence();
-    }
-  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, 2 * P::NCOL);
@@ -576,10 +566,9 @@ struct FiTC {
 constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
 constexpr int FI_TQ = 8;         // tile ring slots
 
-// Persistent FI contraction: one CTA per SM over output tiles ordered (row band,
-// image, column tile), taken as a contiguous range or from a global counter, so the
-// Cy operand (A, the row band's twiddles) is reloaded only when a CTA's tiles cross a
-// row band.  Tm tiles (B) stream through an NS-stage TMA ring; the two TMEM
+// Persistent FI contraction: one CTA per SM takes a contiguous range of output tiles
+// ordered (row band, image, column tile), so the Cy operand (A, the row band's
+// twiddles) is reloaded only when the range crosses a row band.  Tm tiles (B) stream through an NS-stage TMA ring; the two TMEM
 // accumulators alternate between tiles.  Roles (320 threads):
 //   warp 8   : TMA producer  [band change: wait emptyA] A -> fullA;
 //              [wait emptyB[s]] B -> fullB[s]
@@ -598,8 +587,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
                                                               const __grid_constant__ CUtensorMap tmTl,
                                                               const __grid_constant__ CUtensorMap tmOut, int Lx,
                                                               int batch, int ntile, int ntiles,
-                                                              const float* __restrict__ t0g, int* __restrict__ err,
-                                                              int* __restrict__ ctr) {
+                                                              const float* __restrict__ t0g, int* __restrict__ err) {
   using P = FiTC<KBLK, BN>;
   constexpr int NS = P::NS, NOUT = P::NOUT;
   extern __shared__ unsigned char smraw[];
@@ -661,9 +649,9 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   tc_fence_after();
   const uint32_t tmem = *tslot;
   // Tiles come through a ring of FI_TQ slots, as in the window kernel: the producer takes
-  // the next tile (from the global counter ctr[0] when given, so CTAs that start late take
-  // fewer tiles; else the next of its contiguous range [i0, i1)) and publishes it; the MMA
-  // lane and every epilogue warp (its lane 0) read it and release the slot.
+  // the next tile of its contiguous range [i0, i1) and publishes it (-1 at the end); the
+  // MMA lane and every epilogue warp (its lane 0) read it and release the slot.  The
+  // epilogue peeks at the next slot to fetch that tile's DC row one tile ahead.
   auto ring_read = [&](int seq, int& t) {  // false: the wait gave up (abort is set)
     const int j = seq & (FI_TQ - 1);
     if (!mbar_wait_ab(&tqf[j], (uint32_t)(seq / FI_TQ) & 1u, abort)) {
@@ -688,8 +676,8 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
           *abort = 1;
           break;
         }
-        int i = ctr != nullptr ? atomicAdd(ctr, 1) : i0 + seq;
-        if (i >= (ctr != nullptr ? ntiles : i1)) i = -1;
+        int i = i0 + seq;
+        if (i >= i1) i = -1;
         tq[j] = i;
         mbar_arrive(&tqf[j]);  // release: the slot's tile index is visible to the readers
         if (i < 0) break;
@@ -883,15 +871,6 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
     }
     if (tid == 0) atomicExch(err, 1);
   }
-  if (ctr != nullptr && tid == 0) {
-    // the last CTA to finish resets the tile counter for the next launch
-    __threadfence();
-    if (atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1) {
-      ctr[0] = 0;
-      ctr[1] = 0;
-      __threadfence();
-    }
-  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, 4 * BN);
@@ -986,8 +965,7 @@ static int cached_table(litho_ctx* ctx, std::tuple<int, int, int, int> key, size
 }
 
 template <int NBH>
-static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err,
-                         int* ctr, int grid_cap) {
+static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
   const ImgGeom& g = p.g;
   bool fresh = false;
   float* tw = nullptr;
@@ -1022,26 +1000,25 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
                                            (int)smem));
   const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
   const int tiles = rows * p.batch * ncs;
-  // persistent: one CTA per SM (at most grid_cap SMs when given)
-  const int grid = std::min(tiles, grid_cap > 0 ? std::min(grid_cap, ctx->sm_count) : ctx->sm_count);
+  const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
   win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, rows,
                                                                   p.batch, ncs, S,
                                                                   reinterpret_cast<const float2*>(yt), win_part,
-                                                                  p.part_stride, err, ctx->test_stall_chunk, ctr);
+                                                                  p.part_stride, err, ctx->test_stall_chunk);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
 
-int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* ctr, int grid_cap) {
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
   int* err = nullptr;
   LITHO_RET(tc_err_flag(ctx, &err));
   switch (nb_for(p.g.Nx)) {
-    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err, ctr, grid_cap);
-    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err, ctr, grid_cap);
-    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err, ctr, grid_cap);
-    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err, ctr, grid_cap);
-    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err, ctr, grid_cap);
+    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err);
+    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err);
+    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err);
+    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err);
+    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err);
     default:
       set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT supports Nx <= 16");
       return LITHO_ERR_UNSUPPORTED;
@@ -1050,7 +1027,7 @@ int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2*
 
 template <int KBLK, int BN>
 static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, const float* cyl, const float* tmh,
-                        const float* tml, const float* t0, float* images, int* err, int* ctr, int grid_cap) {
+                        const float* tml, const float* t0, float* images, int* err) {
   const ImgGeom& g = p.g;
   const int KP = 32 * KBLK;
   CUtensorMap mCh, mCl, mTh, mTl, mO;
@@ -1066,10 +1043,10 @@ static int launch_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float* cyh, cons
   // persistent: one CTA per SM over all (row band, image, column tile) tiles
   const int ntile = (g.Lx + BN - 1) / BN, rows = (g.Ly + 127) / 128;
   const int ntiles = rows * p.batch * ntile;
-  const int grid = std::min(ntiles, grid_cap > 0 ? std::min(grid_cap, ctx->sm_count) : ctx->sm_count);
+  const int grid = std::min(ntiles, ctx->sm_count);
   StageScope sc(ctx, LITHO_STAGE_FI_OUT);
   fi_tc_kernel<KBLK, BN><<<grid, FI_THREADS, smem, ctx->stream>>>(mCh, mCl, mTh, mTl, mO, g.Lx, p.batch, ntile,
-                                                                  ntiles, t0, err, ctr);
+                                                                  ntiles, t0, err);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
@@ -1103,7 +1080,7 @@ int run_fi_rows_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, co
 }
 
 // FI step 2: the tensor-core contraction writing the images, on the context's stream.
-int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* images, int* ctr, int grid_cap) {
+int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* images) {
   const ImgGeom& g = p.g;
   const int KBLK = kblk_for(g.Ny);
   const int KP = 32 * KBLK;
@@ -1121,22 +1098,21 @@ int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* im
     cyT_init_kernel<<<dim3((g.Ly + 127) / 128, KP), 128, 0, ctx->stream>>>(cyh, cyl, g.Ly, g.Fy, g.Ny, KP);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err, ctr, grid_cap);
-  // K = 64: 64-column tiles keep three B stages and two staging tiles per group
-  return launch_fi_tc<2, 64>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err, ctr, grid_cap);
+  if (KBLK == 1) return launch_fi_tc<1, 128>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err);
+  // K = 64: 64-column tiles keep three B stages and two staging tiles per warp
+  return launch_fi_tc<2, 64>(ctx, p, cyh, cyl, b.tmh, b.tml, b.t0, images, err);
 }
 
 // tmT: caller-provided workspace of fi_tc_workspace_bytes(g, batch) bytes, or
 // nullptr to use the context's grow-only buffer.
-int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images, int* ctr,
-              int grid_cap) {
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images) {
   if (tmT == nullptr) {
     LITHO_RET(ctx->mx_b.ensure(ctx, fi_tc_workspace_bytes(p.g, p.batch)));
     tmT = ctx->mx_b.as<float>();
   }
   const FiTcBufs b = fi_tc_bufs(tmT, p.g, p.batch, 0);
   LITHO_RET(run_fi_rows_tc(ctx, p, band_part, b));
-  return run_fi_out_tc(ctx, p, b, images, ctr, grid_cap);
+  return run_fi_out_tc(ctx, p, b, images);
 }
 
 }  // namespace litho

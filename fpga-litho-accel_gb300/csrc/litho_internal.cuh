@@ -225,19 +225,14 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
                    const float2* krn, const float* scales, float* images, int precision);
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
-// ctr: a pair of zeroed ints (the persistent kernel's tile counter; the kernel leaves it
-// zeroed) for dynamic tile fetching, or nullptr for a static tile order; grid_cap > 0
-// limits the persistent grid to that many SMs
-int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* ctr = nullptr,
-                   int grid_cap = 0);
-int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images,
-              int* ctr = nullptr, int grid_cap = 0);
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images);
 struct FiTcBufs {
   float *tmh, *tml, *t0;
 };
 FiTcBufs fi_tc_bufs(float* base, const ImgGeom& g, int total, int first);
 int run_fi_rows_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, const FiTcBufs& b);
-int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* images, int* ctr, int grid_cap);
+int run_fi_out_tc(litho_ctx* ctx, const ImgPlan& p, const FiTcBufs& b, float* images);
 size_t fi_tc_workspace_bytes(const ImgGeom& g, int batch);
 bool tc_supported(const ImgGeom& g);
 int tc_check_flag(litho_ctx* ctx);
