@@ -47,8 +47,8 @@ L_SIZE, K_KERNELS, NA, WAVELENGTH, DEFOCUS = 1024, 24, 0.8, 193.0, 0.0
 # ncu capture of one launch of each on 48 masks of this workload (the traffic scales with
 # the masks).  The FI kernel's figure is what DRAM saw during its launch: part of its
 # image writes is still in L2 when it ends and drains during the next launch.
-TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.648128e6 + 3.824128e6) / 48,
-                     ("mixed", "fi_out"): (13.070848e6 + 141.268992e6) / 48}
+TRAFFIC_PER_IMAGE = {("mixed", "win_dft"): (201.65e6 + 3.31e6) / 48,
+                     ("mixed", "fi_out"): (13.07e6 + 140.29e6) / 48}
 TRAFFIC_KERNEL = {"win_dft": "win_dft_tc", "fi_out": "fi_tc"}
 WORKLOAD = ("1024x1024 float32 Manhattan masks (L/S + contacts, ~50% density), K=24 SOCS kernels from a "
             "~2000-point quasar source (sigma 0.7-0.9), NA 0.8, 193 nm; fixed kernels, batch of masks per step")
