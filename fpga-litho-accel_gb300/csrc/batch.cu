@@ -63,6 +63,10 @@ struct litho_batch_plan {
   std::vector<litho::ClassRun> classes;
   std::vector<float*> item_mask, item_image;
   litho::DevBuf mask_pool, image_pool;
+  // the window DFTs of a class's sub-batches run as parallel branches: streams for all
+  // but the largest, a fork event and one join event per branch
+  std::vector<cudaStream_t> wstreams;
+  std::vector<cudaEvent_t> wevents;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -78,6 +82,14 @@ static int default_conv(int Nx, int Ny) {
   return n < 32 ? 32 : n;
 }
 
+// Switch the context's launch stream for a scope (the stage timers follow it).
+struct StreamScope {
+  litho_ctx* ctx;
+  cudaStream_t saved;
+  StreamScope(litho_ctx* c, cudaStream_t s) : ctx(c), saved(c->stream) { c->stream = s; }
+  ~StreamScope() { ctx->stream = saved; }
+};
+
 // enqueue one class on the context's stream: windows of its sub-batches, SOCS,
 // interpolation
 static int run_class(litho_batch_plan* bp, int ci) {
@@ -87,16 +99,41 @@ static int run_class(litho_batch_plan* bp, int ci) {
   const int Nx = c.ks->Nx, Ny = c.ks->Ny, KY = 2 * Ny + 1;
   LITHO_CUDA_TRY(ctx, cudaMemsetAsync(c.win.p, 0, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2),
                                       ctx->stream));
-  for (const SubBatch& s : bp->subs) {
-    if (s.cls != ci) continue;
+  // The sub-batches' window DFTs (one per mask size; each writes its own images'
+  // partials) run as parallel branches, the largest on the context's stream: all of them
+  // stream masks from HBM, so each fills the others' ramps and tails.
+  std::vector<const SubBatch*> sb;
+  for (const SubBatch& s : bp->subs)
+    if (s.cls == ci) sb.push_back(&s);
+  std::stable_sort(sb.begin(), sb.end(), [](const SubBatch* a, const SubBatch* b) {
+    return (size_t)a->count * a->mLx * a->mLy > (size_t)b->count * b->mLx * b->mLy;
+  });
+  auto win_plan = [&](const SubBatch& s) {
     ImgGeom gw{s.mLx, s.mLy, c.L, c.L, Nx, Ny, c.ks->nk, c.convN};
     ImgPlan pw = make_plan(gw, s.count, ctx->sm_count);
     pw.colSplits = std::min(c.colSplits, std::max(1, tc ? (s.mLx + 63) / 64 / 2 : (s.mLx + 63) / 64));
     pw.part_stride = c.part_stride;
+    return pw;
+  };
+  if (sb.size() > 1) {
+    // tables shared between sub-batches are built here, before the fork
+    for (const SubBatch* s : sb) {
+      const ImgPlan pw = win_plan(*s);
+      LITHO_RET(tc ? prepare_win_dft_tc(ctx, pw) : prepare_win_dft(ctx, pw));
+    }
+    LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[0], ctx->stream));
+    for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(bp->wstreams[k - 1], bp->wevents[0], 0));
+  }
+  for (size_t k = 0; k < sb.size(); ++k) {
+    const SubBatch& s = *sb[k];
+    StreamScope scope(ctx, k == 0 ? ctx->stream : bp->wstreams[k - 1]);
+    const ImgPlan pw = win_plan(s);
     float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
     if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));
     else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
+    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[k], ctx->stream));
   }
+  for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->wevents[k], 0));
   ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
   p.kpg = std::min(c.kpg, c.ks->nk);
   p.ngroups = (c.ks->nk + p.kpg - 1) / p.kpg;
@@ -295,6 +332,27 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
       return rc;
     }
   }
+  // branch streams and events for the sub-batches' window DFTs (as many as the largest
+  // class has sub-batches)
+  {
+    std::vector<int> per(nsets, 0);
+    int most = 0;
+    for (const auto& sbt : bp->subs) most = std::max(most, ++per[sbt.cls]);
+    for (int k = 0; k < most && rc == LITHO_OK; ++k) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = LITHO_ERR_CUDA;
+      else bp->wevents.push_back(e);
+      if (rc == LITHO_OK && k > 0) {
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = LITHO_ERR_CUDA;
+        else bp->wstreams.push_back(st);
+      }
+    }
+    if (rc != LITHO_OK) {
+      litho_batch_plan_destroy(bp);
+      return rc;
+    }
+  }
   // zero the mask slots so tuning runs read defined data
   if (cudaMemsetAsync(bp->mask_pool.p, 0, mask_floats * sizeof(float), ctx->stream) != cudaSuccess) {
     litho_batch_plan_destroy(bp);
@@ -397,6 +455,11 @@ int litho_batch_plan_destroy(litho_batch_plan* bp) {
     c.band.release();
     c.tmbuf.release();
   }
+  for (cudaStream_t st : bp->wstreams) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  for (cudaEvent_t e : bp->wevents) cudaEventDestroy(e);
   bp->mask_pool.release();
   bp->image_pool.release();
   delete bp;

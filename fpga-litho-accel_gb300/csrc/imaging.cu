@@ -1083,6 +1083,15 @@ static int launch_win_dft_t(litho_ctx* ctx, const ImgPlan& p, const float* masks
   return LITHO_OK;
 }
 
+// Build the cached column-twiddle table a plain window DFT of this geometry reads, on the
+// context's stream (so that launches on other streams find it ready).
+int prepare_win_dft(litho_ctx* ctx, const ImgPlan& p) {
+  const int NJT = njt_for(p.g.Nx);
+  if (NJT < 0) return LITHO_OK;  // the launch reports the unsupported size
+  const float* twx = nullptr;
+  return twx_table(ctx, p.g.Lx, p.g.Fx, p.g.Nx, NJT, &twx);
+}
+
 int run_win_dft(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
   const int NJT = njt_for(p.g.Nx);
   if (NJT < 0) {

@@ -964,30 +964,38 @@ static int cached_table(litho_ctx* ctx, std::tuple<int, int, int, int> key, size
   return LITHO_OK;
 }
 
+// Column twiddles (hi/lo TF32 rows) and epilogue row twiddles of one window geometry,
+// cached in the context and built on first use on the context's stream.
 template <int NBH>
-static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
-  const ImgGeom& g = p.g;
+static int win_tc_tables(litho_ctx* ctx, const ImgGeom& g, float** twh, float** yt) {
   bool fresh = false;
   float* tw = nullptr;
   LITHO_RET(cached_table(ctx, std::make_tuple(g.Lx, g.Fx, g.Nx, -NBH), (size_t)2 * NBH * g.Lx * sizeof(float),
                          &fresh, &tw));
-  float* twh = tw;
-  float* twl = tw + (size_t)NBH * g.Lx;
   if (fresh) {
     StageScope sc(ctx, LITHO_STAGE_UPLOAD);
-    twT_init_kernel<<<dim3((g.Lx + 127) / 128, NBH), 128, 0, ctx->stream>>>(twh, twl, g.Lx, g.Fx, g.Nx, NBH);
+    twT_init_kernel<<<dim3((g.Lx + 127) / 128, NBH), 128, 0, ctx->stream>>>(tw, tw + (size_t)NBH * g.Lx, g.Lx, g.Fx,
+                                                                            g.Nx, NBH);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   // row twiddles of the epilogue, cached per (Ly, Fy, Ny)
-  float* yt = nullptr;
   LITHO_RET(cached_table(ctx, std::make_tuple(g.Ly, g.Fy, g.Ny, -3000), (size_t)(g.Ny + 1) * g.Ly * sizeof(float2),
-                         &fresh, &yt));
+                         &fresh, yt));
   if (fresh) {
     StageScope sc(ctx, LITHO_STAGE_UPLOAD);
     ytab_init_kernel<<<dim3((g.Ly + 127) / 128, g.Ny + 1), 128, 0, ctx->stream>>>(
-        reinterpret_cast<float2*>(yt), g.Ly, g.Fy);
+        reinterpret_cast<float2*>(*yt), g.Ly, g.Fy);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
+  *twh = tw;
+  return LITHO_OK;
+}
+
+template <int NBH>
+static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
+  const ImgGeom& g = p.g;
+  float *twh = nullptr, *yt = nullptr;
+  LITHO_RET(win_tc_tables<NBH>(ctx, g, &twh, &yt));
   CUtensorMap mM, mB;
   LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
   LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
@@ -1008,6 +1016,22 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
                                                                   p.part_stride, err, ctx->test_stall_chunk);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
+}
+
+// Build the cached tables and the timeout flag a mixed window DFT of this geometry reads,
+// on the context's stream (so that launches on other streams find them ready).
+int prepare_win_dft_tc(litho_ctx* ctx, const ImgPlan& p) {
+  int* err = nullptr;
+  LITHO_RET(tc_err_flag(ctx, &err));
+  float *twh = nullptr, *yt = nullptr;
+  switch (nb_for(p.g.Nx)) {
+    case 8: return win_tc_tables<8>(ctx, p.g, &twh, &yt);
+    case 16: return win_tc_tables<16>(ctx, p.g, &twh, &yt);
+    case 24: return win_tc_tables<24>(ctx, p.g, &twh, &yt);
+    case 32: return win_tc_tables<32>(ctx, p.g, &twh, &yt);
+    case 40: return win_tc_tables<40>(ctx, p.g, &twh, &yt);
+    default: return LITHO_OK;  // the launch reports the unsupported size
+  }
 }
 
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {

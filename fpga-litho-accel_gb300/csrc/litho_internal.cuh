@@ -207,6 +207,7 @@ struct WindowSrc {
 };
 
 int run_win_dft(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+int prepare_win_dft(litho_ctx* ctx, const ImgPlan& p);  // cached tables, on ctx->stream
 int run_socs(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const float2* krn,
              const float* scales, float2* band_part, float* tmpImgp);
 int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm, float* images);
@@ -226,6 +227,7 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
+int prepare_win_dft_tc(litho_ctx* ctx, const ImgPlan& p);  // cached tables and timeout flag
 int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images);
 struct FiTcBufs {
   float *tmh, *tml, *t0;

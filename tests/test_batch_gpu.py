@@ -48,9 +48,13 @@ def test_batch_plan_uneven_sizes(ctx, L, classes, prec_name, tol):
     prec = L.PREC_FP32 if prec_name == "fp32" else L.PREC_MIXED
     sets = [ctx.kernel_set(k[0], k[1], k[2], k[2]) for _, k in classes]
     periods = [p for p, _ in classes]
-    items = [(0, 256, 256), (1, 512, 512), (0, 512, 512), (1, 1024, 1024), (1, 768, 768), (0, 256, 256)]
+    # (class, Lx, Ly): several sizes per class, whose window DFTs run as parallel branches;
+    # the rectangular ones share a row or column length (and so a twiddle table) with others
+    items = [(0, 256, 256), (1, 512, 512), (0, 512, 512), (1, 1024, 1024), (1, 768, 768), (0, 256, 256),
+             (1, 768, 1024), (0, 512, 256)]
     plan = L.BatchPlan(ctx, sets, periods, items, precision=prec)
-    masks = [synth.density_rect_mask(m, 0.2 + 0.08 * i, seed=60 + i) for i, (_, m, _) in enumerate(items)]
+    masks = [np.ascontiguousarray(synth.density_rect_mask(max(x, y), 0.2 + 0.06 * i, seed=60 + i)[:y, :x])
+             for i, (_, x, y) in enumerate(items)]
     for i, m in enumerate(masks):
         plan.mask(i).copy_(torch.from_numpy(m))
     torch.cuda.synchronize()
