@@ -704,112 +704,170 @@ __global__ void __launch_bounds__(S128_THREADS) socs128_kernel(
 
 // ---------------------------------------------------------------------------
 // FI, step 1: T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx} for fy = 0..2Ny
-// (T[-fy] = conj(T[fy]) because the intensity is real).  One thread per image
-// column X and half of the fy rows; the column twiddles live in registers and
-// the band, summed over its kernel-group partials in a fixed order, sits in
-// shared memory pre-combined as C[fy][d] = (Re(p+q), -Im(p-q), Im(p+q), Re(p-q))
-// for p = S[fy][d], q = S[fy][-d], so that
-//   T = S0 + sum_{d>0} (p t + q conj(t)),  t = e^{+2 pi i d x'/Fx},
-// costs one broadcast shared load and two packed (f32x2) FMAs per (fy, d).
+// (T[-fy] = conj(T[fy]) because the intensity is real), x' = X + (Fx-Lx)/2 - Fx/2.
+// The band, summed over its kernel-group partials in a fixed order, sits in shared
+// memory pre-combined as C[fy][d] = (Re(p+q), -Im(p-q), Im(p+q), Re(p-q)) for
+// p = S[fy][d], q = S[fy][-d].  With t = e^{+2 pi i d x'/Fx},
+//   T(x') = S0 + U + V,  T(-x') = S0 + U - V,
+//   U = sum_{d>0} (p+q) Re t,  V = sum_{d>0} i (p-q) Im t,
+// so one thread serves a column with x' < 0 and its mirror -x': its packed
+// (f32x2) FMAs keep the cos and sin halves apart, and one broadcast shared load
+// and two packed FMAs per (fy, d) give both columns.  The columns with x' < 0
+// are X in [0, nb), nb = Fx/2 - (Fx-Lx)/2; the mirror of X is 2nb - X when that
+// lies inside the image; the column x' = 0 (X = nb) is S0 + sum_{d>0} (p+q) and
+// is summed by one warp of the first column block.  A CTA keeps its columns'
+// twiddles in registers and walks the images blockIdx.y, blockIdx.y + gridDim.y, ...
 // Two output layouts:
 //   plain  tm[img][r][X]: r = 0 Re T0, 1..2Ny Re T, 2Ny+1..4Ny Im T (fi_out_kernel)
 //   K-major (tensor-core FI) t0[img][X] = Re T0 and hi/lo TF32 splits of
 //          tm[img][X][KP]: r = fy-1 Re T, 2Ny+fy-1 Im T, zero to KP
 // ---------------------------------------------------------------------------
-constexpr int FR_THREADS = 256, FR_COLS = 128;
+constexpr int FR_THREADS = 256, FR_COLS = 128, FR_ROWS = 2 * FR_COLS + 1;  // column, mirror, x' = 0
 
 template <int MAXD, bool KMAJ>
 __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __restrict__ band_part, int ngroups,
                                                              const float2* __restrict__ twF, int Lx, int Fx,
-                                                             int Nx, int Ny, int KP, float* __restrict__ tm,
-                                                             float* __restrict__ tmh, float* __restrict__ tml,
-                                                             float* __restrict__ t0) {
+                                                             int Nx, int Ny, int KP, int batch,
+                                                             float* __restrict__ tm, float* __restrict__ tmh,
+                                                             float* __restrict__ tml, float* __restrict__ t0) {
   extern __shared__ __align__(16) float4 frs[];
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
   float4* sC = frs;                                       // [BH][MAXD]
-  float* sO = reinterpret_cast<float*>(sC + BH * MAXD);  // K-major: [FR_COLS][KP + 1]
-  const int tid = threadIdx.x, img = blockIdx.y, X0 = blockIdx.x * FR_COLS;
-  const int xl = tid & (FR_COLS - 1), grp = tid / FR_COLS;
-  const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-  const size_t pst = (size_t)BH * BW;
-  for (int idx = tid; idx < BH * ND; idx += FR_THREADS) {
-    const int fy = idx / ND, d = idx - fy * ND;
-    const float2* S = B + fy * BW + 2 * Nx;
-    const float2 pv = sum_strided(S + d, pst, ngroups);
-    if (d == 0) {
-      sC[fy * MAXD] = make_float4(pv.x, pv.y, 0.f, 0.f);
-    } else {
-      const float2 qv = sum_strided(S - d, pst, ngroups);
-      sC[fy * MAXD + d] = make_float4(pv.x + qv.x, -(pv.y - qv.y), pv.y + qv.y, pv.x - qv.x);
-    }
-  }
-  if (KMAJ)
-    for (int idx = tid; idx < FR_COLS * (KP - 4 * Ny); idx += FR_THREADS) {
-      const int c = idx / (KP - 4 * Ny), r = 4 * Ny + idx % (KP - 4 * Ny);
-      sO[c * (KP + 1) + r] = 0.f;
-    }
-  const int X = X0 + xl;
-  const bool live = X < Lx;
-  const long long xp = (long long)X + (Fx - Lx) / 2 - Fx / 2;
+  float* sO = reinterpret_cast<float*>(sC + BH * MAXD);  // K-major: [FR_ROWS][KP + 1]
+  const int tid = threadIdx.x, xl = tid & (FR_COLS - 1), grp = tid / FR_COLS;
+  const int nb = Fx / 2 - (Fx - Lx) / 2, M = 2 * nb;
+  const int X0 = blockIdx.x * FR_COLS, X = X0 + xl, Xm = M - X;
+  const bool live = X < nb, mlive = live && Xm < Lx;
+  const bool xtra = blockIdx.x == 0 && nb < Lx;  // this block adds the column x' = 0
   float2 tw[MAXD];
 #pragma unroll
   for (int d = 1; d < MAXD; ++d)
-    tw[d] = (d < ND && live) ? (twF != nullptr ? twF[(size_t)d * Lx + X] : cis_exact((long long)d * xp, Fx, 1.f))
+    tw[d] = (d < ND && live) ? (twF != nullptr ? twF[(size_t)d * Lx + X] : cis_exact((long long)d * (X - nb), Fx, 1.f))
                              : make_float2(0.f, 0.f);
-  __syncthreads();
+  if (KMAJ)  // the K padding columns stay zero for every image
+    for (int idx = tid; idx < FR_ROWS * (KP - 4 * Ny); idx += FR_THREADS) {
+      const int c = idx / (KP - 4 * Ny), r = 4 * Ny + idx % (KP - 4 * Ny);
+      sO[c * (KP + 1) + r] = 0.f;
+    }
   const int fy0 = grp == 0 ? 0 : Ny + 1, fy1 = grp == 0 ? Ny + 1 : BH;
-  float* out = KMAJ ? nullptr : tm + (size_t)img * (4 * Ny + 1) * Lx;
-  for (int fy = fy0; fy < fy1; ++fy) {
-    const float4* C = sC + fy * MAXD;
-    // four independent FMA chains as two packed pairs: (ra, rb) += (c0, c1) * t and
-    // (ia, ib) += (c2, c3) * t with t = (cos, sin) of the column, one f32x2 FMA each
-    // (per component the same fmaf); without the term guard when 2Nx+1 is the table width
-    float2 r = make_float2(C[0].x, 0.f), i2 = make_float2(C[0].y, 0.f);
-    if (ND == MAXD) {
-#pragma unroll
-      for (int d = 1; d < MAXD; ++d) {
-        const float4 a = C[d];
-        r = __ffma2_rn(make_float2(a.x, a.y), tw[d], r);
-        i2 = __ffma2_rn(make_float2(a.z, a.w), tw[d], i2);
+  const size_t pst = (size_t)BH * BW;
+  // rows of this block in the K-major store: its columns X0.., their mirrors (ascending
+  // X = Mlo + j for slots FR_COLS + nbase - 1 - j) and, in the first block, x' = 0
+  const int nbase = max(0, min(FR_COLS, nb - X0));
+  const int imin = max(0, M - X0 - Lx + 1);
+  const int nmir = max(0, nbase - imin), Mlo = M - X0 - nbase + 1;
+  const int nrows = nbase + nmir + (xtra ? 1 : 0);
+  for (int img = blockIdx.y; img < batch; img += gridDim.y) {
+    __syncthreads();  // the previous image is out of sC and sO
+    const float2* B = band_part + (size_t)img * ngroups * BH * BW;
+    for (int idx = tid; idx < BH * ND; idx += FR_THREADS) {
+      const int fy = idx / ND, d = idx - fy * ND;
+      const float2* S = B + fy * BW + 2 * Nx;
+      const float2 pv = sum_strided(S + d, pst, ngroups);
+      if (d == 0) {
+        sC[fy * MAXD] = make_float4(pv.x, pv.y, 0.f, 0.f);
+      } else {
+        const float2 qv = sum_strided(S - d, pst, ngroups);
+        sC[fy * MAXD + d] = make_float4(pv.x + qv.x, -(pv.y - qv.y), pv.y + qv.y, pv.x - qv.x);
       }
-    } else {
+    }
+    __syncthreads();
+    float* out = KMAJ ? nullptr : tm + (size_t)img * (4 * Ny + 1) * Lx;
+    for (int fy = fy0; fy < fy1; ++fy) {
+      const float4* C = sC + fy * MAXD;
+      // four independent FMA chains as two packed pairs: (ra, rb) += (c0, c1) * t and
+      // (ia, ib) += (c2, c3) * t with t = (cos, sin) of the column, one f32x2 FMA each
+      // (per component the same fmaf); without the term guard when 2Nx+1 is the table width
+      float2 r = make_float2(C[0].x, 0.f), i2 = make_float2(C[0].y, 0.f);
+      if (ND == MAXD) {
 #pragma unroll
-      for (int d = 1; d < MAXD; ++d) {
-        if (d < ND) {
+        for (int d = 1; d < MAXD; ++d) {
           const float4 a = C[d];
           r = __ffma2_rn(make_float2(a.x, a.y), tw[d], r);
           i2 = __ffma2_rn(make_float2(a.z, a.w), tw[d], i2);
         }
-      }
-    }
-    const float re = r.x + r.y, im = i2.x + i2.y;
-    if (!live) continue;
-    if (KMAJ) {
-      if (fy == 0) {
-        t0[(size_t)img * Lx + X] = re;
       } else {
-        sO[xl * (KP + 1) + fy - 1] = re;
-        sO[xl * (KP + 1) + 2 * Ny + fy - 1] = im;
+#pragma unroll
+        for (int d = 1; d < MAXD; ++d) {
+          if (d < ND) {
+            const float4 a = C[d];
+            r = __ffma2_rn(make_float2(a.x, a.y), tw[d], r);
+            i2 = __ffma2_rn(make_float2(a.z, a.w), tw[d], i2);
+          }
+        }
       }
-    } else if (fy == 0) {
-      out[X] = re;
-    } else {
-      out[(size_t)fy * Lx + X] = re;
-      out[(size_t)(2 * Ny + fy) * Lx + X] = im;
+      if (!live) continue;
+      const float re = r.x + r.y, im = i2.x + i2.y, rem = r.x - r.y, imm = i2.x - i2.y;
+      if (KMAJ) {
+        if (fy == 0) {
+          t0[(size_t)img * Lx + X] = re;
+          if (mlive) t0[(size_t)img * Lx + Xm] = rem;
+        } else {
+          sO[xl * (KP + 1) + fy - 1] = re;
+          sO[xl * (KP + 1) + 2 * Ny + fy - 1] = im;
+          sO[(FR_COLS + xl) * (KP + 1) + fy - 1] = rem;  // unused when the mirror is outside
+          sO[(FR_COLS + xl) * (KP + 1) + 2 * Ny + fy - 1] = imm;
+        }
+      } else if (fy == 0) {
+        out[X] = re;
+        if (mlive) out[Xm] = rem;
+      } else {
+        out[(size_t)fy * Lx + X] = re;
+        out[(size_t)(2 * Ny + fy) * Lx + X] = im;
+        if (mlive) {
+          out[(size_t)fy * Lx + Xm] = rem;
+          out[(size_t)(2 * Ny + fy) * Lx + Xm] = imm;
+        }
+      }
     }
-  }
-  if (KMAJ) {
-    __syncthreads();
-    // rows X0 .. X0 + ncol - 1 of [X][KP] are one contiguous run: float4 stores
-    const int ncol = min(FR_COLS, Lx - X0);
-    const size_t base = ((size_t)img * Lx + X0) * KP;
-    for (int e = tid; e < ncol * KP / 4; e += FR_THREADS) {
-      const int xr = (4 * e) / KP, r = 4 * e - xr * KP;
-      const float* v = sO + xr * (KP + 1) + r;
-      const float h0 = tc::tf32_round(v[0]), h1 = tc::tf32_round(v[1]), h2 = tc::tf32_round(v[2]),
-                  h3 = tc::tf32_round(v[3]);
-      reinterpret_cast<float4*>(tmh + base)[e] = make_float4(h0, h1, h2, h3);
-      reinterpret_cast<float4*>(tml + base)[e] = make_float4(v[0] - h0, v[1] - h1, v[2] - h2, v[3] - h3);
+    if (xtra && tid < 32) {  // the column x' = 0: S0 + sum_{d>0} (p + q), d in order
+      for (int fy = tid; fy < BH; fy += 32) {
+        const float4* C = sC + fy * MAXD;
+        float re = C[0].x, im = C[0].y;
+        for (int d = 1; d < ND; ++d) {
+          re += C[d].x;
+          im += C[d].z;
+        }
+        if (KMAJ) {
+          if (fy == 0) {
+            t0[(size_t)img * Lx + nb] = re;
+          } else {
+            sO[2 * FR_COLS * (KP + 1) + fy - 1] = re;
+            sO[2 * FR_COLS * (KP + 1) + 2 * Ny + fy - 1] = im;
+          }
+        } else if (fy == 0) {
+          out[nb] = re;
+        } else {
+          out[(size_t)fy * Lx + nb] = re;
+          out[(size_t)(2 * Ny + fy) * Lx + nb] = im;
+        }
+      }
+    }
+    if (KMAJ) {
+      __syncthreads();
+      // each row is KP floats of [X][KP]: float4 stores, rows of one run contiguous
+      const int q4 = KP / 4;
+      for (int e = tid; e < nrows * q4; e += FR_THREADS) {
+        const int s = e / q4, c = 4 * (e - s * q4);
+        int srow, Xg;
+        if (s < nbase) {
+          srow = s;
+          Xg = X0 + s;
+        } else if (s < nbase + nmir) {
+          const int j = s - nbase;
+          srow = FR_COLS + nbase - 1 - j;
+          Xg = Mlo + j;
+        } else {
+          srow = 2 * FR_COLS;
+          Xg = nb;
+        }
+        const float* v = sO + srow * (KP + 1) + c;
+        const float h0 = tc::tf32_round(v[0]), h1 = tc::tf32_round(v[1]), h2 = tc::tf32_round(v[2]),
+                    h3 = tc::tf32_round(v[3]);
+        const size_t o = ((size_t)img * Lx + Xg) * KP + c;
+        *reinterpret_cast<float4*>(tmh + o) = make_float4(h0, h1, h2, h3);
+        *reinterpret_cast<float4*>(tml + o) = make_float4(v[0] - h0, v[1] - h1, v[2] - h2, v[3] - h3);
+      }
     }
   }
 }
@@ -819,12 +877,18 @@ static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const floa
                                     int KP, float* tm, float* tmh, float* tml, float* t0) {
   const ImgGeom& g = p.g;
   const size_t smem = (size_t)(2 * g.Ny + 1) * MAXD * sizeof(float4) +
-                      (KMAJ ? (size_t)FR_COLS * (KP + 1) * sizeof(float) : 0);
+                      (KMAJ ? (size_t)FR_ROWS * (KP + 1) * sizeof(float) : 0);
   auto k = fi_rows_kernel<MAXD, KMAJ>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<dim3((g.Lx + FR_COLS - 1) / FR_COLS, p.batch), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx,
-                                                                          g.Nx, g.Ny, KP, tm, tmh, tml, t0);
+  // column blocks over the x' < 0 half; enough image groups for a few CTAs per SM,
+  // each CTA walking its group's images with its twiddles kept in registers
+  const int nb = g.Fx / 2 - (g.Fx - g.Lx) / 2;
+  const int ncb = std::max(1, (nb + FR_COLS - 1) / FR_COLS);
+  const int sms = p.sms > 0 ? p.sms : 148;
+  const int groups = std::max(1, std::min(p.batch, (4 * sms + ncb - 1) / ncb));
+  k<<<dim3(ncb, groups), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx, g.Nx, g.Ny, KP, p.batch, tm,
+                                                tmh, tml, t0);
   return cudaGetLastError();
 }
 
@@ -1043,6 +1107,7 @@ ImgPlan make_plan(const ImgGeom& g, int batch, int sm_count) {
   ng = std::max(1, std::min(ng, g.nk));
   p.kpg = (g.nk + ng - 1) / ng;
   p.ngroups = (g.nk + p.kpg - 1) / p.kpg;
+  p.sms = sm_count;
   return p;
 }
 

@@ -183,6 +183,7 @@ struct ImgPlan {
   int rowBlocks = 1, colSplits = 1;  // window-DFT partition -> nparts
   int kpg = 1, ngroups = 1;          // SOCS kernels per CTA -> ngroups
   int part_stride = 0;               // >0: window partials per image in a shared per-class array
+  int sms = 0;                       // SMs of the device (launch sizing)
   int nparts() const { return rowBlocks * colSplits; }
 };
 
