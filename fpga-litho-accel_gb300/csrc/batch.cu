@@ -36,16 +36,16 @@ struct ClassRun {
   const litho_kernel_set* ks = nullptr;
   int count = 0, maxM = 0;
   float* images = nullptr;
-  DevBuf win, band, tmbuf;
-  int convN = 0, kpg = 1, colSplits = 1, part_stride = 1;
+  DevBuf win, band, tmbuf, wsum;
+  int convN = 0, kpg = 1, colSplits = 1, part_stride = 1;  // convN == 0: the TCC band (band_tcc.cu)
   double tuned_ms = -1.0;
   int candidates = 0;
 };
 
 struct TuneKey {
-  int L, Nx, nk, count, prec;
+  int L, Nx, nk, count, prec, band;
   bool operator<(const TuneKey& o) const {
-    return std::tie(L, Nx, nk, count, prec) < std::tie(o.L, o.Nx, o.nk, o.count, o.prec);
+    return std::tie(L, Nx, nk, count, prec, band) < std::tie(o.L, o.Nx, o.nk, o.count, o.prec, o.band);
   }
 };
 struct TuneVal {
@@ -134,13 +134,15 @@ static int run_class(litho_batch_plan* bp, int ci) {
     if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[k], ctx->stream));
   }
   for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->wevents[k], 0));
-  ImgPlan p = make_plan(class_geom(c, c.convN), c.count, ctx->sm_count);
-  p.kpg = std::min(c.kpg, c.ks->nk);
-  p.ngroups = (c.ks->nk + p.kpg - 1) / p.kpg;
+  const bool band = c.convN == 0;
+  ImgPlan p = make_plan(class_geom(c, band ? default_conv(Nx, Ny) : c.convN), c.count, ctx->sm_count);
+  p.kpg = band ? c.ks->nk : std::min(c.kpg, c.ks->nk);
+  p.ngroups = band ? c.ks->band_nc : (c.ks->nk + p.kpg - 1) / p.kpg;
   WindowSrc w;
   w.part = c.win.as<float2>();
   w.nparts = c.part_stride;
-  LITHO_RET(run_socs(ctx, p, w, c.ks->krn, c.ks->scales, c.band.as<float2>(), nullptr));
+  if (band) LITHO_RET(run_band_tcc(ctx, p, w, c.ks, c.wsum.as<float2>(), c.band.as<float2>()));
+  else LITHO_RET(run_socs(ctx, p, w, c.ks->krn, c.ks->scales, c.band.as<float2>(), nullptr));
   if (tc) return run_fi_tc(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
   return run_fi(ctx, p, c.band.as<float2>(), c.tmbuf.as<float>(), c.images);
 }
@@ -181,7 +183,9 @@ static int time_class(litho_batch_plan* bp, int ci, float* ms) {
 
 static int tune_class(litho_batch_plan* bp, int ci) {
   ClassRun& c = bp->classes[ci];
-  const TuneKey key{c.L, c.ks->Nx, c.ks->nk, c.count, bp->precision};
+  const bool band_ok = use_band_tcc(bp->ctx, c.ks);
+  const int method = band_ok ? (bp->ctx->band_method == LITHO_BAND_TCC ? 2 : 1) : 0;
+  const TuneKey key{c.L, c.ks->Nx, c.ks->nk, c.count, bp->precision, method};
   auto it = g_tune_cache.find(key);
   if (it != g_tune_cache.end()) {
     c.convN = it->second.convN;
@@ -190,18 +194,25 @@ static int tune_class(litho_batch_plan* bp, int ci) {
     c.tuned_ms = it->second.ms;
     return LITHO_OK;
   }
+  // band forms: conv grids of the FFT form, and 0 for the TCC band where the kernel set
+  // has a table (with LITHO_BAND_TCC the TCC band alone)
   const int n0 = default_conv(c.ks->Nx, c.ks->Ny);
-  std::vector<int> convs{n0};
-  if (2 * n0 <= 128) convs.push_back(2 * n0);
+  std::vector<int> convs;
+  if (method != 2) {
+    convs.push_back(n0);
+    if (2 * n0 <= 128) convs.push_back(2 * n0);
+  }
+  if (band_ok) convs.push_back(0);
   std::vector<int> kpgs;
   for (int k : {2, 3, 4, 6, 8, 12})
     if (k <= c.ks->nk) kpgs.push_back(k);
   if (kpgs.empty()) kpgs.push_back(1);
   std::vector<int> splits{1, 2};
-  TuneVal best{n0, kpgs[0], 1, 1e30};
+  TuneVal best{convs[0], kpgs[0], 1, 1e30};
   for (int cn : convs)
     for (int k : kpgs)
       for (int sp : splits) {
+        if (cn == 0 && k != kpgs[0]) continue;  // kernels per CTA do not apply to the TCC band
         c.convN = cn;
         c.kpg = k;
         c.colSplits = sp;
@@ -322,8 +333,10 @@ int litho_batch_plan_create(litho_ctx* ctx, const litho_kernel_set* const* sets,
     const int Nx = c.ks->Nx, Ny = c.ks->Ny, KY = 2 * Ny + 1;
     c.part_stride = ((c.maxM + 127) / 128) * 2;  // row blocks x up to two column splits
     rc = c.win.ensure(ctx, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2));
-    if (rc == LITHO_OK) rc = c.band.ensure(ctx, (size_t)c.count * c.ks->nk * KY * (4 * Nx + 1) * sizeof(float2));
+    const int groups = std::max(c.ks->nk, c.ks->band_nc);  // the FFT form's kernel groups or the band chunks
+    if (rc == LITHO_OK) rc = c.band.ensure(ctx, (size_t)c.count * groups * KY * (4 * Nx + 1) * sizeof(float2));
     const ImgGeom g = class_geom(c, c.convN);
+    if (rc == LITHO_OK && c.ks->band_nc > 0) rc = c.wsum.ensure(ctx, band_wsum_bytes(g, c.count));
     const size_t tmb = precision == LITHO_PREC_MIXED ? fi_tc_workspace_bytes(g, c.count)
                                                      : (size_t)c.count * (4 * Ny + 1) * c.L * sizeof(float);
     if (rc == LITHO_OK) rc = c.tmbuf.ensure(ctx, tmb);
@@ -423,10 +436,11 @@ int litho_batch_plan_describe(const litho_batch_plan* bp, char* buf, int cap) {
     if (c.count == 0) continue;
     char t[512];
     snprintf(t, sizeof t,
-             "%s{\"period\": %d, \"Nx\": %d, \"nk\": %d, \"images\": %d, \"conv_n\": %d, \"kernels_per_cta\": %d, "
-             "\"window_col_splits\": %d, \"tuned_ms\": %.4f, \"candidates\": %d}",
-             first ? "" : ", ", c.L, c.ks->Nx, c.ks->nk, c.count, c.convN, c.kpg, c.colSplits, c.tuned_ms,
-             c.candidates);
+             "%s{\"period\": %d, \"Nx\": %d, \"nk\": %d, \"images\": %d, \"band\": \"%s\", \"conv_n\": %d, "
+             "\"kernels_per_cta\": %d, \"band_chunks\": %d, \"window_col_splits\": %d, \"tuned_ms\": %.4f, "
+             "\"candidates\": %d}",
+             first ? "" : ", ", c.L, c.ks->Nx, c.ks->nk, c.count, c.convN == 0 ? "tcc" : "fft", c.convN,
+             c.convN == 0 ? 0 : c.kpg, c.convN == 0 ? c.ks->band_nc : 0, c.colSplits, c.tuned_ms, c.candidates);
     s += t;
     first = false;
   }
@@ -454,6 +468,7 @@ int litho_batch_plan_destroy(litho_batch_plan* bp) {
     c.win.release();
     c.band.release();
     c.tmbuf.release();
+    c.wsum.release();
   }
   for (cudaStream_t st : bp->wstreams) {
     cudaStreamSynchronize(st);

@@ -126,7 +126,7 @@ int litho_ctx_destroy(litho_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->win_part, &ctx->band_part, &ctx->tm,     &ctx->stage_in, &ctx->stage_out,
                     &ctx->stage_k,  &ctx->stage_s,   &ctx->stage_x, &ctx->tcc_a,   &ctx->tcc_b,
                     &ctx->tcc_c,    &ctx->tcc_pq,  &ctx->eig_w,     &ctx->eig_v,   &ctx->eig_work, &ctx->eig_info,
-                    &ctx->mx_b,     &ctx->mx_c,      &ctx->mx_d};
+                    &ctx->mx_b,     &ctx->mx_c,      &ctx->mx_d,    &ctx->band_w};
   for (DevBuf* b : bufs) b->release();
   for (auto& kv : ctx->twx_tables) kv.second.release();
   for (auto& p : ctx->pending) {
@@ -172,6 +172,14 @@ int litho_ctx_set_test_stall(litho_ctx* ctx, int chunk) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_ARG_CHECK(ctx, chunk >= -1, "chunk must be >= -1 (-1 turns the hook off)");
   ctx->test_stall_chunk = chunk;
+  return LITHO_OK;
+}
+
+int litho_ctx_set_band_method(litho_ctx* ctx, int method) {
+  if (ctx == nullptr) return LITHO_ERR_ARG;
+  LITHO_ARG_CHECK(ctx, method == LITHO_BAND_AUTO || method == LITHO_BAND_FFT || method == LITHO_BAND_TCC,
+                  "bad band method %d", method);
+  ctx->band_method = method;
   return LITHO_OK;
 }
 
@@ -341,7 +349,7 @@ static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* 
     LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_in[sl], ctx->copy_in));
     LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[sl], 0));
     if (k >= NS) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_out[sl], 0));  // slot drained
-    LITHO_RET(image_pipeline(ctx, g, nb, reinterpret_cast<const float*>(in), ks->krn, ks->scales,
+    LITHO_RET(image_pipeline(ctx, g, nb, reinterpret_cast<const float*>(in), ks,
                              reinterpret_cast<float*>(out), precision));
     LITHO_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_comp[sl], ctx->stream));
     LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_comp[sl], 0));
@@ -430,10 +438,12 @@ int litho_kernel_set_create(litho_ctx* ctx, const float* krn_r, const float* krn
     return LITHO_ERR_NOMEM;
   }
   int rc = upload_kernels(ctx, krn_r, krn_i, scales, nk, kdim, mem, ks->krn, ks->scales);
+  if (rc == LITHO_OK) rc = build_band_table(ctx, ks, ctx->stream);
   if (rc == LITHO_OK) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? LITHO_OK : LITHO_ERR_CUDA;
   if (rc != LITHO_OK) {
     cudaFree(ks->krn);
     cudaFree(ks->scales);
+    if (ks->band_tab) cudaFree(ks->band_tab);
     delete ks;
     return rc;
   }
@@ -446,6 +456,7 @@ int litho_kernel_set_destroy(litho_kernel_set* ks) {
   cudaSetDevice(ks->ctx->device);
   cudaFree(ks->krn);
   cudaFree(ks->scales);
+  if (ks->band_tab) cudaFree(ks->band_tab);
   delete ks;
   return LITHO_OK;
 }
@@ -466,7 +477,7 @@ int litho_image_batch(litho_ctx* ctx, const litho_kernel_set* ks, const float* m
   }
   const size_t img = (size_t)Lx * Ly * sizeof(float);
   if (mem == LITHO_MEM_DEVICE) {
-    return image_pipeline(ctx, g, batch, masks, ks->krn, ks->scales, images, precision);
+    return image_pipeline(ctx, g, batch, masks, ks, images, precision);
   }
   LITHO_RET(host_batch(ctx, g, batch, masks, ks, images, precision, img));
   LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

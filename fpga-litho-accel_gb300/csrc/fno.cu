@@ -1843,7 +1843,7 @@ int litho_surrogate_image(litho_fno* f, const litho_kernel_set* ks, const float*
       LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(f->stage_m.as<char>() + i * img, reinterpret_cast<const char*>(masks) + rej[i] * img,
                                           img, cudaMemcpyDeviceToDevice, ctx->stream));
     const ImgGeom g{L, L, L, L, ks->Nx, ks->Ny, ks->nk, default_conv_n(ks->Nx, ks->Ny)};
-    LITHO_RET(image_pipeline(ctx, g, n, f->stage_m.as<float>(), ks->krn, ks->scales, f->stage_i.as<float>(),
+    LITHO_RET(image_pipeline(ctx, g, n, f->stage_m.as<float>(), ks, f->stage_i.as<float>(),
                              LITHO_PREC_FP32));
     for (int i = 0; i < n; ++i)
       LITHO_CUDA_TRY(ctx, cudaMemcpyAsync(reinterpret_cast<char*>(images) + rej[i] * img, f->stage_i.as<char>() + i * img,

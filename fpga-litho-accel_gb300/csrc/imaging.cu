@@ -1398,13 +1398,19 @@ static ImgPlan mixed_plan(const ImgGeom& g, int batch, int sm_count) {
   return p;
 }
 
-int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const float2* krn,
-                   const float* scales, float* images, int precision) {
+int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
+                   float* images, int precision) {
   const int KY = 2 * g.Ny + 1;
   const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
+  const bool band = use_band_tcc(ctx, ks);
   ImgPlan p = tc ? mixed_plan(g, batch, ctx->sm_count) : make_plan(g, batch, ctx->sm_count);
+  if (band) {
+    p.ngroups = ks->band_nc;
+    p.kpg = g.nk;
+  }
   LITHO_RET(ctx->win_part.ensure(ctx, (size_t)batch * p.nparts() * KY * (g.Nx + 1) * sizeof(float2)));
   LITHO_RET(ctx->band_part.ensure(ctx, (size_t)batch * p.ngroups * KY * (4 * g.Nx + 1) * sizeof(float2)));
+  if (band) LITHO_RET(ctx->band_w.ensure(ctx, band_wsum_bytes(g, batch)));
   if (tc) {
     LITHO_RET(run_win_dft_tc(ctx, p, masks, ctx->win_part.as<float2>()));
   } else {
@@ -1414,7 +1420,8 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
   WindowSrc w;
   w.part = ctx->win_part.as<float2>();
   w.nparts = p.nparts();
-  LITHO_RET(run_socs(ctx, p, w, krn, scales, ctx->band_part.as<float2>(), nullptr));
+  if (band) LITHO_RET(run_band_tcc(ctx, p, w, ks, ctx->band_w.as<float2>(), ctx->band_part.as<float2>()));
+  else LITHO_RET(run_socs(ctx, p, w, ks->krn, ks->scales, ctx->band_part.as<float2>(), nullptr));
   if (tc) return run_fi_tc(ctx, p, ctx->band_part.as<float2>(), nullptr, images);
   return run_fi(ctx, p, ctx->band_part.as<float2>(), ctx->tm.as<float>(), images);
 }

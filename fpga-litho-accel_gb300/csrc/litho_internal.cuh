@@ -119,7 +119,10 @@ struct litho_ctx {
   cudaStream_t stream = nullptr;
   std::string last_error;
   // imaging workspaces
-  litho::DevBuf win_part, band_part, tm, stage_in, stage_out, stage_k, stage_s, stage_x;
+  litho::DevBuf win_part, band_part, tm, stage_in, stage_out, stage_k, stage_s, stage_x, band_w;
+  // how the SOCS band is formed for kernel sets that carry a TCC band table
+  // (litho_ctx_set_band_method): LITHO_BAND_AUTO / _FFT / _TCC
+  int band_method = 0;
   // window-DFT column twiddle tables keyed by (Lx, Fx, Nx, NJT)
   std::map<std::tuple<int, int, int, int>, litho::DevBuf> twx_tables;
   // TCC / eigensolver workspaces
@@ -151,6 +154,10 @@ struct litho_kernel_set {
   int nk = 0, Nx = 0, Ny = 0;
   float2* krn = nullptr;    // [nk][(2Ny+1)(2Nx+1)]
   float* scales = nullptr;  // [nk]
+  // rank-K TCC over the window, T(p, q) = sum_k s_k K_k(p) conj(K_k(q)), laid out for
+  // band_tcc_kernel in band_nc row chunks (band_tcc.cu); band_nc == 0: none
+  float2* band_tab = nullptr;
+  int band_nc = 0;
 };
 
 namespace litho {
@@ -224,7 +231,17 @@ int upload_kernels(litho_ctx* ctx, const float* krn_r, const float* krn_i, const
 // Full imaging pipeline on device pointers for one size class (window DFT ->
 // SOCS -> FI), FP32 or mixed precision.
 int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks,
-                   const float2* krn, const float* scales, float* images, int precision);
+                   const litho_kernel_set* ks, float* images, int precision);
+
+// the SOCS band as the bilinear form of the kernel set's rank-K TCC (band_tcc.cu)
+int build_band_table(litho_ctx* ctx, litho_kernel_set* ks, cudaStream_t stream);
+size_t band_wsum_bytes(const ImgGeom& g, int batch);
+int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const litho_kernel_set* ks,
+                 float2* wsum, float2* band_part);
+// whether a kernel set's images take the TCC band under the context's band method
+inline bool use_band_tcc(const litho_ctx* ctx, const litho_kernel_set* ks) {
+  return ks->band_nc > 0 && ctx->band_method != LITHO_BAND_FFT;
+}
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);

@@ -36,6 +36,10 @@ MEM_HOST = 0
 MEM_DEVICE = 1
 PREC_FP32 = 0
 PREC_MIXED = 1
+# how the SOCS band is formed (litho_ctx_set_band_method)
+BAND_AUTO = 0
+BAND_FFT = 1
+BAND_TCC = 2
 TCC_FP64 = 0
 TCC_SPLIT_BF16 = 1
 
@@ -73,6 +77,7 @@ _SIGS = {
     "litho_ctx_enable_timing": (_i, [_p, _i]),
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
     "litho_ctx_set_test_stall": (_i, [_p, _i]),
+    "litho_ctx_set_band_method": (_i, [_p, _i]),
     "litho_tcc_gemm_shape": (_i, [_p, _i, _i, _i]),
     "litho_tcc_gemm_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
@@ -308,6 +313,11 @@ class Context:
         """Error-path test hook (litho_ctx_set_test_stall): chunk >= 0 makes the mixed window
         DFT's TMA producer stop at that chunk, so the call returns LITHO_ERR_TIMEOUT; -1 = off."""
         self._check(_lib.litho_ctx_set_test_stall(self.h, int(chunk)))
+
+    def set_band_method(self, method: int):
+        """BAND_AUTO (default: the TCC form where the kernel set has its table), BAND_FFT (per
+        kernel FFTs on the conv grid) or BAND_TCC (litho_ctx_set_band_method)."""
+        self._check(_lib.litho_ctx_set_band_method(self.h, int(method)))
 
     def stage_times(self, reset: bool = True):
         """{stage: (device ms, kernel launches)} since the last reset (synchronises the stream)."""

@@ -60,6 +60,21 @@ extern "C" {
 #define LITHO_PREC_FP32  0
 #define LITHO_PREC_MIXED 1
 
+/* How the SOCS band is formed for a kernel set (litho_ctx_set_band_method).
+ * calcSOCS (litho.cpp:795-1006) sums s_k |IFFT(K_k . M)|^2 on the conv grid and the
+ * interpolation (FI, litho.cpp:674-754) keeps the band |f| <= 2N of that intensity.
+ * LITHO_BAND_FFT : per kernel a 2-D inverse FFT on the conv grid, |E|^2 summed,
+ *                  one forward FFT of the intensity (the reference's order).
+ * LITHO_BAND_TCC : the same band as the bilinear form of the rank-K TCC
+ *                  T(p, q) = sum_k s_k K_k(p) conj(K_k(q)) over the kernel window,
+ *                  band(f) = sum_{p-q=f} M(p) conj(M(q)) T(p, q); T is built once
+ *                  per kernel set (FP64 sums, rounded to FP32), the sums in FP32.
+ * LITHO_BAND_AUTO: TCC where the kernel set has a table (1 <= Nx <= 16, Ny <= 16),
+ *                  FFT otherwise (the default).                                  */
+#define LITHO_BAND_AUTO 0
+#define LITHO_BAND_FFT  1
+#define LITHO_BAND_TCC  2
+
 /* Arithmetic of the TCC contraction (litho.cpp:428-516).
  * LITHO_TCC_FP64      : pupil in FP32 exactly as the reference, FP64 accumulation.
  * LITHO_TCC_SPLIT_BF16: pupil split into three BF16 terms (hi*hi + hi*lo + lo*hi),
@@ -119,6 +134,14 @@ int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int r
  * (and baked into a batch plan's graph when the plan is created).  For tests of
  * the error path only. */
 int litho_ctx_set_test_stall(litho_ctx* ctx, int chunk);
+
+/* ---- band method -------------------------------------------------------------
+ * No reference counterpart (the reference has the FFT form only): selects
+ * LITHO_BAND_AUTO / _FFT / _TCC for this context's batched imaging
+ * (litho_image_batch, litho_batch_plan_create, the surrogate's fallback).  _TCC
+ * with a kernel set that has no table images with the FFT form.  Read when work is
+ * enqueued (and when a batch plan is created). */
+int litho_ctx_set_band_method(litho_ctx* ctx, int method);
 
 /* ---- optics helpers (litho.cpp:414-426, 1297-1302) --------------------- */
 /* getOuterSigma: max lit-pixel radius / ((srcSize-1)/2), clamped to 1 as

@@ -1,0 +1,143 @@
+"""Work schedule of the TCC band kernel (csrc/band_sched.hpp), compiled with g++ and
+checked on the CPU.
+
+The band of an image is band(f) = sum_{p - q = f} W(p) conj(W(q)) T(p, q) over the
+(2Ny+1) x (2Nx+1) window, for the rows fy >= 0 the interpolation reads.  The kernel
+splits that sum into task-chunks (a pair of band rows fy, 2Ny - fy, or the row Ny
+alone, cut into row chunks that write separate partial groups) and, inside a chunk,
+into 2Nx lanes that each walk three column segments over every row of the chunk.
+The schedule must visit every pair (p, q) of every band entry exactly once, each lane's
+segments must lie on the diagonal px - qx of the band column it reports, the lanes'
+reported columns must cover -2Nx..2Nx once, the table entries of a chunk must be
+addressed once each, and a chunk's table must fit the kernel's shared-memory budget.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "fpga-litho-accel_gb300", "csrc")
+
+DRIVER = r"""
+#include "band_sched.hpp"
+#include <cstdio>
+#include <map>
+#include <tuple>
+#include <vector>
+using namespace litho;
+static int fail(const char* m, int a, int b, int c) { std::printf("fail %s %d %d %d\n", m, a, b, c); return 1; }
+static int check(int Nx, int Ny) {
+  const int nc = band_tcc_chunks(Nx, Ny);
+  if (nc <= 0) return fail("no chunking", Nx, Ny, nc);
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, NL = 2 * Nx, NIT = KX + 2;
+  // lanes' reported columns
+  std::vector<int> cov(4 * Nx + 1, 0);
+  for (int j = 0; j < NL; ++j) {
+    const BtLane s = bt_lane(j, Nx);
+    if (s.len1 + s.len2 + (j == 0 ? KX : 1) != NIT) return fail("lane steps", j, s.len1, s.len2);
+    cov[s.f1 + 2 * Nx]++;
+    cov[s.f2 + 2 * Nx]++;
+    if (j == 0) cov[s.f3 + 2 * Nx]++;
+  }
+  for (int i = 0; i < 4 * Nx + 1; ++i)
+    if (cov[i] != 1) return fail("column cover", i - 2 * Nx, cov[i], 0);
+  std::map<std::tuple<int, int, int, int, int, int>, int> seen;  // (fy, fx, py, px, qy, qx)
+  long long off = 0;
+  for (int b = 0; b < (Ny + 1) * nc; ++b) {
+    const BandTask d = bt_task(b, Nx, Ny, nc);
+    if (d.toff != off) return fail("table offset", b, (int)d.toff, (int)off);
+    off += d.size;
+    if ((size_t)d.size * 8 > BT_TAB_BUDGET) return fail("chunk over budget", b, d.size, 0);
+    if (d.size % 2) return fail("odd chunk (16-byte copies)", b, d.size, 0);
+    std::vector<int> used(d.size, 0);
+    for (int l = 0; l < d.nfy; ++l) {
+      const int fy = d.fy[l];
+      if (fy < 0 || fy > 2 * Ny) return fail("band row", b, l, fy);
+      if (d.npy[l] < 0 || d.py0[l] < fy || d.py0[l] + d.npy[l] > KY) return fail("rows", b, l, d.py0[l]);
+      for (int j = 0; j < NL; ++j) {
+        const BtLane s = bt_lane(j, Nx);
+        for (int it = 0; it < NIT; ++it) {
+          int px, qx, seg;
+          bt_step(s, it, &px, &qx, &seg);
+          if (px < 0 || px >= KX || qx < 0 || qx >= KX) return fail("column range", j, it, px);
+          for (int r = 0; r < d.npy[l]; ++r) {
+            const int e = ((l ? NIT * d.npy[0] : 0) + it * d.npy[l] + r) * NL + j;
+            if (e < 0 || e >= d.size || used[e]++) return fail("table entry", b, e, d.size);
+          }
+          if (seg == 3 && j > 0) continue;  // idle step
+          const int f = seg == 1 ? s.f1 : seg == 2 ? s.f2 : s.f3;
+          if (px - qx != f) return fail("diagonal", j, it, f);
+          for (int r = 0; r < d.npy[l]; ++r) {
+            const int py = d.py0[l] + r, qy = py - fy;
+            if (qy < 0) return fail("q row", b, py, fy);
+            seen[std::make_tuple(fy, f, py, px, qy, qx)]++;
+          }
+        }
+      }
+    }
+    for (int e = 0; e < d.size; ++e)
+      if (used[e] != 1) return fail("table hole", b, e, used[e]);
+  }
+  if ((size_t)off != band_tcc_entries(Nx, Ny, nc)) return fail("table size", (int)off, 0, 0);
+  // every pair of every band entry once
+  size_t want = 0;
+  for (int fy = 0; fy <= 2 * Ny; ++fy)
+    for (int fx = -2 * Nx; fx <= 2 * Nx; ++fx)
+      for (int py = fy; py < KY; ++py)
+        for (int px = std::max(0, fx); px < KX + std::min(0, fx); ++px) {
+          ++want;
+          auto it = seen.find(std::make_tuple(fy, fx, py, px, py - fy, px - fx));
+          if (it == seen.end() || it->second != 1) return fail("pair", fy, fx, py * KX + px);
+        }
+  if (want != seen.size()) return fail("extra pairs", (int)want, (int)seen.size(), 0);
+  std::printf("ok %d %zu\n", nc, want);
+  return 0;
+}
+int main() {
+  int Nx, Ny;
+  while (std::scanf("%d %d", &Nx, &Ny) == 2)
+    if (check(Nx, Ny)) return 1;
+  return 0;
+}
+"""
+
+# (Nx, Ny): the metric's 1024^2 optics (8, 8), the 2048^2 class (16, 16), the small
+# configurations, rectangular windows and the edges of the supported range
+CASES = [(8, 8), (16, 16), (2, 2), (1, 0), (1, 1), (4, 7), (7, 4), (12, 12), (16, 3), (3, 16), (5, 5), (9, 13)]
+
+
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("band_sched")
+    src, exe = d / "drv.cpp", d / "drv"
+    src.write_text(DRIVER)
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", CSRC, str(src), "-o", str(exe)], check=True)
+    return str(exe)
+
+
+def test_schedule_visits_every_pair_once(driver):
+    inp = "".join(f"{nx} {ny}\n" for nx, ny in CASES)
+    r = subprocess.run([driver], input=inp, capture_output=True, text=True)
+    lines = r.stdout.split("\n")
+    assert r.returncode == 0, r.stdout
+    got = [ln.split() for ln in lines if ln]
+    assert len(got) == len(CASES)
+    for (nx, ny), g in zip(CASES, got):
+        assert g[0] == "ok"
+        kx, ky = 2 * nx + 1, 2 * ny + 1
+        # pairs with fy >= 0: sum over fy of (rows) x sum over fx of (diagonal length)
+        assert int(g[2]) == (ky * (ky + 1) // 2) * kx * kx, (nx, ny)
+
+
+def test_chunking_of_the_metric_optics(driver):
+    # a chunk's table shares shared memory with a window per image of every warp: at
+    # Nx = Ny = 8 a whole task fits (18 rows, one partial group), at Nx = Ny = 16 the
+    # tasks are cut into row chunks
+    r = subprocess.run([driver], input="8 8\n16 16\n", capture_output=True, text=True)
+    (a, b) = [ln.split() for ln in r.stdout.split("\n") if ln]
+    assert a[1] == "1"
+    assert 2 < int(b[1]) <= 16
