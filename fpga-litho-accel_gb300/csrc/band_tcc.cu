@@ -86,6 +86,8 @@ __global__ void win_sum_kernel(const float2* __restrict__ win_part, int nparts, 
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, KD = KX * KY;
   if (idx >= KDP) return;
+  // several images per thread: their partial loads are in flight together
+#pragma unroll 4
   for (int img = blockIdx.y; img < batch; img += gridDim.y) {
     float2 w = make_float2(0.f, 0.f);
     if (idx < KD) {
@@ -124,17 +126,30 @@ __device__ __forceinline__ void bt_term(float2 a, float2 b, float2 t, float2& ac
   acc.y = fmaf(ux, t.y, fmaf(uy, t.x, acc.y));
 }
 
-// The n rows of one column step (p, q and T rows kx, kx and nl apart), even rows into
-// e and odd rows into o: two independent FMA chains.
-__device__ __forceinline__ void bt_rows(const float2* pp, const float2* qq, const float2* tt, int n, int kx, int nl,
-                                        float2& e, float2& o) {
-  int r = 0;
-#pragma unroll 2
-  for (; r + 1 < n; r += 2) {
-    bt_term(pp[r * kx], qq[r * kx], tt[r * nl], e);
-    bt_term(pp[(r + 1) * kx], qq[(r + 1) * kx], tt[(r + 1) * nl], o);
+// The n rows of one column step (p, q and T rows KXS, KXS and NLS apart; 0: the runtime
+// kx, nl), even rows into e and odd rows into o: two independent FMA chains, four rows
+// per step of three base pointers so that every load has an immediate offset.
+template <int KXS, int NLS>
+__device__ __forceinline__ void bt_rows(const float2* p, const float2* q, const float2* t, int n, int kx_rt,
+                                        int nl_rt, float2& e, float2& o) {
+  const int kx = KXS > 0 ? KXS : kx_rt, nl = NLS > 0 ? NLS : nl_rt;
+  for (; n >= 4; n -= 4) {
+    bt_term(p[0], q[0], t[0], e);
+    bt_term(p[kx], q[kx], t[nl], o);
+    bt_term(p[2 * kx], q[2 * kx], t[2 * nl], e);
+    bt_term(p[3 * kx], q[3 * kx], t[3 * nl], o);
+    p += 4 * kx;
+    q += 4 * kx;
+    t += 4 * nl;
   }
-  if (r < n) bt_term(pp[r * kx], qq[r * kx], tt[r * nl], e);
+  if (n >= 2) {
+    bt_term(p[0], q[0], t[0], e);
+    bt_term(p[kx], q[kx], t[nl], o);
+    p += 2 * kx;
+    q += 2 * kx;
+    t += 2 * nl;
+  }
+  if (n & 1) bt_term(p[0], q[0], t[0], e);
 }
 
 __device__ __forceinline__ float2 bt_sum(float2 e, float2 o) { return make_float2(e.x + o.x, e.y + o.y); }
@@ -214,12 +229,12 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
       {
         const float2* pp = W + pyA * KX + px;
         const float2* qq = W + (pyA - fy0) * KX + qx;
-        bt_rows(pp, qq, sT + (size_t)it * np0 * NL + j, np0, KX, NL, a0, b0);
+        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, sT + (size_t)it * np0 * NL + j, np0, KX, NL, a0, b0);
       }
       {
         const float2* pp = W + pyB * KX + px;
         const float2* qq = W + (pyB - fy1) * KX + qx;
-        bt_rows(pp, qq, T1 + (size_t)it * np1 * NL + j, np1, KX, NL, a1, b1);
+        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, T1 + (size_t)it * np1 * NL + j, np1, KX, NL, a1, b1);
       }
     }
     if (live) {
@@ -272,7 +287,9 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
   const int KD = (2 * g.Nx + 1) * (2 * g.Ny + 1), KDP = (KD + 1) & ~1;
   {
     StageScope sc(ctx, LITHO_STAGE_SOCS, 2);
-    win_sum_kernel<<<dim3((KDP + 127) / 128, std::min(p.batch, 65535)), 128, 0, ctx->stream>>>(
+    const int bx = (KDP + 127) / 128;
+    const int by = std::max(1, std::min(65535, (p.batch + 3) / 4));  // about four images per thread
+    win_sum_kernel<<<dim3(bx, by), 128, 0, ctx->stream>>>(
         w.part, w.nparts, w.mskf_r, w.mskf_i, g.Fx, g.Fy, g.Nx, g.Ny, KDP, p.batch, wsum);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     int most = 0;
