@@ -21,6 +21,7 @@ constexpr int BT_MAX_CHUNKS = 16;
 struct BandTask {
   int nfy;                // 1 or 2 rows of the band
   int fy[2], py0[2], npy[2];
+  int st0, nst;           // the chunk's column steps [st0, st0 + nst)
   int group;
   long long toff;         // first T entry of the chunk
   int size;               // T entries of the chunk
@@ -28,27 +29,24 @@ struct BandTask {
 
 LITHO_HD inline int bt_rows(int Ny, int fy) { return 2 * Ny + 1 - fy; }
 
-// task-chunk b = t * nc + c: t < Ny pairs fy = t with 2Ny - t, t = Ny is alone;
-// chunk c of a row range of R rows is [R c / nc, R (c + 1) / nc)
+// task-chunk b = t * nc + c: t < Ny pairs fy = t with 2Ny - t, t = Ny is alone; a
+// task's rows are all of its band rows' window rows (py in [fy, 2Ny]), and chunk c takes
+// the column steps [S c / nc, S (c + 1) / nc) of the S = 2Nx + 3 (every chunk keeps whole
+// row loops; its partial band goes to group c)
 LITHO_HD inline BandTask bt_task_shape(int b, int Nx, int Ny, int nc) {
   BandTask d;
-  const int t = b / nc, c = b - t * nc;
+  const int t = b / nc, c = b - t * nc, S = 2 * Nx + 3;
   d.nfy = t < Ny ? 2 : 1;
   d.fy[0] = t;
   d.fy[1] = t < Ny ? 2 * Ny - t : -1;
   for (int l = 0; l < 2; ++l) {
-    if (l >= d.nfy) {
-      d.py0[l] = 0;
-      d.npy[l] = 0;
-      continue;
-    }
-    const int R = bt_rows(Ny, d.fy[l]);
-    const int r0 = R * c / nc, r1 = R * (c + 1) / nc;
-    d.py0[l] = d.fy[l] + r0;
-    d.npy[l] = r1 - r0;
+    d.py0[l] = l < d.nfy ? d.fy[l] : 0;
+    d.npy[l] = l < d.nfy ? bt_rows(Ny, d.fy[l]) : 0;
   }
+  d.st0 = S * c / nc;
+  d.nst = S * (c + 1) / nc - d.st0;
   d.group = c;
-  d.size = (d.npy[0] + d.npy[1]) * (2 * Nx + 3) * (2 * Nx);
+  d.size = (d.npy[0] + d.npy[1]) * d.nst * (2 * Nx);
   d.toff = 0;
   return d;
 }

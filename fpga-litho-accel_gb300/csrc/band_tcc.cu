@@ -51,14 +51,14 @@ __device__ __forceinline__ void cp_async_wait() {
 __global__ void band_tab_kernel(const float2* __restrict__ krn, const float* __restrict__ scales, int nk, int Nx,
                                 int Ny, int nc, float2* __restrict__ tab) {
   const BandTask d = bt_task(blockIdx.x, Nx, Ny, nc);
-  const int KX = 2 * Nx + 1, KD = KX * (2 * Ny + 1), NL = 2 * Nx, NIT = KX + 2;
+  const int KX = 2 * Nx + 1, KD = KX * (2 * Ny + 1), NL = 2 * Nx;
   for (int e = threadIdx.x; e < d.size; e += blockDim.x) {
     const int j = e % NL;
     int rest = e / NL;
-    const int l = rest >= NIT * d.npy[0] ? 1 : 0;
-    if (l == 1) rest -= NIT * d.npy[0];
+    const int l = rest >= d.nst * d.npy[0] ? 1 : 0;
+    if (l == 1) rest -= d.nst * d.npy[0];
     const int npy = l ? d.npy[1] : d.npy[0], py0 = l ? d.py0[1] : d.py0[0], fy = l ? d.fy[1] : d.fy[0];
-    const int it = rest / npy, r = rest - it * npy;
+    const int il = rest / npy, r = rest - il * npy, it = d.st0 + il;
     const BtLane s = bt_lane(j, Nx);
     int px, qx, seg;
     bt_step(s, it, &px, &qx, &seg);
@@ -167,15 +167,15 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
   extern __shared__ __align__(16) float2 bts[];
   const int Nx = NXC > 0 ? NXC : nx;
   const BandTask d = bt_task(blockIdx.x, Nx, Ny, nc);
-  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, BW = 4 * Nx + 1, NL = 2 * Nx, NIT = KX + 2;
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, BW = 4 * Nx + 1, NL = 2 * Nx;
   const int IPW = 32 / NL;
   const int tsz = d.size;                              // even: whole 16-byte pairs
   float2* sT = bts;                                   // [tsz]
-  float2* sW = bts + tsz;                             // [BT_WARPS][IPW][KDP]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float2* sW = bts + tsz;                             // [warps][IPW][KDP]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   {
     const float2* src = tab + d.toff;
-    for (int e = tid; e < tsz / 2; e += BT_THREADS) cp_async16(sT + 2 * e, src + 2 * e, 16);
+    for (int e = tid; e < tsz / 2; e += blockDim.x) cp_async16(sT + 2 * e, src + 2 * e, 16);
     cp_async_commit();
   }
   const bool active = lane < IPW * NL;
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
   float4* myW = reinterpret_cast<float4*>(sW + (size_t)warp * IPW * KDP);
   const float2* W = sW + (size_t)warp * IPW * KDP + (size_t)sub * KDP;
   const int h = KDP / 2, n4 = IPW * h;
-  const int istep = gridDim.y * BT_WARPS * IPW;
-  int ibase = (blockIdx.y * BT_WARPS + warp) * IPW;
+  const int istep = gridDim.y * nw * IPW;
+  int ibase = (blockIdx.y * nw + warp) * IPW;
   float4 pf[BT_PF];
 #pragma unroll
   for (int k = 0; k < BT_PF; ++k)
@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
   // task rows: l = 0 always, l = 1 for a pair
   const int fy0 = d.fy[0], np0 = d.npy[0], fy1 = d.fy[1], np1 = d.npy[1];
   const int pyA = d.py0[0], pyB = d.py0[1];
-  const float2* T1 = sT + (size_t)NIT * np0 * NL;
+  const int st0 = d.st0, st1 = d.st0 + d.nst;
+  const float2* T1 = sT + (size_t)d.nst * np0 * NL;
   cp_async_wait<0>();
   __syncthreads();
   for (; ibase < batch; ibase += istep) {
@@ -213,7 +214,7 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
     const bool live = active && img < batch;
     const float2 z = make_float2(0.f, 0.f);
     float2 a0 = z, b0 = z, a1 = z, b1 = z, s10 = z, s20 = z, s11 = z, s21 = z;  // a/b: even/odd rows
-    for (int it = 0; it < NIT; ++it) {
+    for (int it = st0; it < st1; ++it) {
       if (it == sw1) {
         s10 = bt_sum(a0, b0);
         s11 = bt_sum(a1, b1);
@@ -229,24 +230,40 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
       {
         const float2* pp = W + pyA * KX + px;
         const float2* qq = W + (pyA - fy0) * KX + qx;
-        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, sT + (size_t)it * np0 * NL + j, np0, KX, NL, a0, b0);
+        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, sT + (size_t)(it - st0) * np0 * NL + j, np0, KX, NL, a0, b0);
       }
       {
         const float2* pp = W + pyB * KX + px;
         const float2* qq = W + (pyB - fy1) * KX + qx;
-        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, T1 + (size_t)it * np1 * NL + j, np1, KX, NL, a1, b1);
+        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, T1 + (size_t)(it - st0) * np1 * NL + j, np1, KX, NL, a1, b1);
+      }
+    }
+    // the running sums belong to the segment of the chunk's last step (segments the chunk
+    // does not reach stay zero in its partial band)
+    float2 s30 = z, s31 = z;
+    {
+      const float2 e0 = bt_sum(a0, b0), e1 = bt_sum(a1, b1);
+      if (st1 <= sw1) {
+        s10 = e0;
+        s11 = e1;
+      } else if (st1 <= sw2) {
+        s20 = e0;
+        s21 = e1;
+      } else {
+        s30 = e0;
+        s31 = e1;
       }
     }
     if (live) {
       float2* out = band_part + (((size_t)img * nc + d.group) * KY + fy0) * BW + 2 * Nx;
       out[s.f1] = s10;
       out[s.f2] = s20;
-      if (j == 0) out[s.f3] = bt_sum(a0, b0);
+      if (j == 0) out[s.f3] = s30;
       if (d.nfy == 2) {
         out = band_part + (((size_t)img * nc + d.group) * KY + fy1) * BW + 2 * Nx;
         out[s.f1] = s11;
         out[s.f2] = s21;
-        if (j == 0) out[s.f3] = bt_sum(a1, b1);
+        if (j == 0) out[s.f3] = s31;
       }
     }
   }
@@ -296,7 +313,6 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
     const int ntc = (g.Ny + 1) * nc;
     for (int b = 0; b < ntc; ++b) most = std::max(most, bt_task_shape(b, g.Nx, g.Ny, nc).size);
     const int IPW = 32 / (2 * g.Nx);
-    const size_t smem = ((size_t)most + (size_t)BT_WARPS * IPW * KDP) * sizeof(float2);
     decltype(&band_tcc_kernel<0>) k;
     switch (g.Nx) {
       case 2: k = band_tcc_kernel<2>; break;
@@ -305,14 +321,24 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
       case 16: k = band_tcc_kernel<16>; break;
       default: k = band_tcc_kernel<0>; break;
     }
-    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto smem_for = [&](int nw) { return ((size_t)most + (size_t)nw * IPW * KDP) * sizeof(float2); };
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(BT_WARPS)));
+    // warps per CTA: the largest that still gives every SM a CTA (small batches take
+    // smaller CTAs, so that the tasks spread over the whole GPU)
+    const int sms = std::max(1, p.sms > 0 ? p.sms : ctx->sm_count);
+    int nw = 2;
+    for (int w = BT_WARPS; w >= 2; w /= 2)
+      if ((long long)ntc * ((p.batch + w * IPW - 1) / (w * IPW)) >= sms) {
+        nw = w;
+        break;
+      }
     int per_sm = 0;
-    LITHO_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, BT_THREADS, smem));
-    const int per_pass = BT_WARPS * IPW;
-    const int want = std::max(1, per_sm) * std::max(1, p.sms > 0 ? p.sms : ctx->sm_count);
-    const int groups = std::max(1, std::min((p.batch + per_pass - 1) / per_pass, (want + ntc - 1) / ntc));
-    k<<<dim3(ntc, groups), BT_THREADS, smem, ctx->stream>>>(ks->band_tab, wsum, KDP, g.Nx, g.Ny, nc, p.batch,
-                                                            band_part);
+    LITHO_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * nw, smem_for(nw)));
+    per_sm = std::max(1, per_sm);
+    const int per_pass = nw * IPW;
+    const int groups = std::max(1, std::min((p.batch + per_pass - 1) / per_pass, (per_sm * sms + ntc - 1) / ntc));
+    k<<<dim3(ntc, groups), 32 * nw, smem_for(nw), ctx->stream>>>(ks->band_tab, wsum, KDP, g.Nx, g.Ny, nc, p.batch,
+                                                                 band_part);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   return LITHO_OK;

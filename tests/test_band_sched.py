@@ -4,8 +4,8 @@ checked on the CPU.
 The band of an image is band(f) = sum_{p - q = f} W(p) conj(W(q)) T(p, q) over the
 (2Ny+1) x (2Nx+1) window, for the rows fy >= 0 the interpolation reads.  The kernel
 splits that sum into task-chunks (a pair of band rows fy, 2Ny - fy, or the row Ny
-alone, cut into row chunks that write separate partial groups) and, inside a chunk,
-into 2Nx lanes that each walk three column segments over every row of the chunk.
+alone, its column steps cut into chunks that write separate partial groups) and,
+inside a chunk, into 2Nx lanes that each walk their column segments over every row.
 The schedule must visit every pair (p, q) of every band entry exactly once, each lane's
 segments must lie on the diagonal px - qx of the band column it reports, the lanes'
 reported columns must cover -2Nx..2Nx once, the table entries of a chunk must be
@@ -56,14 +56,15 @@ static int check(int Nx, int Ny) {
       const int fy = d.fy[l];
       if (fy < 0 || fy > 2 * Ny) return fail("band row", b, l, fy);
       if (d.npy[l] < 0 || d.py0[l] < fy || d.py0[l] + d.npy[l] > KY) return fail("rows", b, l, d.py0[l]);
+      if (d.nst < 1 || d.st0 < 0 || d.st0 + d.nst > NIT) return fail("steps", b, d.st0, d.nst);
       for (int j = 0; j < NL; ++j) {
         const BtLane s = bt_lane(j, Nx);
-        for (int it = 0; it < NIT; ++it) {
+        for (int it = d.st0; it < d.st0 + d.nst; ++it) {
           int px, qx, seg;
           bt_step(s, it, &px, &qx, &seg);
           if (px < 0 || px >= KX || qx < 0 || qx >= KX) return fail("column range", j, it, px);
           for (int r = 0; r < d.npy[l]; ++r) {
-            const int e = ((l ? NIT * d.npy[0] : 0) + it * d.npy[l] + r) * NL + j;
+            const int e = ((l ? d.nst * d.npy[0] : 0) + (it - d.st0) * d.npy[l] + r) * NL + j;
             if (e < 0 || e >= d.size || used[e]++) return fail("table entry", b, e, d.size);
           }
           if (seg == 3 && j > 0) continue;  // idle step
@@ -135,8 +136,8 @@ def test_schedule_visits_every_pair_once(driver):
 
 def test_chunking_of_the_metric_optics(driver):
     # a chunk's table shares shared memory with a window per image of every warp: at
-    # Nx = Ny = 8 a whole task fits (18 rows, one partial group), at Nx = Ny = 16 the
-    # tasks are cut into row chunks
+    # Nx = Ny = 8 a whole task fits (one partial group), at Nx = Ny = 16 the tasks'
+    # column steps are cut into chunks
     r = subprocess.run([driver], input="8 8\n16 16\n", capture_output=True, text=True)
     (a, b) = [ln.split() for ln in r.stdout.split("\n") if ln]
     assert a[1] == "1"

@@ -38,6 +38,8 @@ def _cases():
         "256_annular_k8": (256, 256, ann, 8),
         # Nx = 6: the kernel without a compile-time support size; Fx = 1024 > Lx
         "768_annular_k10": (768, 768, ann, 10),
+        # Nx = 16: the table cut into column-step chunks (several partial groups)
+        "2048_annular_k12": (2048, 2048, ann, 12),
     }
 
 
@@ -46,8 +48,9 @@ def case(request):
     from litho_gb300 import synth
     Lx, Ly, src, K = _cases()[request.param]
     krn, scales, nx, ny = _kernels(src, Lx, Ly, K)
+    seeds = ((0.3, 11), (0.5, 12), (0.45, 13)) if Lx * Ly <= 1024 * 1024 else ((0.4, 14),)
     masks = np.stack([synth.density_rect_mask(max(Lx, Ly), d, seed=s)[:Ly, :Lx]
-                      for d, s in ((0.3, 11), (0.5, 12), (0.45, 13))]).astype(np.float32)
+                      for d, s in seeds]).astype(np.float32)
     masks = np.ascontiguousarray(masks)
     ref = [R.mask_to_image(m, krn, scales, nx, ny) for m in masks]
     return dict(name=request.param, krn=krn, scales=scales, nx=nx, ny=ny, masks=masks, ref=ref)
