@@ -724,13 +724,14 @@ __global__ void __launch_bounds__(S128_THREADS) socs128_kernel(
 // ---------------------------------------------------------------------------
 constexpr int FR_THREADS = 256, FR_COLS = 128, FR_ROWS = 2 * FR_COLS + 1;  // column, mirror, x' = 0
 
-template <int MAXD, bool KMAJ>
+template <int MAXD, bool KMAJ, int KPC>
 __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __restrict__ band_part, int ngroups,
                                                              const float2* __restrict__ twF, int Lx, int Fx,
-                                                             int Nx, int Ny, int KP, int batch,
+                                                             int Nx, int Ny, int kp_rt, int batch,
                                                              float* __restrict__ tm, float* __restrict__ tmh,
                                                              float* __restrict__ tml, float* __restrict__ t0) {
   extern __shared__ __align__(16) float4 frs[];
+  const int KP = KPC > 0 ? KPC : kp_rt;  // K-major row width (compile time where known)
   const int BH = 2 * Ny + 1, BW = 4 * Nx + 1, ND = 2 * Nx + 1;
   float4* sC = frs;                                       // [BH][MAXD]
   float* sO = reinterpret_cast<float*>(sC + BH * MAXD);  // K-major: [FR_ROWS][KP + 1]
@@ -760,8 +761,9 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
   for (int img = blockIdx.y; img < batch; img += gridDim.y) {
     __syncthreads();  // the previous image is out of sC and sO
     const float2* B = band_part + (size_t)img * ngroups * BH * BW;
-    for (int idx = tid; idx < BH * ND; idx += FR_THREADS) {
-      const int fy = idx / ND, d = idx - fy * ND;
+    for (int idx = tid; idx < BH * MAXD; idx += FR_THREADS) {
+      const int fy = idx / MAXD, d = idx - fy * MAXD;  // MAXD: a compile-time divisor
+      if (d >= ND) continue;
       const float2* S = B + fy * BW + 2 * Nx;
       const float2 pv = sum_strided(S + d, pst, ngroups);
       if (d == 0) {
@@ -872,13 +874,13 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
   }
 }
 
-template <int MAXD, bool KMAJ>
+template <int MAXD, bool KMAJ, int KPC = 0>
 static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const float2* band_part, const float2* twF,
                                     int KP, float* tm, float* tmh, float* tml, float* t0) {
   const ImgGeom& g = p.g;
   const size_t smem = (size_t)(2 * g.Ny + 1) * MAXD * sizeof(float4) +
                       (KMAJ ? (size_t)FR_ROWS * (KP + 1) * sizeof(float) : 0);
-  auto k = fi_rows_kernel<MAXD, KMAJ>;
+  auto k = fi_rows_kernel<MAXD, KMAJ, KPC>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // column blocks over the x' < 0 half; enough image groups for a few CTAs per SM,
@@ -896,6 +898,12 @@ cudaError_t launch_fi_rows(cudaStream_t s, const ImgPlan& p, const float2* band_
                            float* tm, float* tmh, float* tml, float* t0) {
   const int ND = 2 * p.g.Nx + 1;
   const bool km = tmh != nullptr;
+  if (km && KP == 32) {  // the K-major width of Ny <= 8 at compile time
+    if (ND <= 5) return launch_fi_rows_t<5, true, 32>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+    if (ND <= 9) return launch_fi_rows_t<9, true, 32>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+    if (ND <= 17) return launch_fi_rows_t<17, true, 32>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+    return launch_fi_rows_t<33, true, 32>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
+  }
   if (ND <= 5) return km ? launch_fi_rows_t<5, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
                          : launch_fi_rows_t<5, false>(s, p, band_part, twF, KP, tm, tmh, tml, t0);
   if (ND <= 9) return km ? launch_fi_rows_t<9, true>(s, p, band_part, twF, KP, tm, tmh, tml, t0)
