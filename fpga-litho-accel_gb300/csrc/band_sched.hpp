@@ -1,6 +1,14 @@
 // Work schedule of the TCC band kernel (band_tcc.cu): task-chunks over the band rows,
-// the three column segments of every lane, and the table sizes.  Plain C++ (host and
-// device), so the schedule is also checked on the CPU.
+// the column slots of every lane, and the table sizes.  Plain C++ (host and device),
+// so the schedule is also checked on the CPU.
+//
+// For one band row fy, the pairs (p, q) with p - q = (fy, fx) are, for every window row
+// py in [fy, 2Ny] (q row py - fy), the pairs of columns (px, qx) with px - qx = fx.  Lane
+// j of an image (2Nx lanes) owns the p column px = j: in slot s < 2Nx+1 it takes q column
+// qx = s (band column j - s).  The last p column, px = 2Nx, is shared out: in slot 2Nx+1
+// lane j takes (2Nx, j) (band column 2Nx - j), and in slot 2Nx+2 lane 0 takes (2Nx, 2Nx)
+// (band column 0; the other lanes idle there).  So every lane runs the same 2Nx+3 slots
+// per window row, with its p value fixed along them.
 #pragma once
 #include <algorithm>
 #include <cstddef>
@@ -21,32 +29,34 @@ constexpr int BT_MAX_CHUNKS = 16;
 struct BandTask {
   int nfy;                // 1 or 2 rows of the band
   int fy[2], py0[2], npy[2];
-  int st0, nst;           // the chunk's column steps [st0, st0 + nst)
   int group;
   long long toff;         // first T entry of the chunk
   int size;               // T entries of the chunk
 };
 
 LITHO_HD inline int bt_rows(int Ny, int fy) { return 2 * Ny + 1 - fy; }
+LITHO_HD inline int bt_slots(int Nx) { return 2 * Nx + 3; }
 
-// task-chunk b = t * nc + c: t < Ny pairs fy = t with 2Ny - t, t = Ny is alone; a
-// task's rows are all of its band rows' window rows (py in [fy, 2Ny]), and chunk c takes
-// the column steps [S c / nc, S (c + 1) / nc) of the S = 2Nx + 3 (every chunk keeps whole
-// row loops; its partial band goes to group c)
+// task-chunk b = t * nc + c: t < Ny pairs fy = t with 2Ny - t, t = Ny is alone; chunk c
+// takes the window rows [R c / nc, R (c + 1) / nc) of the task's R = rows(fy0) + rows(fy1)
+// (fy0's rows first); its partial band goes to group c
 LITHO_HD inline BandTask bt_task_shape(int b, int Nx, int Ny, int nc) {
   BandTask d;
-  const int t = b / nc, c = b - t * nc, S = 2 * Nx + 3;
+  const int t = b / nc, c = b - t * nc;
   d.nfy = t < Ny ? 2 : 1;
   d.fy[0] = t;
   d.fy[1] = t < Ny ? 2 * Ny - t : -1;
-  for (int l = 0; l < 2; ++l) {
-    d.py0[l] = l < d.nfy ? d.fy[l] : 0;
-    d.npy[l] = l < d.nfy ? bt_rows(Ny, d.fy[l]) : 0;
-  }
-  d.st0 = S * c / nc;
-  d.nst = S * (c + 1) / nc - d.st0;
+  const int R0 = bt_rows(Ny, d.fy[0]), R1 = d.nfy == 2 ? bt_rows(Ny, d.fy[1]) : 0, R = R0 + R1;
+  const int r0 = R * c / nc, r1 = R * (c + 1) / nc;
+  // rows [r0, r1) of the concatenation: fy0's part, then fy1's
+  const int a0 = r0 < R0 ? r0 : R0, b0 = r1 < R0 ? r1 : R0;
+  const int a1 = (r0 > R0 ? r0 : R0) - R0, b1 = (r1 > R0 ? r1 : R0) - R0;
+  d.py0[0] = d.fy[0] + a0;
+  d.npy[0] = b0 - a0;
+  d.py0[1] = d.nfy == 2 ? d.fy[1] + a1 : 0;
+  d.npy[1] = d.nfy == 2 ? b1 - a1 : 0;
   d.group = c;
-  d.size = (d.npy[0] + d.npy[1]) * d.nst * (2 * Nx);
+  d.size = (d.npy[0] + d.npy[1]) * bt_slots(Nx) * (2 * Nx);
   d.toff = 0;
   return d;
 }
@@ -59,40 +69,24 @@ LITHO_HD inline BandTask bt_task(int b, int Nx, int Ny, int nc) {
   return d;
 }
 
-// Lane j's three segments (length, start column of p, start column of q, band column):
-// see the header.  Segment 3 of lanes j >= 1 is an idle step (its T entries are zero).
-struct BtLane {
-  int len1, len2;
-  int p1, q1, p2, q2, p3, q3;
-  int f1, f2, f3;  // band columns fx; f3 < -2Nx: none
-};
-
-LITHO_HD inline BtLane bt_lane(int j, int Nx) {
-  BtLane s;
+// Slot s of lane j: the p and q columns, and whether the slot carries a pair (in the
+// last slot lane 0 alone does).  Its band column is px - qx.
+LITHO_HD inline bool bt_slot(int j, int s, int Nx, int* px, int* qx) {
   const int KX = 2 * Nx + 1;
-  if (j == 0) {
-    s.len1 = 1; s.p1 = 2 * Nx; s.q1 = 0; s.f1 = 2 * Nx;
-    s.len2 = 1; s.p2 = 0; s.q2 = 2 * Nx; s.f2 = -2 * Nx;
-    s.p3 = 0; s.q3 = 0; s.f3 = 0;
-  } else {
-    s.len1 = KX - j; s.p1 = j; s.q1 = 0; s.f1 = j;
-    s.len2 = j + 1; s.p2 = 0; s.q2 = 2 * Nx - j; s.f2 = j - 2 * Nx;
-    s.p3 = 0; s.q3 = 0; s.f3 = -(1 << 20);
+  if (s < KX) {
+    *px = j;
+    *qx = s;
+    return true;
   }
-  return s;
+  *px = 2 * Nx;
+  *qx = s == KX ? j : 2 * Nx;
+  return s == KX || j == 0;
 }
 
-// column step it of lane s: (px, qx, segment 1..3)
-LITHO_HD inline void bt_step(const BtLane& s, int it, int* px, int* qx, int* seg) {
-  if (it < s.len1) {
-    *px = s.p1 + it; *qx = s.q1 + it; *seg = 1;
-  } else if (it < s.len1 + s.len2) {
-    const int k = it - s.len1;
-    *px = s.p2 + k; *qx = s.q2 + k; *seg = 2;
-  } else {
-    const int k = it - s.len1 - s.len2;
-    *px = s.p3 + k; *qx = s.q3 + k; *seg = 3;
-  }
+// T entry of (band row l of the task, row r of the chunk's rows of l, slot s, lane j)
+LITHO_HD inline int bt_entry(const BandTask& d, int l, int r, int s, int j, int Nx) {
+  const int NS = bt_slots(Nx), NL = 2 * Nx;
+  return ((l ? d.npy[0] : 0) + r) * NS * NL + s * NL + j;
 }
 
 inline int band_tcc_chunks(int Nx, int Ny) {

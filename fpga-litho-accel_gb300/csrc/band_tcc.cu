@@ -12,20 +12,16 @@
 // sum over the window's pairs (p, q) with fy >= 0 -- ~44K products at Nx = Ny = 8
 // instead of K inverse 2-D FFTs, |E|^2 and one forward FFT.
 //
-// Work layout.  For a row f = (fy, fx) of the band, the pairs are, for each window
-// row py in [fy, 2Ny] (q row py - fy), the diagonal px - qx = fx of the 2Nx+1
-// columns: 2Nx+1 - |fx| terms.  The 4Nx+1 diagonals of one row pair split into 2Nx
-// lanes of 2Nx+2 or 2Nx+3 terms each: lane j >= 1 takes fx = j then fx = j - 2Nx
-// (lengths 2Nx+1-j and j+1) and one idle step; lane 0 takes fx = 2Nx, fx = -2Nx
-// (one term each) and fx = 0 (2Nx+1 terms).  So every lane runs the same 2Nx+3
-// column steps, each over all rows py of its fy, and its accumulator is saved and
-// cleared at two lane-specific steps.  Rows fy and 2Ny - fy pair into one task of
-// 2Ny+2 rows (fy = Ny alone has Ny+1); a task's rows may be cut into chunks, whose
-// partial bands go to separate groups (summed by the interpolation in order).
-// T is stored per task-chunk in exactly the order a lane consumes it
-// ([fy of the task][column step][row][lane]), so that a CTA holds its chunk in
-// shared memory and every warp streams it while imaging its own images: 2Nx lanes
-// per image, 32 / (2Nx) images per warp.
+// Work layout (band_sched.hpp).  Rows fy and 2Ny - fy pair into one task of 2Ny+2 window
+// rows (fy = Ny alone has Ny+1); a task's rows may be cut into chunks whose partial bands
+// go to separate groups (summed by the interpolation in order).  Within a window row, lane
+// j of an image owns the p column j and walks the q columns (plus a share of the last p
+// column): its p value stays in a register, every q value is one load broadcast to the
+// image's lanes, and its 2Nx+1 running sums (one per q column, band column j - qx) are
+// summed along the band diagonals through shared memory once per band row.  T is stored
+// per task-chunk in the order the lanes consume it ([row][slot][lane]), so that a CTA
+// holds its chunk in shared memory and every warp streams it while imaging its own
+// images: 2Nx lanes per image, 32 / (2Nx) images per warp.
 #include "litho_internal.cuh"
 #include "band_sched.hpp"
 
@@ -47,23 +43,18 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // T entries of task-chunk blockIdx.x in consumption order, accumulated in FP64 over
-// the kernels in order and rounded once.
+// the kernels in order and rounded once; zero for idle slots.
 __global__ void band_tab_kernel(const float2* __restrict__ krn, const float* __restrict__ scales, int nk, int Nx,
                                 int Ny, int nc, float2* __restrict__ tab) {
   const BandTask d = bt_task(blockIdx.x, Nx, Ny, nc);
-  const int KX = 2 * Nx + 1, KD = KX * (2 * Ny + 1), NL = 2 * Nx;
+  const int KX = 2 * Nx + 1, KD = KX * (2 * Ny + 1), NL = 2 * Nx, NS = bt_slots(Nx);
   for (int e = threadIdx.x; e < d.size; e += blockDim.x) {
-    const int j = e % NL;
-    int rest = e / NL;
-    const int l = rest >= d.nst * d.npy[0] ? 1 : 0;
-    if (l == 1) rest -= d.nst * d.npy[0];
-    const int npy = l ? d.npy[1] : d.npy[0], py0 = l ? d.py0[1] : d.py0[0], fy = l ? d.fy[1] : d.fy[0];
-    const int il = rest / npy, r = rest - il * npy, it = d.st0 + il;
-    const BtLane s = bt_lane(j, Nx);
-    int px, qx, seg;
-    bt_step(s, it, &px, &qx, &seg);
+    const int j = e % NL, rest = e / NL, sl = rest % NS, rr = rest / NS;
+    const int l = rr >= d.npy[0] ? 1 : 0, r = rr - (l ? d.npy[0] : 0);
+    const int py0 = l ? d.py0[1] : d.py0[0], fy = l ? d.fy[1] : d.fy[0];
+    int px, qx;
     double tr = 0.0, ti = 0.0;
-    if (!(seg == 3 && j > 0)) {
+    if (bt_slot(j, sl, Nx, &px, &qx)) {
       const int py = py0 + r, qy = py - fy;
       for (int k = 0; k < nk; ++k) {
         const float2 a = krn[(size_t)k * KD + py * KX + px], b = krn[(size_t)k * KD + qy * KX + qx];
@@ -108,10 +99,8 @@ __global__ void win_sum_kernel(const float2* __restrict__ win_part, int nparts, 
   }
 }
 
-// Per-lane register staging of a warp's windows (16-byte pieces): up to BT_PF pieces per
+// Per-lane register staging of a warp's windows (16-byte pieces): up to PF pieces per
 // lane are loaded one pass ahead; the rest of a larger window set is loaded when stored.
-constexpr int BT_PF = 10;
-
 __device__ __forceinline__ float4 bt_window_piece(const float2* __restrict__ wsum, int ibase, int e, int h,
                                                   int batch) {
   const int si = e / h, img = ibase + si;
@@ -119,60 +108,37 @@ __device__ __forceinline__ float4 bt_window_piece(const float2* __restrict__ wsu
   return *reinterpret_cast<const float4*>(wsum + (size_t)img * 2 * h + 2 * (e - si * h));
 }
 
-// acc += (a conj(b)) t for one row of a column step
+// acc += (a conj(b)) t
 __device__ __forceinline__ void bt_term(float2 a, float2 b, float2 t, float2& acc) {
   const float ux = fmaf(a.x, b.x, a.y * b.y), uy = fmaf(a.y, b.x, -a.x * b.y);
   acc.x = fmaf(ux, t.x, fmaf(-uy, t.y, acc.x));
   acc.y = fmaf(ux, t.y, fmaf(uy, t.x, acc.y));
 }
 
-// The n rows of one column step (p, q and T rows KXS, KXS and NLS apart; 0: the runtime
-// kx, nl), even rows into e and odd rows into o: two independent FMA chains, four rows
-// per step of three base pointers so that every load has an immediate offset.
-template <int KXS, int NLS>
-__device__ __forceinline__ void bt_rows(const float2* p, const float2* q, const float2* t, int n, int kx_rt,
-                                        int nl_rt, float2& e, float2& o) {
-  const int kx = KXS > 0 ? KXS : kx_rt, nl = NLS > 0 ? NLS : nl_rt;
-  for (; n >= 4; n -= 4) {
-    bt_term(p[0], q[0], t[0], e);
-    bt_term(p[kx], q[kx], t[nl], o);
-    bt_term(p[2 * kx], q[2 * kx], t[2 * nl], e);
-    bt_term(p[3 * kx], q[3 * kx], t[3 * nl], o);
-    p += 4 * kx;
-    q += 4 * kx;
-    t += 4 * nl;
-  }
-  if (n >= 2) {
-    bt_term(p[0], q[0], t[0], e);
-    bt_term(p[kx], q[kx], t[nl], o);
-    p += 2 * kx;
-    q += 2 * kx;
-    t += 2 * nl;
-  }
-  if (n & 1) bt_term(p[0], q[0], t[0], e);
-}
+__device__ __forceinline__ float2 bt_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 
-__device__ __forceinline__ float2 bt_sum(float2 e, float2 o) { return make_float2(e.x + o.x, e.y + o.y); }
-
-// One CTA per (task-chunk, image group): its T chunk in shared memory, each warp
-// imaging 32 / (2Nx) images at a time (2Nx lanes each) from its own window copies,
-// the next images' windows in flight in registers meanwhile.  Every column step of a
-// lane runs over all rows of both band rows of the task (two accumulator sets).
-// NXC > 0 fixes Nx at compile time (row strides become immediates); 0 reads nx.
+// One CTA per (task-chunk, image group): its T chunk in shared memory, each warp imaging
+// 32 / (2Nx) images at a time (2Nx lanes each) from its own window copies, the next images'
+// windows in flight in registers meanwhile.  Lane j owns p column j of every window row
+// (band_sched.hpp): per row its p value and the shared last-column value are two loads,
+// then 2Nx+3 slots of one broadcast q load, one T load and eight FP32 operations each.
+// Per band row the lanes' running sums (slot s: band column j - s) are added along the
+// band diagonals by shuffles within the image's lanes, in a fixed order: for the band
+// column j - c of lane j, round k takes slot k + c of lane j + k (the same register in
+// every lane).
 template <int NXC>
 __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* __restrict__ tab,
-                                                              const float2* __restrict__ wsum, int KDP, int nx,
-                                                              int Ny, int nc, int batch,
-                                                              float2* __restrict__ band_part) {
+                                                                 const float2* __restrict__ wsum, int KDP, int Ny,
+                                                                 int nc, int batch, float2* __restrict__ band_part) {
+  constexpr int Nx = NXC, KX = 2 * Nx + 1, NL = 2 * Nx, NS = KX + 2, BW = 4 * Nx + 1, IPW = 32 / NL;
+  constexpr int PF = Nx <= 8 ? 10 : 4;  // window pieces prefetched per lane
   extern __shared__ __align__(16) float2 bts[];
-  const int Nx = NXC > 0 ? NXC : nx;
   const BandTask d = bt_task(blockIdx.x, Nx, Ny, nc);
-  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, BW = 4 * Nx + 1, NL = 2 * Nx;
-  const int IPW = 32 / NL;
+  const int KY = 2 * Ny + 1;
   const int tsz = d.size;                              // even: whole 16-byte pairs
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   float2* sT = bts;                                   // [tsz]
   float2* sW = bts + tsz;                             // [warps][IPW][KDP]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   {
     const float2* src = tab + d.toff;
     for (int e = tid; e < tsz / 2; e += blockDim.x) cp_async16(sT + 2 * e, src + 2 * e, 16);
@@ -180,92 +146,102 @@ __global__ void __launch_bounds__(BT_THREADS, 2) band_tcc_kernel(const float2* _
   }
   const bool active = lane < IPW * NL;
   const int sub = active ? lane / NL : 0, j = active ? lane - sub * NL : lane % NL;
-  const BtLane s = bt_lane(j, Nx);
-  const int sw1 = s.len1, sw2 = s.len1 + s.len2;
   float4* myW = reinterpret_cast<float4*>(sW + (size_t)warp * IPW * KDP);
   const float2* W = sW + (size_t)warp * IPW * KDP + (size_t)sub * KDP;
   const int h = KDP / 2, n4 = IPW * h;
   const int istep = gridDim.y * nw * IPW;
   int ibase = (blockIdx.y * nw + warp) * IPW;
-  float4 pf[BT_PF];
+  float4 pf[PF];
 #pragma unroll
-  for (int k = 0; k < BT_PF; ++k)
+  for (int k = 0; k < PF; ++k)
     pf[k] = (lane + 32 * k < n4 && ibase < batch) ? bt_window_piece(wsum, ibase, lane + 32 * k, h, batch)
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
-  // task rows: l = 0 always, l = 1 for a pair
-  const int fy0 = d.fy[0], np0 = d.npy[0], fy1 = d.fy[1], np1 = d.npy[1];
-  const int pyA = d.py0[0], pyB = d.py0[1];
-  const int st0 = d.st0, st1 = d.st0 + d.nst;
-  const float2* T1 = sT + (size_t)d.nst * np0 * NL;
   cp_async_wait<0>();
   __syncthreads();
   for (; ibase < batch; ibase += istep) {
     __syncwarp();  // the previous images' windows are no longer read
 #pragma unroll
-    for (int k = 0; k < BT_PF; ++k)
+    for (int k = 0; k < PF; ++k)
       if (lane + 32 * k < n4) myW[lane + 32 * k] = pf[k];
-    for (int e = lane + 32 * BT_PF; e < n4; e += 32) myW[e] = bt_window_piece(wsum, ibase, e, h, batch);
+    for (int e = lane + 32 * PF; e < n4; e += 32) myW[e] = bt_window_piece(wsum, ibase, e, h, batch);
     __syncwarp();
     const int inext = ibase + istep;
 #pragma unroll
-    for (int k = 0; k < BT_PF; ++k)
+    for (int k = 0; k < PF; ++k)
       if (lane + 32 * k < n4 && inext < batch) pf[k] = bt_window_piece(wsum, inext, lane + 32 * k, h, batch);
     const int img = ibase + sub;
     const bool live = active && img < batch;
-    const float2 z = make_float2(0.f, 0.f);
-    float2 a0 = z, b0 = z, a1 = z, b1 = z, s10 = z, s20 = z, s11 = z, s21 = z;  // a/b: even/odd rows
-    for (int it = st0; it < st1; ++it) {
-      if (it == sw1) {
-        s10 = bt_sum(a0, b0);
-        s11 = bt_sum(a1, b1);
-        a0 = b0 = a1 = b1 = z;
+#pragma unroll 1
+    for (int l = 0; l < d.nfy; ++l) {
+      const int fy = l ? d.fy[1] : d.fy[0], np = l ? d.npy[1] : d.npy[0], py0 = l ? d.py0[1] : d.py0[0];
+      float2 acc[KX];
+#pragma unroll
+      for (int k = 0; k < KX; ++k) acc[k] = make_float2(0.f, 0.f);
+      float2 e1 = make_float2(0.f, 0.f), e2 = e1;
+      const float2* tt = sT + (size_t)bt_entry(d, l, 0, 0, j, Nx);
+#pragma unroll 1
+      for (int r = 0; r < np; ++r, tt += NS * NL) {
+        const int py = py0 + r, qy = py - fy;
+        const float2* wq = W + qy * KX;
+        const float2 wp = W[py * KX + j], wl = W[py * KX + 2 * Nx];
+#pragma unroll
+        for (int sl = 0; sl < KX; ++sl) bt_term(wp, wq[sl], tt[sl * NL], acc[sl]);
+        bt_term(wl, wq[j], tt[KX * NL], e1);
+        bt_term(wl, wq[2 * Nx], tt[(KX + 1) * NL], e2);  // T is zero here but for lane 0
       }
-      if (it == sw2) {
-        s20 = bt_sum(a0, b0);
-        s21 = bt_sum(a1, b1);
-        a0 = b0 = a1 = b1 = z;
+      // band column f: the sum over lanes j' of acc_j'[j' - f], plus the last column's terms
+      const unsigned full = 0xffffffffu;
+      const int base = lane - j;  // this image's first lane (2Nx need not be a power of two)
+      auto from = [&](float2 v, int src) {
+        return make_float2(__shfl_sync(full, v.x, src), __shfl_sync(full, v.y, src));
+      };
+      float2 vneg = acc[2 * Nx], vpos = make_float2(0.f, 0.f), vz = acc[0];
+#pragma unroll
+      for (int k = 1; k <= 2 * Nx; ++k) {  // f = j - 2Nx: lanes j - k, slot 2Nx - k
+        const float2 v = from(acc[2 * Nx - k], j >= k ? lane - k : lane);
+        if (j >= k) vneg = bt_add(vneg, v);
       }
-      int px, qx, seg;
-      bt_step(s, it, &px, &qx, &seg);
-      {
-        const float2* pp = W + pyA * KX + px;
-        const float2* qq = W + (pyA - fy0) * KX + qx;
-        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, sT + (size_t)(it - st0) * np0 * NL + j, np0, KX, NL, a0, b0);
+#pragma unroll
+      for (int k = 1; k < NL; ++k) {  // f = j + 1: lanes j + k, slot k - 1; f = 0 (lane 0): slot k
+        const int src = j + k < NL ? lane + k : lane;
+        const float2 v = from(acc[k - 1], src), w = from(acc[k], src);
+        if (j + k < NL) {
+          vpos = bt_add(vpos, v);
+          vz = bt_add(vz, w);
+        }
       }
-      {
-        const float2* pp = W + pyB * KX + px;
-        const float2* qq = W + (pyB - fy1) * KX + qx;
-        bt_rows<NXC ? 2 * NXC + 1 : 0, 2 * NXC>(pp, qq, T1 + (size_t)(it - st0) * np1 * NL + j, np1, KX, NL, a1, b1);
-      }
-    }
-    // the running sums belong to the segment of the chunk's last step (segments the chunk
-    // does not reach stay zero in its partial band)
-    float2 s30 = z, s31 = z;
-    {
-      const float2 e0 = bt_sum(a0, b0), e1 = bt_sum(a1, b1);
-      if (st1 <= sw1) {
-        s10 = e0;
-        s11 = e1;
-      } else if (st1 <= sw2) {
-        s20 = e0;
-        s21 = e1;
-      } else {
-        s30 = e0;
-        s31 = e1;
-      }
-    }
-    if (live) {
-      float2* out = band_part + (((size_t)img * nc + d.group) * KY + fy0) * BW + 2 * Nx;
-      out[s.f1] = s10;
-      out[s.f2] = s20;
-      if (j == 0) out[s.f3] = s30;
-      if (d.nfy == 2) {
-        out = band_part + (((size_t)img * nc + d.group) * KY + fy1) * BW + 2 * Nx;
-        out[s.f1] = s11;
-        out[s.f2] = s21;
-        if (j == 0) out[s.f3] = s31;
+      // (2Nx, qx) of lane qx is band column 2Nx - qx: lane j takes lane 2Nx - 1 - j's
+      const float2 ex = from(e1, base + NL - 1 - j);
+      if (live) {
+        float2* out = band_part + (((size_t)img * nc + d.group) * KY + fy) * BW + 2 * Nx;
+        out[j - 2 * Nx] = vneg;
+        out[j + 1] = bt_add(vpos, ex);
+        if (j == 0) out[0] = bt_add(vz, e2);
       }
     }
+  }
+}
+
+// the band kernel for a support half-width 1 <= Nx <= 16 (compile-time row strides and
+// register arrays)
+static decltype(&band_tcc_kernel<1>) band_kernel_for(int Nx) {
+  switch (Nx) {
+    case 1: return band_tcc_kernel<1>;
+    case 2: return band_tcc_kernel<2>;
+    case 3: return band_tcc_kernel<3>;
+    case 4: return band_tcc_kernel<4>;
+    case 5: return band_tcc_kernel<5>;
+    case 6: return band_tcc_kernel<6>;
+    case 7: return band_tcc_kernel<7>;
+    case 8: return band_tcc_kernel<8>;
+    case 9: return band_tcc_kernel<9>;
+    case 10: return band_tcc_kernel<10>;
+    case 11: return band_tcc_kernel<11>;
+    case 12: return band_tcc_kernel<12>;
+    case 13: return band_tcc_kernel<13>;
+    case 14: return band_tcc_kernel<14>;
+    case 15: return band_tcc_kernel<15>;
+    default: return band_tcc_kernel<16>;
   }
 }
 
@@ -313,14 +289,7 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
     const int ntc = (g.Ny + 1) * nc;
     for (int b = 0; b < ntc; ++b) most = std::max(most, bt_task_shape(b, g.Nx, g.Ny, nc).size);
     const int IPW = 32 / (2 * g.Nx);
-    decltype(&band_tcc_kernel<0>) k;
-    switch (g.Nx) {
-      case 2: k = band_tcc_kernel<2>; break;
-      case 4: k = band_tcc_kernel<4>; break;
-      case 8: k = band_tcc_kernel<8>; break;
-      case 16: k = band_tcc_kernel<16>; break;
-      default: k = band_tcc_kernel<0>; break;
-    }
+    decltype(&band_tcc_kernel<1>) k = band_kernel_for(g.Nx);
     auto smem_for = [&](int nw) { return ((size_t)most + (size_t)nw * IPW * KDP) * sizeof(float2); };
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(BT_WARPS)));
     // warps per CTA: the largest that still gives every SM a CTA (small batches take
@@ -337,7 +306,7 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
     per_sm = std::max(1, per_sm);
     const int per_pass = nw * IPW;
     const int groups = std::max(1, std::min((p.batch + per_pass - 1) / per_pass, (per_sm * sms + ntc - 1) / ntc));
-    k<<<dim3(ntc, groups), 32 * nw, smem_for(nw), ctx->stream>>>(ks->band_tab, wsum, KDP, g.Nx, g.Ny, nc, p.batch,
+    k<<<dim3(ntc, groups), 32 * nw, smem_for(nw), ctx->stream>>>(ks->band_tab, wsum, KDP, g.Ny, nc, p.batch,
                                                                  band_part);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }

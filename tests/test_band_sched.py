@@ -4,12 +4,12 @@ checked on the CPU.
 The band of an image is band(f) = sum_{p - q = f} W(p) conj(W(q)) T(p, q) over the
 (2Ny+1) x (2Nx+1) window, for the rows fy >= 0 the interpolation reads.  The kernel
 splits that sum into task-chunks (a pair of band rows fy, 2Ny - fy, or the row Ny
-alone, its column steps cut into chunks that write separate partial groups) and,
-inside a chunk, into 2Nx lanes that each walk their column segments over every row.
-The schedule must visit every pair (p, q) of every band entry exactly once, each lane's
-segments must lie on the diagonal px - qx of the band column it reports, the lanes'
-reported columns must cover -2Nx..2Nx once, the table entries of a chunk must be
-addressed once each, and a chunk's table must fit the kernel's shared-memory budget.
+alone, its window rows cut into chunks that write separate partial groups) and, inside
+a chunk, into 2Nx lanes that each own a p column and walk the q columns (plus a share of
+the last p column).  The schedule must visit every pair (p, q) of every band entry
+exactly once, cover every window row of every band row once over the chunks, address
+every table entry of a chunk once, and fit a chunk's table in the kernel's
+shared-memory budget.
 """
 import os
 import shutil
@@ -31,19 +31,9 @@ static int fail(const char* m, int a, int b, int c) { std::printf("fail %s %d %d
 static int check(int Nx, int Ny) {
   const int nc = band_tcc_chunks(Nx, Ny);
   if (nc <= 0) return fail("no chunking", Nx, Ny, nc);
-  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, NL = 2 * Nx, NIT = KX + 2;
-  // lanes' reported columns
-  std::vector<int> cov(4 * Nx + 1, 0);
-  for (int j = 0; j < NL; ++j) {
-    const BtLane s = bt_lane(j, Nx);
-    if (s.len1 + s.len2 + (j == 0 ? KX : 1) != NIT) return fail("lane steps", j, s.len1, s.len2);
-    cov[s.f1 + 2 * Nx]++;
-    cov[s.f2 + 2 * Nx]++;
-    if (j == 0) cov[s.f3 + 2 * Nx]++;
-  }
-  for (int i = 0; i < 4 * Nx + 1; ++i)
-    if (cov[i] != 1) return fail("column cover", i - 2 * Nx, cov[i], 0);
+  const int KX = 2 * Nx + 1, KY = 2 * Ny + 1, NL = 2 * Nx, NS = bt_slots(Nx);
   std::map<std::tuple<int, int, int, int, int, int>, int> seen;  // (fy, fx, py, px, qy, qx)
+  std::vector<int> rows_seen(KY * KY, 0);                        // (fy, py) covered once over chunks
   long long off = 0;
   for (int b = 0; b < (Ny + 1) * nc; ++b) {
     const BandTask d = bt_task(b, Nx, Ny, nc);
@@ -51,37 +41,33 @@ static int check(int Nx, int Ny) {
     off += d.size;
     if ((size_t)d.size * 8 > BT_TAB_BUDGET) return fail("chunk over budget", b, d.size, 0);
     if (d.size % 2) return fail("odd chunk (16-byte copies)", b, d.size, 0);
+    if (d.group != b % nc) return fail("group", b, d.group, 0);
     std::vector<int> used(d.size, 0);
     for (int l = 0; l < d.nfy; ++l) {
       const int fy = d.fy[l];
       if (fy < 0 || fy > 2 * Ny) return fail("band row", b, l, fy);
       if (d.npy[l] < 0 || d.py0[l] < fy || d.py0[l] + d.npy[l] > KY) return fail("rows", b, l, d.py0[l]);
-      if (d.nst < 1 || d.st0 < 0 || d.st0 + d.nst > NIT) return fail("steps", b, d.st0, d.nst);
-      for (int j = 0; j < NL; ++j) {
-        const BtLane s = bt_lane(j, Nx);
-        for (int it = d.st0; it < d.st0 + d.nst; ++it) {
-          int px, qx, seg;
-          bt_step(s, it, &px, &qx, &seg);
-          if (px < 0 || px >= KX || qx < 0 || qx >= KX) return fail("column range", j, it, px);
-          for (int r = 0; r < d.npy[l]; ++r) {
-            const int e = ((l ? d.nst * d.npy[0] : 0) + (it - d.st0) * d.npy[l] + r) * NL + j;
+      for (int r = 0; r < d.npy[l]; ++r) {
+        const int py = d.py0[l] + r, qy = py - fy;
+        rows_seen[fy * KY + py]++;
+        for (int s = 0; s < NS; ++s)
+          for (int j = 0; j < NL; ++j) {
+            const int e = bt_entry(d, l, r, s, j, Nx);
             if (e < 0 || e >= d.size || used[e]++) return fail("table entry", b, e, d.size);
+            int px, qx;
+            if (!bt_slot(j, s, Nx, &px, &qx)) continue;
+            if (px < 0 || px >= KX || qx < 0 || qx >= KX) return fail("column range", j, s, px);
+            seen[std::make_tuple(fy, px - qx, py, px, qy, qx)]++;
           }
-          if (seg == 3 && j > 0) continue;  // idle step
-          const int f = seg == 1 ? s.f1 : seg == 2 ? s.f2 : s.f3;
-          if (px - qx != f) return fail("diagonal", j, it, f);
-          for (int r = 0; r < d.npy[l]; ++r) {
-            const int py = d.py0[l] + r, qy = py - fy;
-            if (qy < 0) return fail("q row", b, py, fy);
-            seen[std::make_tuple(fy, f, py, px, qy, qx)]++;
-          }
-        }
       }
     }
     for (int e = 0; e < d.size; ++e)
       if (used[e] != 1) return fail("table hole", b, e, used[e]);
   }
   if ((size_t)off != band_tcc_entries(Nx, Ny, nc)) return fail("table size", (int)off, 0, 0);
+  for (int fy = 0; fy <= 2 * Ny; ++fy)
+    for (int py = 0; py < KY; ++py)
+      if (rows_seen[fy * KY + py] != (py >= fy ? 1 : 0)) return fail("window row", fy, py, rows_seen[fy * KY + py]);
   // every pair of every band entry once
   size_t want = 0;
   for (int fy = 0; fy <= 2 * Ny; ++fy)
@@ -137,7 +123,7 @@ def test_schedule_visits_every_pair_once(driver):
 def test_chunking_of_the_metric_optics(driver):
     # a chunk's table shares shared memory with a window per image of every warp: at
     # Nx = Ny = 8 a whole task fits (one partial group), at Nx = Ny = 16 the tasks'
-    # column steps are cut into chunks
+    # window rows are cut into chunks
     r = subprocess.run([driver], input="8 8\n16 16\n", capture_output=True, text=True)
     (a, b) = [ln.split() for ln in r.stdout.split("\n") if ln]
     assert a[1] == "1"
