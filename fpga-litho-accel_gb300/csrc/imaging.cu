@@ -727,7 +727,7 @@ constexpr int FR_THREADS = 256, FR_COLS = 128, FR_ROWS = 2 * FR_COLS + 1;  // co
 template <int MAXD, bool KMAJ, int KPC>
 __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __restrict__ band_part, int ngroups,
                                                              const float2* __restrict__ twF, int Lx, int Fx,
-                                                             int Nx, int Ny, int kp_rt, int batch,
+                                                             int Nx, int Ny, int kp_rt, int batch, int raw_n,
                                                              float* __restrict__ tm, float* __restrict__ tmh,
                                                              float* __restrict__ tml, float* __restrict__ t0) {
   extern __shared__ __align__(16) float4 frs[];
@@ -758,18 +758,46 @@ __global__ void __launch_bounds__(FR_THREADS) fi_rows_kernel(const float2* __res
   const int imin = max(0, M - X0 - Lx + 1);
   const int nmir = max(0, nbase - imin), Mlo = M - X0 - nbase + 1;
   const int nrows = nbase + nmir + (xtra ? 1 : 0);
-  for (int img = blockIdx.y; img < batch; img += gridDim.y) {
-    __syncthreads();  // the previous image is out of sC and sO
-    const float2* B = band_part + (size_t)img * ngroups * BH * BW;
+  // the next image's band partials stream into shared memory (8-byte cp.async) while
+  // this image is computed, when the two buffers fit (raw_n > 0)
+  const int RAWN = ngroups * BH * BW;
+  float2* raw = raw_n > 0 ? reinterpret_cast<float2*>(
+                                (reinterpret_cast<uintptr_t>(sO + (KMAJ ? FR_ROWS * (KP + 1) : 0)) + 15) & ~uintptr_t(15))
+                          : nullptr;
+  auto fetch = [&](int im, float2* dst) {
+    const float2* src = band_part + (size_t)im * RAWN;
+    for (int e = tid; e < RAWN; e += FR_THREADS) {
+      const unsigned da = (unsigned)__cvta_generic_to_shared(dst + e);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(da), "l"(src + e) : "memory");
+    }
+  };
+  if (raw != nullptr) {
+    if ((int)blockIdx.y < batch) fetch(blockIdx.y, raw);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  for (int img = blockIdx.y, k = 0; img < batch; img += gridDim.y, ++k) {
+    if (raw != nullptr) {
+      if (img + (int)gridDim.y < batch) fetch(img + gridDim.y, raw + (size_t)((k + 1) & 1) * RAWN);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 1;" ::: "memory");  // this image's partials have landed
+    }
+    __syncthreads();  // the previous image is out of sC and sO (and this one's partials are visible)
+    const float2* B = raw != nullptr ? raw + (size_t)(k & 1) * RAWN : band_part + (size_t)img * RAWN;
     for (int idx = tid; idx < BH * MAXD; idx += FR_THREADS) {
       const int fy = idx / MAXD, d = idx - fy * MAXD;  // MAXD: a compile-time divisor
       if (d >= ND) continue;
       const float2* S = B + fy * BW + 2 * Nx;
-      const float2 pv = sum_strided(S + d, pst, ngroups);
+      float2 pv = S[d], qv = S[-d];
+      for (int gi = 1; gi < ngroups; ++gi) {  // the kernel groups' partials, in order
+        const float2 a = S[gi * pst + d], b = S[gi * pst - d];
+        pv.x += a.x;
+        pv.y += a.y;
+        qv.x += b.x;
+        qv.y += b.y;
+      }
       if (d == 0) {
         sC[fy * MAXD] = make_float4(pv.x, pv.y, 0.f, 0.f);
       } else {
-        const float2 qv = sum_strided(S - d, pst, ngroups);
         sC[fy * MAXD + d] = make_float4(pv.x + qv.x, -(pv.y - qv.y), pv.y + qv.y, pv.x - qv.x);
       }
     }
@@ -878,8 +906,12 @@ template <int MAXD, bool KMAJ, int KPC = 0>
 static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const float2* band_part, const float2* twF,
                                     int KP, float* tm, float* tmh, float* tml, float* t0) {
   const ImgGeom& g = p.g;
+  // two shared buffers for the band partials of the next image when they fit in 32 KB
+  const int rawn = p.ngroups * (2 * g.Ny + 1) * (4 * g.Nx + 1);
+  const bool pre = (size_t)2 * rawn * sizeof(float2) <= 32 * 1024;
   const size_t smem = (size_t)(2 * g.Ny + 1) * MAXD * sizeof(float4) +
-                      (KMAJ ? (size_t)FR_ROWS * (KP + 1) * sizeof(float) : 0);
+                      (KMAJ ? (size_t)FR_ROWS * (KP + 1) * sizeof(float) : 0) +
+                      (pre ? 2 * (size_t)rawn * sizeof(float2) + 16 : 0);
   auto k = fi_rows_kernel<MAXD, KMAJ, KPC>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -889,8 +921,8 @@ static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const floa
   const int ncb = std::max(1, (nb + FR_COLS - 1) / FR_COLS);
   const int sms = p.sms > 0 ? p.sms : 148;
   const int groups = std::max(1, std::min(p.batch, (4 * sms + ncb - 1) / ncb));
-  k<<<dim3(ncb, groups), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx, g.Nx, g.Ny, KP, p.batch, tm,
-                                                tmh, tml, t0);
+  k<<<dim3(ncb, groups), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx, g.Nx, g.Ny, KP, p.batch,
+                                                pre ? rawn : 0, tm, tmh, tml, t0);
   return cudaGetLastError();
 }
 
