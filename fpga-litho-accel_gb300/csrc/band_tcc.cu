@@ -18,7 +18,7 @@
 // j of an image owns the p column j and walks the q columns (plus a share of the last p
 // column): its p value stays in a register, every q value is one load broadcast to the
 // image's lanes, and its 2Nx+1 running sums (one per q column, band column j - qx) are
-// summed along the band diagonals through shared memory once per band row.  T is stored
+// summed along the band diagonals by warp shuffles once per band row.  T is stored
 // per task-chunk in the order the lanes consume it ([row][slot][lane]), so that a CTA
 // holds its chunk in shared memory and every warp streams it while imaging its own
 // images: 2Nx lanes per image, 32 / (2Nx) images per warp.

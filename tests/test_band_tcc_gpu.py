@@ -38,7 +38,9 @@ def _cases():
         "256_annular_k8": (256, 256, ann, 8),
         # Nx = 6: the kernel without a compile-time support size; Fx = 1024 > Lx
         "768_annular_k10": (768, 768, ann, 10),
-        # Nx = 16: the table cut into column-step chunks (several partial groups)
+        # Nx = 1: two lanes per image, sixteen images per warp
+        "128_annular_k4": (128, 128, ann, 4),
+        # Nx = 16: the table cut into row chunks (several partial groups)
         "2048_annular_k12": (2048, 2048, ann, 12),
     }
 
