@@ -627,6 +627,15 @@ def main():
     ms_g, _ = timed("mixed", args.steps, False, grey)
     value_g = job_images_per_s(ws, B, args.steps, ms_g / 1e3)
     del grey
+    # the same step with the band formed by per-kernel 2-D inverse FFTs on the conv grid
+    # (LITHO_BAND_FFT) instead of the default TCC bilinear form
+    ctx.set_band_method(L.BAND_FFT)
+    for _ in range(3):
+        step("mixed")
+    ms_fft, _ = timed("mixed", args.steps, False)
+    _, st_fft = timed("mixed", max(10, args.steps // 5), True)
+    ctx.set_band_method(L.BAND_AUTO)
+    value_fft = job_images_per_s(ws, B, args.steps, ms_fft / 1e3)
     # per-kernel durations: a shorter pass with every launch bracketed by CUDA events
     ksteps = max(10, args.steps // 5)
     _, st_o = timed(other, ksteps, True)
@@ -667,6 +676,10 @@ def main():
     forms = {"mixed_grey_masks": {"images_per_s": value_g, "ms_per_step": ms_g / args.steps,
                                   "masks": "the step's masks as 8-bit grey levels / 255 (binary pattern x "
                                            "levels 200-255 on a background of levels 0-55)"},
+             "mixed_band_fft": {"images_per_s": value_fft, "ms_per_step": ms_fft / args.steps,
+                                "band_ms_per_step": st_fft["socs"][0] / max(10, args.steps // 5),
+                                "band": "per-kernel 2-D inverse FFTs on the 64^2 conv grid, sum of s_k |E_k|^2, "
+                                        "forward FFT (LITHO_BAND_FFT); the head forms use the TCC bilinear form"},
              head: {"images_per_s": value, "ms_per_step": ms / args.steps,
                     "stage_ms_per_step_serial": {s: st[s][0] / ksteps for s in names}},
              other: {"images_per_s": value_o, "ms_per_step": ms_o / args.steps,
