@@ -104,7 +104,8 @@ def test_default_is_tcc_band_where_available(ctx, case):
     assert np.array_equal(auto, tcc)
 
 
-def test_batch_plan_under_each_band_method(ctx):
+@pytest.mark.parametrize("prec_name,tol", [("fp32", PLAIN_TOL), ("mixed", MIXED_TOL)])
+def test_batch_plan_under_each_band_method(ctx, prec_name, tol):
     import torch
     import litho_gb300 as L
     from litho_gb300 import synth
@@ -117,14 +118,15 @@ def test_batch_plan_under_each_band_method(ctx):
         ctx.set_band_method(method)
         try:
             ks = ctx.kernel_set(krn, scales, nx, ny)
-            plan = L.BatchPlan(ctx, [ks], [512], items, precision=L.PREC_MIXED)
+            prec = L.PREC_FP32 if prec_name == "fp32" else L.PREC_MIXED
+            plan = L.BatchPlan(ctx, [ks], [512], items, precision=prec)
             for i, m in enumerate(masks):
                 plan.mask(i).copy_(torch.from_numpy(m))
             torch.cuda.synchronize()
             plan.run()
             ctx.synchronize()
             for i, r in enumerate(refs):
-                assert R.rel_l2(plan.image(i).cpu().numpy(), r) < MIXED_TOL, (name, i)
+                assert R.rel_l2(plan.image(i).cpu().numpy(), r) < tol, (name, prec_name, i)
             assert [c["band"] for c in plan.describe()["classes"]] == [name]
             plan.close()
             ks.close()
