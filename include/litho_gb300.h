@@ -209,7 +209,9 @@ int litho_image(litho_ctx* ctx, const float* mask, int Lx, int Ly,
 /* ---- batched imaging ------------------------------------------------------
  * A kernel set is uploaded once and reused by every batch (kernels fixed, as in
  * the reference's FPGA flow).  Masks of one batch share (Lx, Ly); masks are
- * packed back to back (image i at offset i*Lx*Ly), outputs likewise. */
+ * packed back to back (image i at offset i*Lx*Ly), outputs likewise.  Creating a
+ * set with 1 <= Nx <= 16 and Ny <= 16 also builds its rank-K TCC band table on the
+ * device (LITHO_BAND_TCC; 0.37 MB at Nx = Ny = 8, 5.0 MB at 16). */
 typedef struct litho_kernel_set litho_kernel_set;
 int litho_kernel_set_create(litho_ctx* ctx, const float* krn_r, const float* krn_i,
                             const float* scales, int nk, int Nx, int Ny, int mem,
