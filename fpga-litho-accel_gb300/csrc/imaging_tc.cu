@@ -553,15 +553,14 @@ struct FiTC {
   static constexpr uint32_t A_KB = 128 * 128;     // 128 rows x 32 fp32
   static constexpr uint32_t B_KB = BN * 128;      // BN rows x 32 fp32
   static constexpr uint32_t A_BYTES = 2 * KBLK * A_KB;
-  static constexpr uint32_t B_BYTES = 2 * KBLK * B_KB;
-  // B stages and staging tiles per epilogue group: three and two whenever shared
-  // memory holds them (K = 64 rows with 128-column tiles does not)
-  static constexpr bool ROOMY = KBLK == 1 || BN <= 64;
-  static constexpr bool WIDE_OUT = KBLK == 1 && BN == 128;  // two B stages, four staging tiles per warp
-  static constexpr int NS = WIDE_OUT ? 2 : (ROOMY ? 3 : 2);
-  static constexpr int NOUT = WIDE_OUT ? 4 : (ROOMY ? 2 : 1);
+  // a B stage is one K block of a tile (its hi and lo halves back to back); a tile takes
+  // KBLK consecutive stages.  K = 32 tiles: two stages and four staging tiles per
+  // epilogue warp; K = 64 tiles: three stages and two staging tiles.
+  static constexpr uint32_t STAGE_B = 2 * B_KB;
+  static constexpr int NS = KBLK == 1 ? 2 : 3;
+  static constexpr int NOUT = KBLK == 1 ? 4 : 2;
   static constexpr uint32_t OUT_B = 32 * 128;     // 32 rows x 32 fp32 staging tile of one warp
-  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * B_BYTES + 8 * NOUT * OUT_B + 2 * BN * 4 + 512;
+  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * STAGE_B + 8 * NOUT * OUT_B + 2 * BN * 4 + 512;
 };
 constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
 constexpr int FI_TQ = 8;         // tile ring slots
@@ -595,7 +594,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   unsigned char* sAh = sm;
   unsigned char* sAl = sm + KBLK * P::A_KB;
   unsigned char* sB = sm + P::A_BYTES;               // [NS][kb][hi, lo]
-  unsigned char* sOut = sB + NS * P::B_BYTES;        // [8 epilogue warps][NOUT][OUT_B]
+  unsigned char* sOut = sB + NS * P::STAGE_B;        // [8 epilogue warps][NOUT][OUT_B]
   float* sT0 = reinterpret_cast<float*>(sOut + 8 * NOUT * P::OUT_B);  // [2 accumulators][BN]: the tile's DC row
   uint64_t* fullA = reinterpret_cast<uint64_t*>(sT0 + 2 * BN);
   uint64_t* emptyA = fullA + 1;
@@ -664,8 +663,8 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
     return true;
   };
   // the hi and lo tiles of one K block sit back to back, so Ah x [Bh; Bl] is one N = 2 BN MMA
-  auto Bh = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb) * P::B_KB; };
-  auto Bl = [&](int s, int kb) { return sB + (size_t)s * P::B_BYTES + (size_t)(2 * kb + 1) * P::B_KB; };
+  auto Bh = [&](int s) { return sB + (size_t)s * P::STAGE_B; };
+  auto Bl = [&](int s) { return sB + (size_t)s * P::STAGE_B + P::B_KB; };
 
   if (warp == 8) {
     if (lane == 0) {  // TMA producer
@@ -697,17 +696,20 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
           ++gen;
           cur = yb;
         }
-        const int q = seq, s = q % NS;
-        if (q >= NS && !mbar_wait_ab(&emptyB[s], (uint32_t)((q - NS) / NS) & 1u, abort)) {
-          *abort = 1;
-          break;
+        bool stop = false;
+        for (int kb = 0; kb < KBLK; ++kb) {  // stage g: K block kb of tile seq
+          const int g = seq * KBLK + kb, s = g % NS;
+          if (g >= NS && !mbar_wait_ab(&emptyB[s], (uint32_t)((g - NS) / NS) & 1u, abort)) {
+            *abort = 1;
+            stop = true;
+            break;
+          }
+          mbar_arrive_expect_tx(&fullB[s], P::STAGE_B);
+          tma_load_3d(Bh(s), &tmTh, &fullB[s], 32 * kb, xt * BN, img);
+          tma_load_3d(Bl(s), &tmTl, &fullB[s], 32 * kb, xt * BN, img);
+          last_issued[s] = g;
         }
-        mbar_arrive_expect_tx(&fullB[s], P::B_BYTES);
-        for (int kb = 0; kb < KBLK; ++kb) {
-          tma_load_3d(Bh(s, kb), &tmTh, &fullB[s], 32 * kb, xt * BN, img);
-          tma_load_3d(Bl(s, kb), &tmTl, &fullB[s], 32 * kb, xt * BN, img);
-        }
-        last_issued[s] = q;
+        if (stop) break;
       }
     }
   } else if (warp == 9) {
@@ -723,7 +725,7 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
           break;
         }
         if (i < 0) break;
-        const int q = seq, s = q % NS, b = q & 1;
+        const int q = seq, b = q & 1;
         const int yb = band_of(i);
         if (yb != cur) {
           // every MMA on the previous band's A tiles is issued: they may be replaced once those complete
@@ -735,25 +737,30 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
           ++gen;
           cur = yb;
         }
-        if (!mbar_wait_ab(&fullB[s], (uint32_t)(q / NS) & 1u, abort) ||
-            (q >= 2 && !mbar_wait_ab(&accEmpty[b], (uint32_t)((q - 2) >> 1) & 1u, abort))) {
+        if (q >= 2 && !mbar_wait_ab(&accEmpty[b], (uint32_t)((q - 2) >> 1) & 1u, abort)) {
           ok = false;
           break;
         }
-        tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * 2 * BN);
 #pragma unroll
         for (int kb = 0; kb < KBLK; ++kb) {
+          const int g = q * KBLK + kb, s = g % NS;
+          if (!mbar_wait_ab(&fullB[s], (uint32_t)(g / NS) & 1u, abort)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
           const uint64_t dah = desc_sw128(sAh + (size_t)kb * P::A_KB), dal = desc_sw128(sAl + (size_t)kb * P::A_KB);
-          const uint64_t dbh = desc_sw128(Bh(s, kb));
+          const uint64_t dbh = desc_sw128(Bh(s));
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
             const uint32_t off = kk * 32;
             mma_tf32(acc, desc_add(dah, off), desc_add(dbh, off), IDESC2, (kb | kk) != 0 ? 1u : 0u);
             mma_tf32(acc, desc_add(dal, off), desc_add(dbh, off), IDESC1, 1u);
           }
+          mma_commit(&emptyB[s]);
         }
-        mma_commit(&emptyB[s]);
+        if (!ok) break;
         mma_commit(&accFull[b]);
       }
       if (!ok) *abort = 1;
