@@ -183,6 +183,12 @@ int litho_ctx_set_band_method(litho_ctx* ctx, int method) {
   return LITHO_OK;
 }
 
+int litho_ctx_set_host_chunk(litho_ctx* ctx, size_t bytes) {
+  if (ctx == nullptr) return LITHO_ERR_ARG;
+  ctx->host_chunk_bytes = bytes;
+  return LITHO_OK;
+}
+
 int litho_ctx_stage_times(litho_ctx* ctx, double* ms, long long* launches, int reset) {
   if (ctx == nullptr) return LITHO_ERR_ARG;
   LITHO_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -302,7 +308,7 @@ int default_conv_n(int Nx, int Ny) {
 
 }  // namespace litho
 
-// Host buffers: the batch moves in chunks of up to about 16 MB through HB_SLOTS
+// Host buffers: the batch moves in chunks of up to 128 MB (host_chunks.hpp) through HB_SLOTS
 // device staging slots each way.  Host->device copies run on one copy stream
 // and device->host copies on another, so chunk k+1 arrives and chunk k-1 leaves
 // while chunk k is imaged on the context's stream; events order the reuse of
@@ -314,7 +320,8 @@ int default_conv_n(int Nx, int Ny) {
 static int host_batch(litho_ctx* ctx, const ImgGeom& g, int batch, const float* masks, const litho_kernel_set* ks,
                       float* images, int precision, size_t img) {
   constexpr int NS = HB_SLOTS;
-  const int CH = litho::host_chunk_masks(batch, img);
+  const int CH = litho::host_chunk_masks(batch, img,
+                                         ctx->host_chunk_bytes ? ctx->host_chunk_bytes : litho::HOST_CHUNK_BYTES);
   std::vector<int> sizes;
   litho::chunk_schedule(batch, CH, sizes);
   if (ctx->copy_in == nullptr) {

@@ -123,6 +123,8 @@ struct litho_ctx {
   // how the SOCS band is formed for kernel sets that carry a TCC band table
   // (litho_ctx_set_band_method): LITHO_BAND_AUTO / _FFT / _TCC
   int band_method = 0;
+  // mask bytes per chunk of the host-buffer path (litho_ctx_set_host_chunk); 0: default
+  size_t host_chunk_bytes = 0;
   // window-DFT column twiddle tables keyed by (Lx, Fx, Nx, NJT)
   std::map<std::tuple<int, int, int, int>, litho::DevBuf> twx_tables;
   // TCC / eigensolver workspaces

@@ -78,6 +78,7 @@ _SIGS = {
     "litho_ctx_stage_times": (_i, [_p, _p, _p, _i]),
     "litho_ctx_set_test_stall": (_i, [_p, _i]),
     "litho_ctx_set_band_method": (_i, [_p, _i]),
+    "litho_ctx_set_host_chunk": (_i, [_p, C.c_size_t]),
     "litho_tcc_gemm_shape": (_i, [_p, _i, _i, _i]),
     "litho_tcc_gemm_describe": (_i, [_p, C.c_char_p, _i]),
     "litho_batch_plan_create": (_i, [_p, _p, _p, _i, _p, _i, _i, _i, C.POINTER(_p)]),
@@ -318,6 +319,11 @@ class Context:
         """BAND_AUTO (default: the TCC form where the kernel set has its table), BAND_FFT (per
         kernel FFTs on the conv grid) or BAND_TCC (litho_ctx_set_band_method)."""
         self._check(_lib.litho_ctx_set_band_method(self.h, int(method)))
+
+    def set_host_chunk(self, nbytes: int = 0):
+        """Mask bytes per chunk of image_batch on host arrays (litho_ctx_set_host_chunk);
+        0 restores the default (128 MB)."""
+        self._check(_lib.litho_ctx_set_host_chunk(self.h, int(nbytes)))
 
     def stage_times(self, reset: bool = True):
         """{stage: (device ms, kernel launches)} since the last reset (synchronises the stream)."""

@@ -143,6 +143,14 @@ int litho_ctx_set_test_stall(litho_ctx* ctx, int chunk);
  * enqueued (and when a batch plan is created). */
 int litho_ctx_set_band_method(litho_ctx* ctx, int method);
 
+/* ---- host-buffer chunks -----------------------------------------------------
+ * No reference counterpart.  litho_image_batch with LITHO_MEM_HOST moves the batch
+ * through the device in chunks of at most `bytes` of masks (at least one mask, and at
+ * least about eight chunks per batch), copies in and out overlapping the imaging.
+ * The device holds three staging slots of a chunk each way.  Larger chunks move
+ * faster over the host link; 0 restores the default, 128 MB (768 MB of slots). */
+int litho_ctx_set_host_chunk(litho_ctx* ctx, size_t bytes);
+
 /* ---- optics helpers (litho.cpp:414-426, 1297-1302) --------------------- */
 /* getOuterSigma: max lit-pixel radius / ((srcSize-1)/2), clamped to 1 as
  * litho.cpp:1298 does.  Host pointer. */

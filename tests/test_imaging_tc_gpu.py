@@ -105,11 +105,12 @@ def test_mixed_unsupported_geometry(ctx, L):
 
 
 
-@pytest.mark.parametrize("prec", ["plain", "mixed"])
-def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec):
-    """Host buffers of 20 masks move through the chunked copy/compute pipeline (ramped
-    chunks of 1, 2, 3, 3, 3, 3, 2, 2, 1 masks on three staging slots); the images equal
-    the device-pointer path's."""
+@pytest.mark.parametrize("prec,chunk", [("plain", 0), ("mixed", 0), ("mixed", 2 << 20), ("mixed", 1)])
+def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec, chunk):
+    """Host buffers of 20 masks of 1 MB move through the chunked copy/compute pipeline on
+    three staging slots: by default ramped chunks of 1, 2, 3, 3, 3, 3, 2, 2, 1 masks (at
+    least eight chunks), with a 2 MB chunk cap 1, 2 x 9, 1, with a 1-byte cap one mask per
+    chunk.  The images equal the device-pointer path's."""
     import torch
     from litho_gb300 import synth
     p = L.PREC_MIXED if prec == "mixed" else L.PREC_FP32
@@ -117,11 +118,13 @@ def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec):
     masks = np.stack([synth.density_rect_mask(512, 0.2 + 0.02 * i, seed=90 + i) for i in range(20)])
     ks = ctx.kernel_set(krns, scales, nx, nx)
     try:
+        ctx.set_host_chunk(chunk)
         host = ctx.image_batch(ks, masks, precision=p)          # numpy in, numpy out
         dev = ctx.image_batch(ks, torch.from_numpy(masks).cuda(), precision=p)
         ctx.synchronize()
         dev = dev.cpu().numpy()
     finally:
+        ctx.set_host_chunk(0)
         ks.close()
     for i in range(20):
         assert R.rel_l2(host[i], dev[i]) < 1e-6, i
