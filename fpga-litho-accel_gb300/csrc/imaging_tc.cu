@@ -69,16 +69,22 @@ __global__ void twT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 
 // ytab[v][y] = e^{-2 pi i v y'/Fy} (v = 0..Ny), y' = y + (Fy - Ly)/2 - Fy/2: the row
 // twiddles of the window DFT's epilogue
-__global__ void ytab_init_kernel(float2* __restrict__ yt, int Ly, int Fy) {
+// yt[v][y] = e^{-2 pi i v y' / Fy} for the rows y < Ly, rows padded to Lyp (a multiple
+// of 128) with zeros, so that a 128-row tile reads whole rows of it.
+__global__ void ytab_init_kernel(float2* __restrict__ yt, int Ly, int Lyp, int Fy) {
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   const int v = blockIdx.y;
-  if (y >= Ly) return;
-  const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
-  long long m = ((long long)v * (y + oyc)) % Fy;
-  if (m < 0) m += Fy;
-  float sn, cs;
-  sincospif(2.0f * (float)m / (float)Fy, &sn, &cs);
-  yt[(size_t)v * Ly + y] = make_float2(cs, -sn);
+  if (y >= Lyp) return;
+  float2 t = make_float2(0.f, 0.f);
+  if (y < Ly) {
+    const long long oyc = (long long)(Fy - Ly) / 2 - Fy / 2;
+    long long m = ((long long)v * (y + oyc)) % Fy;
+    if (m < 0) m += Fy;
+    float sn, cs;
+    sincospif(2.0f * (float)m / (float)Fy, &sn, &cs);
+    t = make_float2(cs, -sn);
+  }
+  yt[(size_t)v * Lyp + y] = t;
 }
 
 // CyT[Y][r] (KP columns): r < 2Ny -> 2cos(2 pi (r+1) y'/Fy); 2Ny <= r < 4Ny ->
@@ -135,8 +141,10 @@ __global__ void cyT_init_kernel(float* __restrict__ hi, float* __restrict__ lo, 
 // The ring is as deep as shared memory allows: under full load a mask tile takes
 // ~3 us from TMA issue to landing, so the bytes in flight per SM, not the work per
 // tile, set the throughput.  Hence the twiddle tile carries only the 2Nx+1 used
-// rows of each half (NBH = 2Nx+1 rounded up to 8) and the epilogue buffers are
-// sized for the actual Ny; the stage count S is chosen at launch.
+// rows of each half (NBH = 2Nx+1 rounded up to 8), the epilogue keeps only the 2Nx+1
+// used accumulator columns in shared memory and reads the row twiddles from their
+// table (through L1), and the stage count S is chosen at launch: four stages (128 KB of
+// mask in flight) up to Nx = 16.
 template <int NBH>
 struct WinTC {
   // a stage carries a 64-column chunk as two 32-column K blocks: each pipeline round
@@ -159,15 +167,12 @@ constexpr int WP_CONS = 256;     // consumer threads
 // reads 16-byte vectors, and 33 / 65 float4 slots apart so the threads of a warp
 // (different u, different |v|) land in different bank groups
 constexpr int WP_RSR = 132;      // sR rows (fp32)
-constexpr int WP_RST = 130;      // sRT rows (float2)
 constexpr int WP_MAX_STAGES = 12;
 constexpr int WP_TQ = 8;         // tile ring: tiles the producer may publish ahead of the slowest role
 constexpr size_t WP_SMEM_CAP = 227 * 1024;
 
-// epilogue buffers: sR [NBH][RSR] fp32 + sRT [Ny+1][RST] float2
-static inline size_t win_epi_bytes(int NBH, int Ny) {
-  return (size_t)NBH * WP_RSR * 4 + (size_t)(Ny + 1) * WP_RST * 8;
-}
+// epilogue buffer: sR [2Nx+1][RSR] fp32 (a multiple of 16 bytes)
+static inline size_t win_epi_bytes(int Nx) { return (size_t)(2 * Nx + 1) * WP_RSR * 4; }
 // mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES): 5 per stage, 5 more,
 // two per tile-ring slot; the TMEM slot, abort flag, per-stage ints, tile ring and the two
 // groups' current tiles
@@ -186,10 +191,10 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   using P = WinTC<NBH>;
   extern __shared__ unsigned char smraw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  constexpr int RS = WP_RSR, RT = WP_RST;
-  float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [NBH][RS]
-  float2* sRT = reinterpret_cast<float2*>(sR + NBH * RS);             // [Ny+1][RT]
-  uint64_t* full = reinterpret_cast<uint64_t*>(sRT + (Ny + 1) * RT);
+  constexpr int RS = WP_RSR;
+  const int KXw = 2 * Nx + 1;                                          // used accumulator columns
+  float* sR = reinterpret_cast<float*>(sm + (size_t)S * P::STAGE_B);  // [KXw][RS]
+  uint64_t* full = reinterpret_cast<uint64_t*>(sR + KXw * RS);
   uint64_t* ready = full + S;
   uint64_t* hidone = ready + S;
   uint64_t* ready2 = hidone + S;
@@ -468,15 +473,12 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         for (int g = 0; g < 2 * NBH / 8; ++g) tmem_ld8_async(trow + 8u * g, &v[8 * g]);
         tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < NBH; ++j) sR[j * RS + row] = __uint_as_float(v[j]) + __uint_as_float(v[NBH + j]);
+        for (int j = 0; j < NBH; ++j)
+          if (j < KXw) sR[j * RS + row] = __uint_as_float(v[j]) + __uint_as_float(v[NBH + j]);
       }
       tc_fence_before();
       mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
       const int y0 = 128 * rb;
-      for (int i = etid; i < (Ny + 1) * 128; i += 128) {
-        const int v = i >> 7, r = i & 127, y = y0 + r;
-        sRT[v * RT + r] = y < Ly ? ytab[(size_t)v * Ly + y] : make_float2(0.f, 0.f);
-      }
       named_bar(2, 128);
       const int nps = part_stride > 0 ? part_stride : rows * ncs;
       float2* out = win_part + ((size_t)img * nps + (rb * ncs + cs)) * KY * NU;
@@ -488,12 +490,13 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         const int av = pq / NU, u = pq - av * NU;
         const float4* rc = reinterpret_cast<const float4*>(sR + u * RS);
         const float4* rs = reinterpret_cast<const float4*>(sR + (Nx + u) * RS);
-        const float4* rt = reinterpret_cast<const float4*>(sRT + av * RT);  // two rows' twiddles per vector
+        // the tile's row twiddles of |v| (zero past Ly), two rows per vector, from L1
+        const float4* rt = reinterpret_cast<const float4*>(ytab + (size_t)av * (128 * rows) + y0);
         float s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
         if (u == 0) {
 #pragma unroll 4
           for (int r4 = 0; r4 < 32; ++r4) {
-            const float4 c = rc[r4], ta = rt[2 * r4], tb = rt[2 * r4 + 1];
+            const float4 c = rc[r4], ta = __ldg(rt + 2 * r4), tb = __ldg(rt + 2 * r4 + 1);
             s1 = fmaf(c.x, ta.x, s1);
             s3 = fmaf(c.x, ta.y, s3);
             s1 = fmaf(c.y, ta.z, s1);
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         } else {
 #pragma unroll 4
           for (int r4 = 0; r4 < 32; ++r4) {
-            const float4 c = rc[r4], sn = rs[r4], ta = rt[2 * r4], tb = rt[2 * r4 + 1];
+            const float4 c = rc[r4], sn = rs[r4], ta = __ldg(rt + 2 * r4), tb = __ldg(rt + 2 * r4 + 1);
             s1 = fmaf(c.x, ta.x, s1);
             s2 = fmaf(sn.x, ta.y, s2);
             s3 = fmaf(c.x, ta.y, s3);
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         out[(Ny + av) * NU + u] = make_float2((s1 - s2) * inv_ff, (s3 + s4) * inv_ff);
         if (av > 0) out[(Ny - av) * NU + u] = make_float2((s1 + s2) * inv_ff, (s4 - s3) * inv_ff);
       }
-      named_bar(2, 128);  // sR / sRT are free for the next tile
+      named_bar(2, 128);  // sR is free for the next tile
     }
   }
   // the MMA lane always commits `done`; everyone waits for the tensor cores to drain
@@ -771,7 +774,6 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
     // row, through its own swizzled staging tiles and its own 32-row TMA stores.  No
     // barrier joins the warps, so each keeps NOUT stores of its own in flight.
     const int quarter = warp & 3, half = warp >> 2;
-    const int row = 32 * quarter + lane;  // this lane's image row in the tile (its TMEM lane)
     unsigned char* stg = sOut + (size_t)warp * NOUT * P::OUT_B;
     int slab_count = 0;
     constexpr int NSL = BN / 64;  // slabs per warp per tile (1 or 2)
@@ -985,13 +987,14 @@ static int win_tc_tables(litho_ctx* ctx, const ImgGeom& g, float** twh, float** 
                                                                             g.Nx, NBH);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
-  // row twiddles of the epilogue, cached per (Ly, Fy, Ny)
-  LITHO_RET(cached_table(ctx, std::make_tuple(g.Ly, g.Fy, g.Ny, -3000), (size_t)(g.Ny + 1) * g.Ly * sizeof(float2),
+  // row twiddles of the epilogue, rows padded to a multiple of 128, cached per (Ly, Fy, Ny)
+  const int Lyp = (g.Ly + 127) / 128 * 128;
+  LITHO_RET(cached_table(ctx, std::make_tuple(g.Ly, g.Fy, g.Ny, -3001), (size_t)(g.Ny + 1) * Lyp * sizeof(float2),
                          &fresh, yt));
   if (fresh) {
     StageScope sc(ctx, LITHO_STAGE_UPLOAD);
-    ytab_init_kernel<<<dim3((g.Ly + 127) / 128, g.Ny + 1), 128, 0, ctx->stream>>>(
-        reinterpret_cast<float2*>(*yt), g.Ly, g.Fy);
+    ytab_init_kernel<<<dim3(Lyp / 128, g.Ny + 1), 128, 0, ctx->stream>>>(reinterpret_cast<float2*>(*yt), g.Ly,
+                                                                          Lyp, g.Fy);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   *twh = tw;
@@ -1008,9 +1011,9 @@ static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, f
   LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
   // as many ring stages as shared memory holds
   using P = WinTC<NBH>;
-  const size_t fixed = 1024 + win_epi_bytes(NBH, g.Ny) + win_bar_bytes(WP_MAX_STAGES);
+  const size_t fixed = 1024 + win_epi_bytes(g.Nx) + win_bar_bytes(WP_MAX_STAGES);
   const int S = (int)std::min<size_t>(WP_MAX_STAGES, (WP_SMEM_CAP - fixed) / P::STAGE_B);
-  const size_t smem = 1024 + (size_t)S * P::STAGE_B + win_epi_bytes(NBH, g.Ny) + win_bar_bytes(S);
+  const size_t smem = 1024 + (size_t)S * P::STAGE_B + win_epi_bytes(g.Nx) + win_bar_bytes(S);
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NBH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
   const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
