@@ -107,11 +107,14 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
   const int ch1 = (int)((long long)nch * (cs + 1) / colSplits);
   const float* M = masks + (size_t)img * Lx * Ly;
 
-  float acc[4][NJT];
+  // accumulators in column pairs: one packed (f32x2) FMA updates two twiddle columns, each
+  // lane rounding as fmaf does
+  float2 acc2[4][NJT / 2];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < NJT; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < NJT / 2; ++j) acc2[i][j] = make_float2(0.f, 0.f);
+  auto acc = [&](int i, int j) -> float& { return (j & 1) ? acc2[i][j >> 1].y : acc2[i][j >> 1].x; };
 
   float4 ra[8];
   const int lc4 = (tid & 15) * 4;
@@ -164,19 +167,21 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
     for (int kk = 0; kk < WD_BK / 8; ++kk) {
       const int k = warp * (WD_BK / 8) + kk;
       const float* a = sA + k * WD_SA + lane;
-      const float a0 = a[0], a1 = a[32], a2 = a[64], a3 = a[96];
+      const float2 a0 = make_float2(a[0], a[0]), a1 = make_float2(a[32], a[32]);
+      const float2 a2 = make_float2(a[64], a[64]), a3 = make_float2(a[96], a[96]);
       const float4* b4 = reinterpret_cast<const float4*>(sB + k * NJT);
 #pragma unroll
       for (int c = 0; c < NJT / 4; ++c) {
         const float4 b = b4[c];
-        const float bb[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          acc[0][4 * c + e] = fmaf(a0, bb[e], acc[0][4 * c + e]);
-          acc[1][4 * c + e] = fmaf(a1, bb[e], acc[1][4 * c + e]);
-          acc[2][4 * c + e] = fmaf(a2, bb[e], acc[2][4 * c + e]);
-          acc[3][4 * c + e] = fmaf(a3, bb[e], acc[3][4 * c + e]);
-        }
+        const float2 blo = make_float2(b.x, b.y), bhi = make_float2(b.z, b.w);
+        acc2[0][2 * c] = __ffma2_rn(a0, blo, acc2[0][2 * c]);
+        acc2[1][2 * c] = __ffma2_rn(a1, blo, acc2[1][2 * c]);
+        acc2[2][2 * c] = __ffma2_rn(a2, blo, acc2[2][2 * c]);
+        acc2[3][2 * c] = __ffma2_rn(a3, blo, acc2[3][2 * c]);
+        acc2[0][2 * c + 1] = __ffma2_rn(a0, bhi, acc2[0][2 * c + 1]);
+        acc2[1][2 * c + 1] = __ffma2_rn(a1, bhi, acc2[1][2 * c + 1]);
+        acc2[2][2 * c + 1] = __ffma2_rn(a2, bhi, acc2[2][2 * c + 1]);
+        acc2[3][2 * c + 1] = __ffma2_rn(a3, bhi, acc2[3][2 * c + 1]);
       }
     }
   }
@@ -190,7 +195,7 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < NJT; ++j) dst[j * WD_BM + lane + 32 * i] = acc[i][j];
+        for (int j = 0; j < NJT; ++j) dst[j * WD_BM + lane + 32 * i] = acc(i, j);
     }
     __syncthreads();
     if (warp < s) {
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < NJT; ++j) acc[i][j] += src[j * WD_BM + lane + 32 * i];
+        for (int j = 0; j < NJT; ++j) acc(i, j) += src[j * WD_BM + lane + 32 * i];
     }
     __syncthreads();
   }
@@ -207,7 +212,7 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < NJT; ++j) sR[j * WD_BM + lane + 32 * i] = acc[i][j];
+      for (int j = 0; j < NJT; ++j) sR[j * WD_BM + lane + 32 * i] = acc(i, j);
   }
   // row twiddles e^{-2 pi i v y'/Fy}, v = 0..Ny
   float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NJT * WD_BM);
@@ -976,9 +981,44 @@ int fi_twiddles(litho_ctx* ctx, const ImgGeom& g, const float2** out) {
 // ---------------------------------------------------------------------------
 constexpr int FO_BM = 64, FO_BN = 128, FO_THREADS = 256;
 
+// Cy[r][Y] for r < 4Ny+1 (r = 0: 1; 1..2Ny: 2cos(2 pi r y'/Fy); 2Ny+1..4Ny: -2sin of r-2Ny),
+// rows Y padded to Lyp (a multiple of FO_BM).  The FI kernel evaluates the same values
+// when it has no table (the allocation-free entry point).
+__device__ __forceinline__ float fo_cy(int r, int Y, int Ly, int Fy, int Ny) {
+  if (r == 0) return 1.f;
+  const long long yp = (long long)Y + (long long)(Fy - Ly) / 2 - Fy / 2;
+  const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
+  const float2 e = cis_exact((long long)dy * yp, Fy, 1.f);
+  return r <= 2 * Ny ? 2.f * e.x : -2.f * e.y;
+}
+
+__global__ void fo_cy_init_kernel(float* __restrict__ cy, int Ly, int Lyp, int Fy, int Ny) {
+  const int Y = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (Y < Lyp) cy[(size_t)r * Lyp + Y] = fo_cy(r, Y, Ly, Fy, Ny);
+}
+
+// the Cy table of a geometry, cached per (Ly, Fy, Ny) on the context
+static int fo_cy_table(litho_ctx* ctx, const ImgGeom& g, const float** out, int* Lyp) {
+  *Lyp = (g.Ly + FO_BM - 1) / FO_BM * FO_BM;
+  auto key = std::make_tuple(g.Ly, g.Fy, g.Ny, -5000);
+  auto it = ctx->twx_tables.find(key);
+  if (it == ctx->twx_tables.end()) {
+    const int KB = 4 * g.Ny + 1;
+    DevBuf b;
+    LITHO_RET(b.ensure(ctx, (size_t)KB * *Lyp * sizeof(float)));
+    StageScope sc(ctx, LITHO_STAGE_UPLOAD);
+    fo_cy_init_kernel<<<dim3(*Lyp / FO_BM, KB), FO_BM, 0, ctx->stream>>>(b.as<float>(), g.Ly, *Lyp, g.Fy, g.Ny);
+    LITHO_CUDA_TRY(ctx, cudaGetLastError());
+    it = ctx->twx_tables.emplace(key, b).first;
+  }
+  *out = it->second.as<float>();
+  return LITHO_OK;
+}
+
 template <bool VEC>
 __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restrict__ tm, int Lx, int Ly, int Fy,
-                                                            int Ny, float* __restrict__ images) {
+                                                            int Ny, const float* __restrict__ cyt, int Lyp,
+                                                            float* __restrict__ images) {
   extern __shared__ __align__(16) float fo[];
   const int KB = 4 * Ny + 1;
   float* sC = fo;                // [KB][FO_BM]
@@ -991,36 +1031,39 @@ __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restr
     const int X = X0 + c;
     sT[idx] = X < Lx ? T[(size_t)r * Lx + X] : 0.f;
   }
-  const long long yoff = (long long)(Fy - Ly) / 2 - Fy / 2;
-  for (int idx = tid; idx < KB * FO_BM; idx += FO_THREADS) {
-    const int r = idx / FO_BM, rr = idx - r * FO_BM;
-    const long long yp = (long long)(Y0 + rr) + yoff;
-    float v = 1.f;
-    if (r > 0) {
-      const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
-      const float2 e = cis_exact((long long)dy * yp, Fy, 1.f);
-      v = r <= 2 * Ny ? 2.f * e.x : -2.f * e.y;
+  if (cyt != nullptr) {  // the cached table: whole 16-byte pieces of the tile's rows
+    for (int idx = tid; idx < KB * (FO_BM / 4); idx += FO_THREADS) {
+      const int r = idx / (FO_BM / 4), q = idx - r * (FO_BM / 4);
+      reinterpret_cast<float4*>(sC)[idx] = __ldg(reinterpret_cast<const float4*>(cyt + (size_t)r * Lyp + Y0) + q);
     }
-    sC[idx] = v;
+  } else {
+    for (int idx = tid; idx < KB * FO_BM; idx += FO_THREADS) {
+      const int r = idx / FO_BM, rr = idx - r * FO_BM;
+      sC[idx] = fo_cy(r, Y0 + rr, Ly, Fy, Ny);
+    }
   }
   __syncthreads();
   const int ty = tid >> 4, tx = tid & 15;
-  float acc[4][8];
+  // accumulators in column pairs: one packed (f32x2) FMA per pair, each lane rounding as fmaf
+  float2 acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
 #pragma unroll 4
   for (int r = 0; r < KB; ++r) {
     const float4 c = *reinterpret_cast<const float4*>(sC + r * FO_BM + 4 * ty);
     const float4 t0 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 4 * tx);
     const float4 t1 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 64 + 4 * tx);
     const float cc[4] = {c.x, c.y, c.z, c.w};
-    const float tt[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+    const float2 tt[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
+                          make_float2(t1.z, t1.w)};
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 4; ++i) {
+      const float2 ci = make_float2(cc[i], cc[i]);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(cc[i], tt[j], acc[i][j]);
+      for (int j = 0; j < 4; ++j) acc[i][j] = __ffma2_rn(ci, tt[j], acc[i][j]);
+    }
   }
   float* O = images + (size_t)img * Lx * Ly;
 #pragma unroll
@@ -1031,13 +1074,13 @@ __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restr
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int X = X0 + 64 * h + 4 * tx;
+      const float o[4] = {acc[i][2 * h].x, acc[i][2 * h].y, acc[i][2 * h + 1].x, acc[i][2 * h + 1].y};
       if (VEC && X + 3 < Lx) {
-        __stcs(reinterpret_cast<float4*>(row + X),
-               make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]));
+        __stcs(reinterpret_cast<float4*>(row + X), make_float4(o[0], o[1], o[2], o[3]));
       } else {
 #pragma unroll
         for (int e = 0; e < 4; ++e)
-          if (X + e < Lx) row[X + e] = acc[i][4 * h + e];
+          if (X + e < Lx) row[X + e] = o[e];
       }
     }
   }
@@ -1266,16 +1309,15 @@ int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm,
   }
   {
     const int KB = 4 * g.Ny + 1;
+    int Lyp = 0;
+    const float* cyt = nullptr;
+    LITHO_RET(fo_cy_table(ctx, g, &cyt, &Lyp));
     const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);
     dim3 grid((g.Lx + FO_BN - 1) / FO_BN, (g.Ly + FO_BM - 1) / FO_BM, p.batch);
     StageScope sc(ctx, LITHO_STAGE_FI_OUT);
-    if ((g.Lx & 3) == 0) {
-      LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_out_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      fi_out_kernel<true><<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, images);
-    } else {
-      LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(fi_out_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      fi_out_kernel<false><<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, images);
-    }
+    auto k = (g.Lx & 3) == 0 ? fi_out_kernel<true> : fi_out_kernel<false>;
+    LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, cyt, Lyp, images);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   return LITHO_OK;
@@ -1419,7 +1461,7 @@ cudaError_t image_pipeline_noctx(cudaStream_t s, const ImgPlan& p, const float* 
     auto k = (g.Lx & 3) == 0 ? fi_out_kernel<true> : fi_out_kernel<false>;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
       return e;
-    k<<<grid, FO_THREADS, smem, s>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, image);
+    k<<<grid, FO_THREADS, smem, s>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, nullptr, 0, image);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
