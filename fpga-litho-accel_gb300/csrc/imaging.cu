@@ -78,24 +78,52 @@ __global__ void twx_init_kernel(float* __restrict__ twx, int Lx, int Fx, int Nx,
 // ---------------------------------------------------------------------------
 // window DFT
 // ---------------------------------------------------------------------------
-constexpr int WD_BM = 128;     // mask rows per CTA
-constexpr int WD_BK = 64;      // mask columns per shared-memory chunk
-constexpr int WD_SA = WD_BM + 1;
+constexpr int WD_BM = 128;          // mask rows per CTA
+constexpr int WD_BK = 32;           // mask columns per ring stage
+constexpr int WD_SA = WD_BK + 4;    // staged row stride (floats): 16-byte rows, conflict-free 16-byte reads
 constexpr int WD_THREADS = 256;
 
+// ring stages: enough mask bytes in flight per SM (two CTAs of 4 x 16 KB where the
+// accumulators leave room for two, else one CTA of 8)
 template <int NJT>
-constexpr size_t win_dft_smem(int Ny) {
-  return 0;  // computed on the host (see run_win_dft)
+struct WinRing {
+  static constexpr int CTAS = NJT <= 20 ? 2 : 1;
+  static constexpr int ST = NJT <= 20 ? 4 : 8;
+  static constexpr int A_F = WD_BM * WD_SA;  // floats of a stage's mask chunk
+  static constexpr int STAGE_F = A_F + WD_BK * NJT;
+};
+
+// shared memory of a window DFT launch: the ring, reused by the k-split reduction and
+// the row transform at the end
+template <int NJT>
+static size_t win_dft_smem(int Ny) {
+  const size_t ring = (size_t)WinRing<NJT>::ST * WinRing<NJT>::STAGE_F * sizeof(float);
+  const size_t red = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(Ny + 1) * WD_BM * sizeof(float2);
+  return std::max(ring, red);
 }
 
+__device__ __forceinline__ void wd_cp16(float* dst, const float* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void wd_cp4(float* dst, const float* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+
+// One CTA per (row block of WD_BM rows, column split, image): the mask chunks of its
+// columns stream through a ring of cp.async stages (row-major, zero-filled past the
+// mask) with the chunk's column twiddles beside them; warp w multiplies columns
+// 4w..4w+3 of every chunk into its 4 rows x NJT accumulators (rows lane + 32i), in
+// packed f32x2 FMAs.  The eight warps' sums are then added in a fixed tree and each
+// row block's row transforms summed over its rows with the row twiddles.
 template <int NJT, bool VEC>
-__global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __restrict__ masks, int Lx, int Ly,
-                                                             int Fx, int Fy, int Nx, int Ny,
-                                                             const float* __restrict__ twx,
-                                                             float2* __restrict__ win_part, int part_stride) {
+__global__ void __launch_bounds__(WD_THREADS, WinRing<NJT>::CTAS) win_dft_kernel(
+    const float* __restrict__ masks, int Lx, int Ly, int Fx, int Fy, int Nx, int Ny, const float* __restrict__ twx,
+    float2* __restrict__ win_part, int part_stride) {
+  using RG = WinRing<NJT>;
+  constexpr int ST = RG::ST;
   extern __shared__ __align__(16) float sm[];
-  float* sA = sm;                    // [WD_BK][WD_SA]   mask chunk, transposed
-  float* sB = sA + WD_BK * WD_SA;    // [WD_BK][NJT]     column twiddles of the chunk
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rb = blockIdx.x, cs = blockIdx.y, img = blockIdx.z;
   const int colSplits = gridDim.y;
@@ -106,6 +134,35 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
   const int ch0 = (int)((long long)nch * cs / colSplits);
   const int ch1 = (int)((long long)nch * (cs + 1) / colSplits);
   const float* M = masks + (size_t)img * Lx * Ly;
+  auto sA = [&](int st) { return sm + (size_t)st * RG::STAGE_F; };        // [WD_BM][WD_SA]
+  auto sB = [&](int st) { return sm + (size_t)st * RG::STAGE_F + RG::A_F; };  // [WD_BK][NJT]
+
+  // chunk ch into ring slot st: 128 rows x 32 columns (four 16-byte pieces a thread) and
+  // the chunk's twiddle rows (NJT / 4 pieces per column)
+  auto issue = [&](int ch, int st) {
+    const int x0 = ch * WD_BK;
+    float* a = sA(st);
+#pragma unroll
+    for (int i = 0; i < WD_BM * WD_BK / 4 / WD_THREADS; ++i) {
+      const int idx = tid + WD_THREADS * i, row = idx >> 3, c4 = (idx & 7) * 4;
+      const int y = y0 + row, x = x0 + c4;
+      const bool rok = y < Ly;
+      const float* src = M + (size_t)(rok ? y : 0) * Lx;
+      float* dst = a + row * WD_SA + c4;
+      if (VEC) {
+        wd_cp16(dst, src + (rok && x < Lx ? x : 0), rok && x < Lx);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) wd_cp4(dst + e, src + (rok && x + e < Lx ? x + e : 0), rok && x + e < Lx);
+      }
+    }
+    constexpr int Q = NJT / 4;
+    float* b = sB(st);
+    for (int idx = tid; idx < WD_BK * Q; idx += WD_THREADS) {
+      const int kr = idx / Q, c = idx - kr * Q, x = x0 + kr;
+      wd_cp16(b + 4 * idx, twx + (size_t)(x < Lx ? x : 0) * NJT + 4 * c, x < Lx);
+    }
+  };
 
   // accumulators in column pairs: one packed (f32x2) FMA updates two twiddle columns, each
   // lane rounding as fmaf does
@@ -116,75 +173,45 @@ __global__ void __launch_bounds__(WD_THREADS) win_dft_kernel(const float* __rest
     for (int j = 0; j < NJT / 2; ++j) acc2[i][j] = make_float2(0.f, 0.f);
   auto acc = [&](int i, int j) -> float& { return (j & 1) ? acc2[i][j >> 1].y : acc2[i][j >> 1].x; };
 
-  float4 ra[8];
-  const int lc4 = (tid & 15) * 4;
-  const int lr = tid >> 4;
-  auto loadA = [&](int ch) {
-    const int x0 = ch * WD_BK + lc4;
+  // one commit group per ring step (empty past the last chunk), so that waiting for all
+  // but the newest ST - 2 groups means the current stage has landed
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int row = y0 + lr + 16 * i;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row < Ly) {
-        const float* p = M + (size_t)row * Lx + x0;
-        if (VEC && x0 + 3 < Lx) {
-          v = __ldcs(reinterpret_cast<const float4*>(p));
-        } else {
-          if (x0 + 0 < Lx) v.x = p[0];
-          if (x0 + 1 < Lx) v.y = p[1];
-          if (x0 + 2 < Lx) v.z = p[2];
-          if (x0 + 3 < Lx) v.w = p[3];
-        }
-      }
-      ra[i] = v;
-    }
-  };
-
-  if (ch0 < ch1) loadA(ch0);
+  for (int k = 0; k < ST - 1; ++k) {
+    if (ch0 + k < ch1) issue(ch0 + k, k);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   for (int ch = ch0; ch < ch1; ++ch) {
-    __syncthreads();
+    const int it = ch - ch0, st = it % ST;
+    asm volatile("cp.async.wait_group %0;" ::"n"(ST - 2) : "memory");
+    __syncthreads();  // the stage is visible to all; every warp is done with the previous one
+    if (ch + ST - 1 < ch1) issue(ch + ST - 1, (it + ST - 1) % ST);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    const float* a = sA(st) + lane * WD_SA + 4 * warp;
+    float4 av[4];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int r = lr + 16 * i;
-      sA[(lc4 + 0) * WD_SA + r] = ra[i].x;
-      sA[(lc4 + 1) * WD_SA + r] = ra[i].y;
-      sA[(lc4 + 2) * WD_SA + r] = ra[i].z;
-      sA[(lc4 + 3) * WD_SA + r] = ra[i].w;
-    }
-    {
-      const float4* T4 = reinterpret_cast<const float4*>(twx);
-      float4* sB4 = reinterpret_cast<float4*>(sB);
-      const int q = NJT / 4;
-      for (int idx = tid; idx < WD_BK * q; idx += WD_THREADS) {
-        const int kr = idx / q, c = idx - kr * q;
-        const int x = ch * WD_BK + kr;
-        sB4[idx] = x < Lx ? T4[(size_t)x * q + c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < 4; ++i) av[i] = *reinterpret_cast<const float4*>(a + 32 * i * WD_SA);
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const float4* b4 = reinterpret_cast<const float4*>(sB(st) + (4 * warp + kk) * NJT);
+      float2 ai[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float v = kk == 0 ? av[i].x : kk == 1 ? av[i].y : kk == 2 ? av[i].z : av[i].w;
+        ai[i] = make_float2(v, v);
       }
-    }
-    __syncthreads();
-    if (ch + 1 < ch1) loadA(ch + 1);
-#pragma unroll 2
-    for (int kk = 0; kk < WD_BK / 8; ++kk) {
-      const int k = warp * (WD_BK / 8) + kk;
-      const float* a = sA + k * WD_SA + lane;
-      const float2 a0 = make_float2(a[0], a[0]), a1 = make_float2(a[32], a[32]);
-      const float2 a2 = make_float2(a[64], a[64]), a3 = make_float2(a[96], a[96]);
-      const float4* b4 = reinterpret_cast<const float4*>(sB + k * NJT);
 #pragma unroll
       for (int c = 0; c < NJT / 4; ++c) {
         const float4 b = b4[c];
         const float2 blo = make_float2(b.x, b.y), bhi = make_float2(b.z, b.w);
-        acc2[0][2 * c] = __ffma2_rn(a0, blo, acc2[0][2 * c]);
-        acc2[1][2 * c] = __ffma2_rn(a1, blo, acc2[1][2 * c]);
-        acc2[2][2 * c] = __ffma2_rn(a2, blo, acc2[2][2 * c]);
-        acc2[3][2 * c] = __ffma2_rn(a3, blo, acc2[3][2 * c]);
-        acc2[0][2 * c + 1] = __ffma2_rn(a0, bhi, acc2[0][2 * c + 1]);
-        acc2[1][2 * c + 1] = __ffma2_rn(a1, bhi, acc2[1][2 * c + 1]);
-        acc2[2][2 * c + 1] = __ffma2_rn(a2, bhi, acc2[2][2 * c + 1]);
-        acc2[3][2 * c + 1] = __ffma2_rn(a3, bhi, acc2[3][2 * c + 1]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          acc2[i][2 * c] = __ffma2_rn(ai[i], blo, acc2[i][2 * c]);
+          acc2[i][2 * c + 1] = __ffma2_rn(ai[i], bhi, acc2[i][2 * c + 1]);
+        }
       }
     }
   }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
 
   // tree reduction of the 8 k-split warps: red[w][j][r], r fastest (conflict free)
@@ -1213,9 +1240,7 @@ template <int NJT>
 static int launch_win_dft_t(litho_ctx* ctx, const ImgPlan& p, const float* masks, const float* twx,
                             float2* win_part) {
   const ImgGeom& g = p.g;
-  const size_t main_sm = (size_t)(WD_BK * WD_SA + WD_BK * NJT) * sizeof(float);
-  const size_t red_sm = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(g.Ny + 1) * WD_BM * sizeof(float2);
-  const size_t smem = std::max(main_sm, red_sm);
+  const size_t smem = win_dft_smem<NJT>(g.Ny);
   dim3 grid(p.rowBlocks, p.colSplits, p.batch);
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
   if ((g.Lx & 3) == 0) {
@@ -1384,9 +1409,7 @@ template <int NJT>
 static cudaError_t noctx_win_dft_t(cudaStream_t s, const ImgPlan& p, const float* masks, const float* twx,
                                    float2* win_part) {
   const ImgGeom& g = p.g;
-  const size_t main_sm = (size_t)(WD_BK * WD_SA + WD_BK * NJT) * sizeof(float);
-  const size_t red_sm = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(g.Ny + 1) * WD_BM * sizeof(float2);
-  const size_t smem = std::max(main_sm, red_sm);
+  const size_t smem = win_dft_smem<NJT>(g.Ny);
   dim3 grid(p.rowBlocks, p.colSplits, p.batch);
   auto k = (g.Lx & 3) == 0 ? win_dft_kernel<NJT, true> : win_dft_kernel<NJT, false>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
