@@ -1006,35 +1006,45 @@ int fi_twiddles(litho_ctx* ctx, const ImgGeom& g, const float2** out) {
 // ---------------------------------------------------------------------------
 // FI, step 2: image = Cy (Ly x KB) * Tm (KB x Lx), KB = 4Ny+1.
 // ---------------------------------------------------------------------------
-constexpr int FO_BM = 64, FO_BN = 128, FO_THREADS = 256;
+constexpr int FO_BM = 32, FO_BN = 128, FO_THREADS = 256;
 
-// Cy[r][Y] for r < 4Ny+1 (r = 0: 1; 1..2Ny: 2cos(2 pi r y'/Fy); 2Ny+1..4Ny: -2sin of r-2Ny),
-// rows Y padded to Lyp (a multiple of FO_BM).  The FI kernel evaluates the same values
-// when it has no table (the allocation-free entry point).
-__device__ __forceinline__ float fo_cy(int r, int Y, int Ly, int Fy, int Ny) {
+// The rows pair up around the centre: with y' = Y + oy (oy = (Fy-Ly)/2 - Fy/2) the image is
+//   image(+b) = A(b) + B(b),  image(-b) = A(b) - B(b),
+//   A(b) = T0 + sum_{r=1..2Ny} 2cos(2 pi r b/Fy) Re T_r,  B(b) = sum_r -2sin(2 pi r b/Fy) Im T_r,
+// so one set of sums over the 4Ny+1 rows of Tm serves rows +b and -b.  Cm[r][b] holds the
+// coefficients of base row b (r = 0: 1; 1..2Ny: 2cos; 2Ny+1..4Ny: -2sin), b < nbp (the
+// base rows |y'| rounded up to FO_BM).  The FI kernel evaluates the same values when it
+// has no table (the allocation-free entry point).
+__device__ __forceinline__ float fo_cm(int r, int b, int Fy, int Ny) {
   if (r == 0) return 1.f;
-  const long long yp = (long long)Y + (long long)(Fy - Ly) / 2 - Fy / 2;
   const int dy = r <= 2 * Ny ? r : r - 2 * Ny;
-  const float2 e = cis_exact((long long)dy * yp, Fy, 1.f);
+  const float2 e = cis_exact((long long)dy * b, Fy, 1.f);
   return r <= 2 * Ny ? 2.f * e.x : -2.f * e.y;
 }
 
-__global__ void fo_cy_init_kernel(float* __restrict__ cy, int Ly, int Lyp, int Fy, int Ny) {
-  const int Y = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
-  if (Y < Lyp) cy[(size_t)r * Lyp + Y] = fo_cy(r, Y, Ly, Fy, Ny);
+__global__ void fo_cm_init_kernel(float* __restrict__ cm, int nbp, int Fy, int Ny) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (b < nbp) cm[(size_t)r * nbp + b] = fo_cm(r, b, Fy, Ny);
 }
 
-// the Cy table of a geometry, cached per (Ly, Fy, Ny) on the context
-static int fo_cy_table(litho_ctx* ctx, const ImgGeom& g, const float** out, int* Lyp) {
-  *Lyp = (g.Ly + FO_BM - 1) / FO_BM * FO_BM;
-  auto key = std::make_tuple(g.Ly, g.Fy, g.Ny, -5000);
+// base rows of a geometry: b = 0 .. max |y'| over the image rows
+__host__ __device__ inline int fo_nbase(int Ly, int Fy) {
+  const long long oy = (long long)(Fy - Ly) / 2 - Fy / 2;
+  const long long lo = oy < 0 ? -oy : oy, hi = oy + Ly - 1 < 0 ? -(oy + Ly - 1) : oy + Ly - 1;
+  return (int)(lo > hi ? lo : hi) + 1;
+}
+
+// the Cm table of a geometry, cached per (Ly, Fy, Ny) on the context
+static int fo_cm_table(litho_ctx* ctx, const ImgGeom& g, const float** out, int* nbp) {
+  *nbp = (fo_nbase(g.Ly, g.Fy) + FO_BM - 1) / FO_BM * FO_BM;
+  auto key = std::make_tuple(g.Ly, g.Fy, g.Ny, -5001);
   auto it = ctx->twx_tables.find(key);
   if (it == ctx->twx_tables.end()) {
     const int KB = 4 * g.Ny + 1;
     DevBuf b;
-    LITHO_RET(b.ensure(ctx, (size_t)KB * *Lyp * sizeof(float)));
+    LITHO_RET(b.ensure(ctx, (size_t)KB * *nbp * sizeof(float)));
     StageScope sc(ctx, LITHO_STAGE_UPLOAD);
-    fo_cy_init_kernel<<<dim3(*Lyp / FO_BM, KB), FO_BM, 0, ctx->stream>>>(b.as<float>(), g.Ly, *Lyp, g.Fy, g.Ny);
+    fo_cm_init_kernel<<<dim3(*nbp / FO_BM, KB), FO_BM, 0, ctx->stream>>>(b.as<float>(), *nbp, g.Fy, g.Ny);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
     it = ctx->twx_tables.emplace(key, b).first;
   }
@@ -1042,66 +1052,87 @@ static int fo_cy_table(litho_ctx* ctx, const ImgGeom& g, const float** out, int*
   return LITHO_OK;
 }
 
+// One CTA per (FO_BM base rows, FO_BN columns, image): thread (warp w, lane l) sums base
+// rows 4w..4w+3 over columns 4l..4l+3, the cos rows of Tm into A and the sin rows into B
+// (packed f32x2 FMAs), and writes A + B to row +b and A - B to row -b where they lie in
+// the image.
 template <bool VEC>
 __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restrict__ tm, int Lx, int Ly, int Fy,
-                                                            int Ny, const float* __restrict__ cyt, int Lyp,
+                                                            int Ny, const float* __restrict__ cmt, int nbp,
                                                             float* __restrict__ images) {
   extern __shared__ __align__(16) float fo[];
   const int KB = 4 * Ny + 1;
   float* sC = fo;                // [KB][FO_BM]
   float* sT = fo + KB * FO_BM;   // [KB][FO_BN]
-  const int tid = threadIdx.x;
-  const int X0 = blockIdx.x * FO_BN, Y0 = blockIdx.y * FO_BM, img = blockIdx.z;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int X0 = blockIdx.x * FO_BN, B0 = blockIdx.y * FO_BM, img = blockIdx.z;
   const float* T = tm + (size_t)img * KB * Lx;
-  for (int idx = tid; idx < KB * FO_BN; idx += FO_THREADS) {
-    const int r = idx / FO_BN, c = idx - r * FO_BN;
-    const int X = X0 + c;
-    sT[idx] = X < Lx ? T[(size_t)r * Lx + X] : 0.f;
+  if (VEC) {
+    for (int idx = tid; idx < KB * (FO_BN / 4); idx += FO_THREADS) {
+      const int r = idx / (FO_BN / 4), c4 = 4 * (idx - r * (FO_BN / 4));
+      const int X = X0 + c4;
+      reinterpret_cast<float4*>(sT)[idx] =
+          X < Lx ? __ldg(reinterpret_cast<const float4*>(T + (size_t)r * Lx + X)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  } else {
+    for (int idx = tid; idx < KB * FO_BN; idx += FO_THREADS) {
+      const int r = idx / FO_BN, c = idx - r * FO_BN;
+      const int X = X0 + c;
+      sT[idx] = X < Lx ? T[(size_t)r * Lx + X] : 0.f;
+    }
   }
-  if (cyt != nullptr) {  // the cached table: whole 16-byte pieces of the tile's rows
+  if (cmt != nullptr) {  // the cached table: whole 16-byte pieces of the tile's base rows
     for (int idx = tid; idx < KB * (FO_BM / 4); idx += FO_THREADS) {
       const int r = idx / (FO_BM / 4), q = idx - r * (FO_BM / 4);
-      reinterpret_cast<float4*>(sC)[idx] = __ldg(reinterpret_cast<const float4*>(cyt + (size_t)r * Lyp + Y0) + q);
+      reinterpret_cast<float4*>(sC)[idx] = __ldg(reinterpret_cast<const float4*>(cmt + (size_t)r * nbp + B0) + q);
     }
   } else {
     for (int idx = tid; idx < KB * FO_BM; idx += FO_THREADS) {
-      const int r = idx / FO_BM, rr = idx - r * FO_BM;
-      sC[idx] = fo_cy(r, Y0 + rr, Ly, Fy, Ny);
+      const int r = idx / FO_BM, bb = idx - r * FO_BM;
+      sC[idx] = fo_cm(r, B0 + bb, Fy, Ny);
     }
   }
   __syncthreads();
-  const int ty = tid >> 4, tx = tid & 15;
-  // accumulators in column pairs: one packed (f32x2) FMA per pair, each lane rounding as fmaf
-  float2 acc[4][4];
+  // A and B of 4 base rows x 4 columns, in column pairs
+  float2 A[4][2], Bs[4][2];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
-#pragma unroll 4
-  for (int r = 0; r < KB; ++r) {
-    const float4 c = *reinterpret_cast<const float4*>(sC + r * FO_BM + 4 * ty);
-    const float4 t0 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 4 * tx);
-    const float4 t1 = *reinterpret_cast<const float4*>(sT + r * FO_BN + 64 + 4 * tx);
+    for (int j = 0; j < 2; ++j) A[i][j] = Bs[i][j] = make_float2(0.f, 0.f);
+  auto step = [&](int r, float2(&acc)[4][2]) {
+    const float4 c = *reinterpret_cast<const float4*>(sC + r * FO_BM + 4 * warp);  // one address per warp
+    const float4 t = *reinterpret_cast<const float4*>(sT + r * FO_BN + 4 * lane);
     const float cc[4] = {c.x, c.y, c.z, c.w};
-    const float2 tt[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
-                          make_float2(t1.z, t1.w)};
+    const float2 tlo = make_float2(t.x, t.y), thi = make_float2(t.z, t.w);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const float2 ci = make_float2(cc[i], cc[i]);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = __ffma2_rn(ci, tt[j], acc[i][j]);
+      acc[i][0] = __ffma2_rn(ci, tlo, acc[i][0]);
+      acc[i][1] = __ffma2_rn(ci, thi, acc[i][1]);
     }
-  }
+  };
+#pragma unroll 4
+  for (int r = 0; r <= 2 * Ny; ++r) step(r, A);
+#pragma unroll 4
+  for (int r = 2 * Ny + 1; r < KB; ++r) step(r, Bs);
+  const int oy = (Fy - Ly) / 2 - Fy / 2;
+  const int nbase = fo_nbase(Ly, Fy);
   float* O = images + (size_t)img * Lx * Ly;
+  const int X = X0 + 4 * lane;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int Y = Y0 + 4 * ty + i;
-    if (Y >= Ly) continue;
-    float* row = O + (size_t)Y * Lx;
+    const int b = B0 + 4 * warp + i;
+    if (b >= nbase) continue;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int X = X0 + 64 * h + 4 * tx;
-      const float o[4] = {acc[i][2 * h].x, acc[i][2 * h].y, acc[i][2 * h + 1].x, acc[i][2 * h + 1].y};
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      if (sgn == 1 && b == 0) continue;  // y' = 0 has no mirror
+      const int Y = (sgn == 0 ? b : -b) - oy;
+      if (Y < 0 || Y >= Ly) continue;
+      const float o[4] = {sgn == 0 ? A[i][0].x + Bs[i][0].x : A[i][0].x - Bs[i][0].x,
+                          sgn == 0 ? A[i][0].y + Bs[i][0].y : A[i][0].y - Bs[i][0].y,
+                          sgn == 0 ? A[i][1].x + Bs[i][1].x : A[i][1].x - Bs[i][1].x,
+                          sgn == 0 ? A[i][1].y + Bs[i][1].y : A[i][1].y - Bs[i][1].y};
+      float* row = O + (size_t)Y * Lx;
       if (VEC && X + 3 < Lx) {
         __stcs(reinterpret_cast<float4*>(row + X), make_float4(o[0], o[1], o[2], o[3]));
       } else {
@@ -1111,6 +1142,12 @@ __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restr
       }
     }
   }
+}
+
+// launch geometry of the FI output kernel
+static inline dim3 fo_grid(const ImgGeom& g, int batch) {
+  const int nb = fo_nbase(g.Ly, g.Fy);
+  return dim3((g.Lx + FO_BN - 1) / FO_BN, (nb + FO_BM - 1) / FO_BM, batch);
 }
 
 // ---------------------------------------------------------------------------
@@ -1334,15 +1371,14 @@ int run_fi(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tm,
   }
   {
     const int KB = 4 * g.Ny + 1;
-    int Lyp = 0;
-    const float* cyt = nullptr;
-    LITHO_RET(fo_cy_table(ctx, g, &cyt, &Lyp));
+    int nbp = 0;
+    const float* cmt = nullptr;
+    LITHO_RET(fo_cm_table(ctx, g, &cmt, &nbp));
     const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);
-    dim3 grid((g.Lx + FO_BN - 1) / FO_BN, (g.Ly + FO_BM - 1) / FO_BM, p.batch);
     StageScope sc(ctx, LITHO_STAGE_FI_OUT);
     auto k = (g.Lx & 3) == 0 ? fi_out_kernel<true> : fi_out_kernel<false>;
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, cyt, Lyp, images);
+    k<<<fo_grid(g, p.batch), FO_THREADS, smem, ctx->stream>>>(tm, g.Lx, g.Ly, g.Fy, g.Ny, cmt, nbp, images);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
   }
   return LITHO_OK;
@@ -1480,7 +1516,7 @@ cudaError_t image_pipeline_noctx(cudaStream_t s, const ImgPlan& p, const float* 
   {
     const int KB = 4 * g.Ny + 1;
     const size_t smem = (size_t)KB * (FO_BM + FO_BN) * sizeof(float);
-    dim3 grid((g.Lx + FO_BN - 1) / FO_BN, (g.Ly + FO_BM - 1) / FO_BM, 1);
+    const dim3 grid = fo_grid(g, 1);
     auto k = (g.Lx & 3) == 0 ? fi_out_kernel<true> : fi_out_kernel<false>;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
       return e;
