@@ -99,6 +99,22 @@ inline int band_tcc_chunks(int Nx, int Ny) {
   return 0;
 }
 
+// Expected band-stage time (us) of each form for `batch` images of a kernel set, fitted to
+// GB300 measurements (1024^2 and 512^2 masks, K = 8 / 24 / 48, 64-1024 images; mixed form).
+// The TCC form costs ~20 us (28 when its table is cut into chunks) plus 0.6 ps (1.1 ps) per
+// window pair (p, q) with fy >= 0 and image; the FFT form ~10 us (29 on the 128 grid) plus
+// 4.2 / 6.8 / 42 ns per kernel and image on the 32 / 64 / 128 conv grids.  LITHO_BAND_AUTO
+// takes the TCC form where it is expected to be faster: at K = 24 and 256 masks for
+// Nx = Ny <= 10 and at 16 (where the FFT form needs the 128 grid), not for 11..15.
+inline double band_tcc_cost_us(int Nx, int Ny, int nc, int batch) {
+  const double KX = 2 * Nx + 1, KY = 2 * Ny + 1, pairs = KY * (KY + 1) / 2 * KX * KX;
+  return nc > 1 ? 28.0 + 1.1e-6 * pairs * batch : 20.0 + 0.6e-6 * pairs * batch;
+}
+inline double band_fft_cost_us(int convN, int nk, int batch) {
+  const double per = convN <= 32 ? 4.2e-3 : convN <= 64 ? 6.8e-3 : 42e-3;
+  return (convN >= 128 ? 29.0 : 10.0) + per * nk * batch;
+}
+
 inline size_t band_tcc_entries(int Nx, int Ny, int nc) {
   size_t n = 0;
   for (int b = 0; b < (Ny + 1) * nc; ++b) n += (size_t)bt_task_shape(b, Nx, Ny, nc).size;

@@ -245,6 +245,13 @@ static decltype(&band_tcc_kernel<1>) band_kernel_for(int Nx) {
   }
 }
 
+bool use_band_tcc(const litho_ctx* ctx, const litho_kernel_set* ks, int batch) {
+  if (!band_tcc_available(ctx, ks)) return false;
+  if (ctx->band_method == LITHO_BAND_TCC) return true;
+  const int convN = default_conv_n(ks->Nx, ks->Ny);
+  return band_tcc_cost_us(ks->Nx, ks->Ny, ks->band_nc, batch) <= band_fft_cost_us(convN, ks->nk, batch);
+}
+
 // Build the T table of a kernel set (krn/scales on the device) on `stream`.
 int build_band_table(litho_ctx* ctx, litho_kernel_set* ks, cudaStream_t stream) {
   ks->band_nc = 0;

@@ -183,7 +183,7 @@ static int time_class(litho_batch_plan* bp, int ci, float* ms, int reps = 3) {
 
 static int tune_class(litho_batch_plan* bp, int ci) {
   ClassRun& c = bp->classes[ci];
-  const bool band_ok = use_band_tcc(bp->ctx, c.ks);
+  const bool band_ok = band_tcc_available(bp->ctx, c.ks);
   const int method = band_ok ? (bp->ctx->band_method == LITHO_BAND_TCC ? 2 : 1) : 0;
   const TuneKey key{c.L, c.ks->Nx, c.ks->nk, c.count, bp->precision, method};
   auto it = g_tune_cache.find(key);

@@ -1543,7 +1543,7 @@ int image_pipeline(litho_ctx* ctx, const ImgGeom& g, int batch, const float* mas
                    float* images, int precision) {
   const int KY = 2 * g.Ny + 1;
   const bool tc = precision == LITHO_PREC_MIXED && tc_supported(g);
-  const bool band = use_band_tcc(ctx, ks);
+  const bool band = use_band_tcc(ctx, ks, batch);
   ImgPlan p = tc ? mixed_plan(g, batch, ctx->sm_count) : make_plan(g, batch, ctx->sm_count);
   if (band) {
     p.ngroups = ks->band_nc;

@@ -240,10 +240,13 @@ int build_band_table(litho_ctx* ctx, litho_kernel_set* ks, cudaStream_t stream);
 size_t band_wsum_bytes(const ImgGeom& g, int batch);
 int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const litho_kernel_set* ks,
                  float2* wsum, float2* band_part);
-// whether a kernel set's images take the TCC band under the context's band method
-inline bool use_band_tcc(const litho_ctx* ctx, const litho_kernel_set* ks) {
+// whether the TCC band may serve a kernel set under the context's band method
+inline bool band_tcc_available(const litho_ctx* ctx, const litho_kernel_set* ks) {
   return ks->band_nc > 0 && ctx->band_method != LITHO_BAND_FFT;
 }
+// whether a batch of images takes the TCC band: LITHO_BAND_TCC wherever the table exists,
+// LITHO_BAND_AUTO where the band cost model (band_sched.hpp) expects it to be faster
+bool use_band_tcc(const litho_ctx* ctx, const litho_kernel_set* ks, int batch);
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);

@@ -316,8 +316,9 @@ class Context:
         self._check(_lib.litho_ctx_set_test_stall(self.h, int(chunk)))
 
     def set_band_method(self, method: int):
-        """BAND_AUTO (default: the TCC form where the kernel set has its table), BAND_FFT (per
-        kernel FFTs on the conv grid) or BAND_TCC (litho_ctx_set_band_method)."""
+        """BAND_AUTO (default: per batch, the form a cost model fitted on GB300 expects to be
+        faster), BAND_FFT (per kernel FFTs on the conv grid) or BAND_TCC (the TCC bilinear form
+        wherever the kernel set has its table) (litho_ctx_set_band_method)."""
         self._check(_lib.litho_ctx_set_band_method(self.h, int(method)))
 
     def set_host_chunk(self, nbytes: int = 0):

@@ -69,8 +69,10 @@ extern "C" {
  *                  T(p, q) = sum_k s_k K_k(p) conj(K_k(q)) over the kernel window,
  *                  band(f) = sum_{p-q=f} M(p) conj(M(q)) T(p, q); T is built once
  *                  per kernel set (FP64 sums, rounded to FP32), the sums in FP32.
- * LITHO_BAND_AUTO: TCC where the kernel set has a table (1 <= Nx <= 16, Ny <= 16),
- *                  FFT otherwise (the default).                                  */
+ * LITHO_BAND_AUTO: per batch, the form a cost model fitted on GB300 expects to be
+ *                  faster (TCC only where the kernel set has a table: 1 <= Nx <= 16,
+ *                  Ny <= 16).  At K = 24 and 256 masks: TCC for Nx = Ny <= 10 and
+ *                  16, FFT for 11..15 and for small batches (the default).         */
 #define LITHO_BAND_AUTO 0
 #define LITHO_BAND_FFT  1
 #define LITHO_BAND_TCC  2

@@ -82,8 +82,15 @@ static int check(int Nx, int Ny) {
   std::printf("ok %d %zu\n", nc, want);
   return 0;
 }
-int main() {
+int main(int argc, char** argv) {
   int Nx, Ny;
+  if (argc > 1) {  // band cost model: "Nx Ny nk convN batch" -> 1 where the TCC form is cheaper
+    int nk, convN, batch;
+    while (std::scanf("%d %d %d %d %d", &Nx, &Ny, &nk, &convN, &batch) == 5)
+      std::printf("%d\n", band_tcc_cost_us(Nx, Ny, band_tcc_chunks(Nx, Ny), batch) <=
+                               band_fft_cost_us(convN, nk, batch) ? 1 : 0);
+    return 0;
+  }
   while (std::scanf("%d %d", &Nx, &Ny) == 2)
     if (check(Nx, Ny)) return 1;
   return 0;
@@ -128,3 +135,25 @@ def test_chunking_of_the_metric_optics(driver):
     (a, b) = [ln.split() for ln in r.stdout.split("\n") if ln]
     assert a[1] == "1"
     assert 2 < int(b[1]) <= 16
+
+
+def _conv(nx, ny):
+    n = 32
+    while n < 4 * max(nx, ny) + 1:
+        n *= 2
+    return n
+
+
+def test_auto_band_cost_model(driver):
+    # (Nx, K, masks) -> TCC form expected faster, from band-stage timings on GB300 (mixed
+    # form, 1024^2 masks): TCC 23.5 / FFT 50.3 us at Nx = 8, K = 24, 256 masks; 50.8 / 51.3
+    # at Nx = 10; 87.4 / 53.5 at Nx = 12; 205 / 55.4 at Nx = 15; 236 / 287 at Nx = 16 (FFT on the
+    # 128 grid); 236 / 121 at Nx = 16, K = 8; 23 / 88 at Nx = 8, K = 48; 43 / 143 at Nx = 8,
+    # K = 24, 1024 masks; 24.0 / 20.9 at Nx = 8, K = 24, 64 masks
+    cases = [((8, 24, 256), 1), ((12, 24, 256), 0), ((15, 24, 256), 0), ((16, 24, 256), 1),
+             ((16, 8, 256), 0), ((8, 48, 256), 1), ((8, 24, 1024), 1), ((8, 24, 64), 0),
+             ((12, 48, 256), 1), ((4, 24, 256), 1)]
+    inp = "".join(f"{nx} {nx} {k} {_conv(nx, nx)} {b}\n" for (nx, k, b), _ in cases)
+    r = subprocess.run([driver, "model"], input=inp, capture_output=True, text=True, check=True)
+    got = [int(x) for x in r.stdout.split()]
+    assert got == [w for _, w in cases], list(zip([c for c, _ in cases], got))

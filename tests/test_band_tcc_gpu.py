@@ -97,11 +97,34 @@ def test_tcc_band_mixed(ctx, case):
         assert R.rel_l2(got[i], r) < MIXED_TOL, (case["name"], i)
 
 
-def test_default_is_tcc_band_where_available(ctx, case):
+def test_default_takes_one_of_the_two_forms(ctx, case):
     import litho_gb300 as L
     auto = _run(ctx, case, L.BAND_AUTO, L.PREC_FP32)
     tcc = _run(ctx, case, L.BAND_TCC, L.PREC_FP32)
-    assert np.array_equal(auto, tcc)
+    fft = _run(ctx, case, L.BAND_FFT, L.PREC_FP32)
+    assert np.array_equal(auto, tcc) or np.array_equal(auto, fft)
+
+
+def test_default_is_tcc_band_for_large_batches_at_nx8(ctx):
+    # 256 masks of 1024^2 with the metric's Nx = 8, K = 24: the cost model takes the TCC form
+    import torch
+    import litho_gb300 as L
+    from litho_gb300 import synth
+    krn, scales, nx, ny = _kernels(synth.quasar_source(2000)[0], 1024, 1024, 24)
+    assert nx == 8
+    m = torch.from_numpy(np.stack([synth.density_rect_mask(1024, 0.3 + 0.001 * i, seed=200 + i)
+                                   for i in range(4)]).astype(np.float32)).cuda().repeat(64, 1, 1)
+    outs = {}
+    ks = ctx.kernel_set(krn, scales, nx, ny)
+    try:
+        for name, meth in (("auto", L.BAND_AUTO), ("tcc", L.BAND_TCC)):
+            ctx.set_band_method(meth)
+            outs[name] = ctx.image_batch(ks, m, precision=L.PREC_MIXED)
+            ctx.synchronize()
+    finally:
+        ctx.set_band_method(L.BAND_AUTO)
+        ks.close()
+    assert torch.equal(outs["auto"], outs["tcc"])
 
 
 @pytest.mark.parametrize("prec_name,tol", [("fp32", PLAIN_TOL), ("mixed", MIXED_TOL)])
