@@ -98,8 +98,9 @@ struct WinRing {
 template <int NJT>
 static size_t win_dft_smem(int Ny) {
   const size_t ring = (size_t)WinRing<NJT>::ST * WinRing<NJT>::STAGE_F * sizeof(float);
-  const size_t red = (size_t)4 * NJT * WD_BM * sizeof(float) + (size_t)(Ny + 1) * WD_BM * sizeof(float2);
-  return std::max(ring, red);
+  const size_t tree = (size_t)4 * NJT * WD_BM * sizeof(float);  // the k-split warps' sums
+  const size_t rows = (size_t)NJT * (WD_BM + 4) * sizeof(float) + (size_t)(Ny + 1) * (WD_BM + 2) * sizeof(float2);
+  return std::max(ring, std::max(tree, rows));
 }
 
 __device__ __forceinline__ void wd_cp16(float* dst, const float* src, bool ok) {
@@ -234,19 +235,22 @@ __global__ void __launch_bounds__(WD_THREADS, WinRing<NJT>::CTAS) win_dft_kernel
     }
     __syncthreads();
   }
-  float* sR = red;  // [NJT][WD_BM] row transforms of this block
+  // row transforms of this block and the row twiddles, rows padded (132 floats, 130 float2)
+  // so that the threads of a warp (different u, |v|) read different banks
+  constexpr int RS = WD_BM + 4, RT = WD_BM + 2;
+  float* sR = red;  // [NJT][RS]
   if (warp == 0) {
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < NJT; ++j) sR[j * WD_BM + lane + 32 * i] = acc(i, j);
+      for (int j = 0; j < NJT; ++j) sR[j * RS + lane + 32 * i] = acc(i, j);
   }
   // row twiddles e^{-2 pi i v y'/Fy}, v = 0..Ny
-  float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NJT * WD_BM);
+  float2* sRT = reinterpret_cast<float2*>(sm + (size_t)NJT * RS);  // [Ny+1][RT]
   const int oyc = (Fy - Ly) / 2 - Fy / 2;
   for (int idx = tid; idx < (Ny + 1) * WD_BM; idx += WD_THREADS) {
     const int v = idx / WD_BM, r = idx - v * WD_BM;
-    sRT[idx] = cis_exact((long long)v * (y0 + r + oyc), Fy, -1.f);
+    sRT[v * RT + r] = cis_exact((long long)v * (y0 + r + oyc), Fy, -1.f);
   }
   __syncthreads();
 
@@ -261,9 +265,9 @@ __global__ void __launch_bounds__(WD_THREADS, WinRing<NJT>::CTAS) win_dft_kernel
     const int v = vi - Ny;
     const int av = v < 0 ? -v : v;
     const float ts = v < 0 ? -1.f : 1.f;
-    const float* rc = sR + u * WD_BM;
-    const float* rs = sR + (Nx + u) * WD_BM;
-    const float2* rt = sRT + av * WD_BM;
+    const float* rc = sR + u * RS;
+    const float* rs = sR + (Nx + u) * RS;
+    const float2* rt = sRT + av * RT;
     float re = 0.f, im = 0.f;
     if (u == 0) {
 #pragma unroll 4
