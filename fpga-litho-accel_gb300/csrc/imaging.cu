@@ -11,17 +11,18 @@
 //   win_dft_kernel : W[v][u] = 1/(FxFy) sum_{y,x} m[y][x] e^{-2 pi i (u x'/Fx + v y'/Fy)}
 //                    (x' = x + (Fx-Lx)/2 - Fx/2).  A separable partial DFT: the
 //                    column stage is a 128 x Lx x (2Nx+1) FP32 contraction per CTA
-//                    with the mask tile staged in shared memory, the row stage a
-//                    small complex contraction in the epilogue.  HBM: one read of
-//                    the mask.
+//                    with the mask chunks streamed through a cp.async ring in
+//                    shared memory, the row stage a small complex contraction in
+//                    the epilogue.  HBM: one read of the mask.
 //   socs_kernel    : per kernel k, embed K_k*W in an N x N grid, 2-D inverse FFT
 //                    (warp-shuffle radix-2, fft_warp.cuh), accumulate s_k|E|^2 in
 //                    registers; then a forward FFT of the intensity and the
 //                    |f| <= 2N band S[fy][fx] / N^2 is written out.
 //   fi_rows_kernel : T[fy][X] = sum_fx S[fy][fx] e^{+2 pi i fx x'/Fx}   (fy >= 0)
 //   fi_out_kernel  : image[Y][X] = T0 + 2 sum_{fy>0} Re(e^{2 pi i fy y'/Fy} T[fy][X]),
-//                    a rank-(4Ny+1) FP32 contraction written once with 16-byte
-//                    streaming stores.  HBM: one write of the image.
+//                    a rank-(4Ny+1) FP32 contraction whose cos and sin halves give
+//                    rows +y' and -y' from one set of sums, written once with
+//                    16-byte streaming stores.  HBM: one write of the image.
 // With C2R's Hermitian completion and the two rolls of litho.cpp:934 and
 // litho.cpp:700, that is exactly FI's zero-padded interpolation followed by
 // crop2DCentered (litho.cpp:164-177, 997-1001).
