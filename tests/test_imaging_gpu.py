@@ -164,6 +164,24 @@ def test_non_power_of_two_and_rectangular(ctx, golden_optics, golden_kernels):
         assert R.rel_l2(img, ref) < TOL, (Ly, Lx)
 
 
+def test_odd_shapes(ctx, golden_optics, golden_kernels, L):
+    """Odd mask sizes: rows and columns that are not 16-byte multiples (4-byte copies in the
+    window ring), an odd row count in the FI kernel's row pairing (row +y' and -y' from one
+    set of sums: the centre row y' = 0 and the unpaired edge row), and the mixed form with an
+    odd row count."""
+    krns, scales = golden_kernels
+    nx = golden_optics["Nx"]
+    rng = np.random.default_rng(13)
+    for Ly, Lx in ((301, 257), (129, 255), (255, 130)):
+        m = (rng.random((Ly, Lx)) > 0.6).astype(np.float32)
+        ref = R.mask_to_image(m, krns, scales, nx, nx)
+        assert R.rel_l2(ctx.image(m, krns, scales, nx, nx), ref) < TOL, (Ly, Lx)
+    m = (rng.random((301, 256)) > 0.6).astype(np.float32)
+    ref = R.mask_to_image(m, krns, scales, nx, nx)
+    got = ctx.image(m, krns, scales, nx, nx, precision=L.PREC_MIXED)
+    assert R.rel_l2(got, ref) < 1e-4
+
+
 def test_edge_cases_report_status(ctx, golden_kernels, L):
     krns, scales = golden_kernels
     m = np.zeros((512, 512), np.float32)
