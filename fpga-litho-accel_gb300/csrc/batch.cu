@@ -100,8 +100,10 @@ static int run_class(litho_batch_plan* bp, int ci) {
   LITHO_CUDA_TRY(ctx, cudaMemsetAsync(c.win.p, 0, (size_t)c.count * c.part_stride * KY * (Nx + 1) * sizeof(float2),
                                       ctx->stream));
   // The sub-batches' window DFTs (one per mask size; each writes its own images'
-  // partials) run as parallel branches, the largest on the context's stream: all of them
-  // stream masks from HBM, so each fills the others' ramps and tails.
+  // partials).  Mixed form: one persistent launch over up to WIN_MAX_SIZES mask sizes, so
+  // that the small sizes' few tiles share the SMs with the large ones'.  Plain form:
+  // parallel branches, the largest on the context's stream: all of them stream masks from
+  // HBM, so each fills the others' ramps and tails.
   std::vector<const SubBatch*> sb;
   for (const SubBatch& s : bp->subs)
     if (s.cls == ci) sb.push_back(&s);
@@ -115,25 +117,29 @@ static int run_class(litho_batch_plan* bp, int ci) {
     pw.part_stride = c.part_stride;
     return pw;
   };
-  if (sb.size() > 1) {
-    // tables shared between sub-batches are built here, before the fork
-    for (const SubBatch* s : sb) {
-      const ImgPlan pw = win_plan(*s);
-      LITHO_RET(tc ? prepare_win_dft_tc(ctx, pw) : prepare_win_dft(ctx, pw));
+  if (tc) {
+    std::vector<WinPart> parts;
+    for (const SubBatch* s : sb) parts.push_back(WinPart{win_plan(*s), s->masks, s->first_in_class});
+    for (size_t i = 0; i < parts.size(); i += WIN_MAX_SIZES)
+      LITHO_RET(run_win_dft_tc_multi(ctx, parts.data() + i, (int)std::min<size_t>(WIN_MAX_SIZES, parts.size() - i),
+                                     c.win.as<float2>()));
+  } else {
+    if (sb.size() > 1) {
+      // tables shared between sub-batches are built here, before the fork
+      for (const SubBatch* s : sb) LITHO_RET(prepare_win_dft(ctx, win_plan(*s)));
+      LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[0], ctx->stream));
+      for (size_t k = 1; k < sb.size(); ++k)
+        LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(bp->wstreams[k - 1], bp->wevents[0], 0));
     }
-    LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[0], ctx->stream));
-    for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(bp->wstreams[k - 1], bp->wevents[0], 0));
+    for (size_t k = 0; k < sb.size(); ++k) {
+      const SubBatch& s = *sb[k];
+      StreamScope scope(ctx, k == 0 ? ctx->stream : bp->wstreams[k - 1]);
+      float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
+      LITHO_RET(run_win_dft(ctx, win_plan(s), s.masks, wp));
+      if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[k], ctx->stream));
+    }
+    for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->wevents[k], 0));
   }
-  for (size_t k = 0; k < sb.size(); ++k) {
-    const SubBatch& s = *sb[k];
-    StreamScope scope(ctx, k == 0 ? ctx->stream : bp->wstreams[k - 1]);
-    const ImgPlan pw = win_plan(s);
-    float2* wp = c.win.as<float2>() + (size_t)s.first_in_class * c.part_stride * KY * (Nx + 1);
-    if (tc) LITHO_RET(run_win_dft_tc(ctx, pw, s.masks, wp));
-    else LITHO_RET(run_win_dft(ctx, pw, s.masks, wp));
-    if (k > 0) LITHO_CUDA_TRY(ctx, cudaEventRecord(bp->wevents[k], ctx->stream));
-  }
-  for (size_t k = 1; k < sb.size(); ++k) LITHO_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, bp->wevents[k], 0));
   const bool band = c.convN == 0;
   ImgPlan p = make_plan(class_geom(c, band ? default_conv(Nx, Ny) : c.convN), c.count, ctx->sm_count);
   p.kpg = band ? c.ks->nk : std::min(c.kpg, c.ks->nk);

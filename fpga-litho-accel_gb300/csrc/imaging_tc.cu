@@ -36,6 +36,8 @@
 #include "litho_internal.cuh"
 #include "tc_common.cuh"
 
+#include <cstring>
+
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -173,6 +175,19 @@ constexpr size_t WP_SMEM_CAP = 227 * 1024;
 
 // epilogue buffer: sR [2Nx+1][RSR] fp32 (a multiple of 16 bytes)
 static inline size_t win_epi_bytes(int Nx) { return (size_t)(2 * Nx + 1) * WP_RSR * 4; }
+// The mask geometries of one window-DFT launch (the mask sizes of a batch class share the
+// period, the kernels and the partial array): per geometry its masks' and twiddles' tensor
+// maps, its row twiddles, width, row blocks, column splits and first image in the partial
+// array.  Tiles are numbered geometry after geometry (tile0: the prefix).
+constexpr int WP_MAX_GEO = WIN_MAX_SIZES;
+struct WinGeo {
+  CUtensorMap mM[WP_MAX_GEO];  // masks [img][Ly][Lx]
+  CUtensorMap mB[WP_MAX_GEO];  // twiddles [hi; lo] x Lx
+  const float2* ytab[WP_MAX_GEO];
+  int Lx[WP_MAX_GEO], rows[WP_MAX_GEO], ncs[WP_MAX_GEO], img0[WP_MAX_GEO], tile0[WP_MAX_GEO + 1];
+  int n;
+};
+
 // mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES): 5 per stage, 5 more,
 // two per tile-ring slot; the TMEM slot, abort flag, per-stage ints, tile ring and the two
 // groups' current tiles
@@ -181,11 +196,8 @@ static inline size_t win_bar_bytes(int S) {
 }
 
 template <int NBH>
-__global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ CUtensorMap tmM,
-                                                                   const __grid_constant__ CUtensorMap tmB,
-                                                                   int Lx, int Ly, int Fx, int Fy, int Nx, int Ny,
-                                                                   int rows, int batch, int ncs, int S,
-                                                                   const float2* __restrict__ ytab,
+__global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_constant__ WinGeo G, int Fx, int Fy,
+                                                                   int Nx, int Ny, int S,
                                                                    float2* __restrict__ win_part, int part_stride,
                                                                    int* __restrict__ err, int stall_at) {
   using P = WinTC<NBH>;
@@ -211,8 +223,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   volatile int* tq = nzflag + S;                          // [WP_TQ] tile index, -1 = no more tiles
   volatile int* gtile = tq + WP_TQ;                       // [2] consumers' / epilogue's current tile
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nch = (Lx + 32 * P::KB - 1) / (32 * P::KB);  // chunks of 32 KB columns
-  const int T = rows * batch * ncs;
+  const int T = G.tile0[G.n];
 
   if (warp == 0) tmem_alloc(tslot, 2 * P::NCOL);
   if (tid == 0) {
@@ -262,10 +273,15 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
 
   auto sA = [&](int s) { return sm + (size_t)s * P::STAGE_B; };
   auto sBh = [&](int s) { return sm + (size_t)s * P::STAGE_B + P::A_B; };  // [Bh; Bl], 2 NBH rows
-  // tile t -> (image, row block, column split) and its chunk range
-  auto decode = [&](int t, int& img, int& rb, int& cs, int& c0, int& c1) {
-    img = t / (rows * ncs);
-    const int r = t - img * rows * ncs;
+  // tile t -> (geometry, image, row block, column split) and its chunk range (chunks of
+  // 32 KB columns)
+  auto decode = [&](int t, int& g, int& img, int& rb, int& cs, int& c0, int& c1) {
+    g = 0;
+    while (g + 1 < G.n && t >= G.tile0[g + 1]) ++g;
+    const int l = t - G.tile0[g], rows = G.rows[g], ncs = G.ncs[g];
+    const int nch = (G.Lx[g] + 32 * P::KB - 1) / (32 * P::KB);
+    img = l / (rows * ncs);
+    const int r = l - img * rows * ncs;
     rb = r / ncs;
     cs = r - rb * ncs;
     c0 = (int)((long long)nch * cs / ncs);
@@ -288,8 +304,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         tq[j] = t;
         mbar_arrive(&tqf[j]);  // release: the slot's tile index is visible to the readers
         if (t < 0) break;
-        int img, rb, cs, c0, c1;
-        decode(t, img, rb, cs, c0, c1);
+        int g, img, rb, cs, c0, c1;
+        decode(t, g, img, rb, cs, c0, c1);
         for (int c = c0; c < c1; ++c, ++q) {
           if (q == stall_at) {  // error-path test hook: the producer is lost here
             ok = false;
@@ -303,8 +319,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
           mbar_arrive_expect_tx(&full[s], P::STAGE_B);
 #pragma unroll
           for (int kb = 0; kb < P::KB; ++kb) {
-            tma_load_3d(sA(s) + kb * P::A_KB, &tmM, &full[s], 32 * (P::KB * c + kb), 128 * rb, img);
-            tma_load_2d(sBh(s) + kb * P::B_KB, &tmB, &full[s], 32 * (P::KB * c + kb), 0);
+            tma_load_3d(sA(s) + kb * P::A_KB, &G.mM[g], &full[s], 32 * (P::KB * c + kb), 128 * rb, img);
+            tma_load_2d(sBh(s) + kb * P::B_KB, &G.mB[g], &full[s], 32 * (P::KB * c + kb), 0);
           }
           last_issued[s] = q;
           if (++s == S) {
@@ -327,8 +343,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       for (int seq = 0; ok; ++seq, ++tl) {
         int t;
         if (!ring_read(seq, t) || t < 0) break;
-        int img, rb, cs, c0, c1;
-        decode(t, img, rb, cs, c0, c1);
+        int g, img, rb, cs, c0, c1;
+        decode(t, g, img, rb, cs, c0, c1);
         const int buf = tl & 1;
         if (tl >= 2 && !mbar_wait_ab(&accempty[buf], (uint32_t)((tl - 2) >> 1) & 1u, abort)) {
           *abort = 1;
@@ -399,8 +415,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       const int t = gtile[0];
       named_bar(1, WP_CONS);  // every consumer holds t before the leader may overwrite it
       if (t < 0) break;
-      int img, rb, cs, c0, c1;
-      decode(t, img, rb, cs, c0, c1);
+      int g, img, rb, cs, c0, c1;
+      decode(t, g, img, rb, cs, c0, c1);
       for (int c = c0; c < c1; ++c) {
         if (!mbar_wait_ab(&full[s], ph, abort)) *abort = 1;
         float4* a = reinterpret_cast<float4*>(sA(s));
@@ -459,8 +475,8 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       const int t = gtile[1];
       named_bar(2, 128);  // every epilogue thread holds t before the leader may overwrite it
       if (t < 0) break;
-      int img, rb, cs, c0, c1;
-      decode(t, img, rb, cs, c0, c1);
+      int g, img, rb, cs, c0, c1;
+      decode(t, g, img, rb, cs, c0, c1);
       const int buf = tl & 1;
       // on a wait that gives up: flag it and carry on with the group (see above)
       if (!mbar_wait_ab(&accfull[buf], (uint32_t)(tl >> 1) & 1u, abort)) *abort = 1;
@@ -480,8 +496,9 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
       const int y0 = 128 * rb;
       named_bar(2, 128);
+      const int rows = G.rows[g], ncs = G.ncs[g];
       const int nps = part_stride > 0 ? part_stride : rows * ncs;
-      float2* out = win_part + ((size_t)img * nps + (rb * ncs + cs)) * KY * NU;
+      float2* out = win_part + ((size_t)(G.img0[g] + img) * nps + (rb * ncs + cs)) * KY * NU;
       // one thread per (|v|, u): four row sums give both outputs +v and -v
       //   S1 = sum c tx, S2 = sum s ty, S3 = sum c ty, S4 = sum s tx
       //   (+v): (S1 - S2, S3 + S4)    (-v): (S1 + S2, S4 - S3)
@@ -491,7 +508,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
         const float4* rc = reinterpret_cast<const float4*>(sR + u * RS);
         const float4* rs = reinterpret_cast<const float4*>(sR + (Nx + u) * RS);
         // the tile's row twiddles of |v| (zero past Ly), two rows per vector, from L1
-        const float4* rt = reinterpret_cast<const float4*>(ytab + (size_t)av * (128 * rows) + y0);
+        const float4* rt = reinterpret_cast<const float4*>(G.ytab[g] + (size_t)av * (128 * rows) + y0);
         float s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
         if (u == 0) {
 #pragma unroll 4
@@ -1002,61 +1019,77 @@ static int win_tc_tables(litho_ctx* ctx, const ImgGeom& g, float** twh, float** 
 }
 
 template <int NBH>
-static int launch_win_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part, int* err) {
-  const ImgGeom& g = p.g;
-  float *twh = nullptr, *yt = nullptr;
-  LITHO_RET(win_tc_tables<NBH>(ctx, g, &twh, &yt));
-  CUtensorMap mM, mB;
-  LITHO_RET(make_map(ctx, &mM, masks, 3, g.Lx, g.Ly, p.batch, 128));
-  LITHO_RET(make_map(ctx, &mB, twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
+static int launch_win_tc(litho_ctx* ctx, const WinPart* parts, int n, float2* win_part, int* err) {
+  WinGeo G;
+  std::memset(&G, 0, sizeof(G));
+  G.n = n;
+  int tiles = 0;
+  for (int i = 0; i < n; ++i) {
+    const ImgPlan& p = parts[i].plan;
+    const ImgGeom& g = p.g;
+    float *twh = nullptr, *yt = nullptr;
+    LITHO_RET(win_tc_tables<NBH>(ctx, g, &twh, &yt));
+    LITHO_RET(make_map(ctx, &G.mM[i], parts[i].masks, 3, g.Lx, g.Ly, p.batch, 128));
+    LITHO_RET(make_map(ctx, &G.mB[i], twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
+    G.ytab[i] = reinterpret_cast<const float2*>(yt);
+    G.Lx[i] = g.Lx;
+    G.rows[i] = (g.Ly + 127) / 128;
+    G.ncs[i] = std::max(1, p.colSplits);
+    G.img0[i] = parts[i].img0;
+    G.tile0[i] = tiles;
+    tiles += G.rows[i] * p.batch * G.ncs[i];
+  }
+  G.tile0[n] = tiles;
+  const ImgGeom& g0 = parts[0].plan.g;
   // as many ring stages as shared memory holds
   using P = WinTC<NBH>;
-  const size_t fixed = 1024 + win_epi_bytes(g.Nx) + win_bar_bytes(WP_MAX_STAGES);
+  const size_t fixed = 1024 + win_epi_bytes(g0.Nx) + win_bar_bytes(WP_MAX_STAGES);
   const int S = (int)std::min<size_t>(WP_MAX_STAGES, (WP_SMEM_CAP - fixed) / P::STAGE_B);
-  const size_t smem = 1024 + (size_t)S * P::STAGE_B + win_epi_bytes(g.Nx) + win_bar_bytes(S);
+  const size_t smem = 1024 + (size_t)S * P::STAGE_B + win_epi_bytes(g0.Nx) + win_bar_bytes(S);
   LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(win_dft_tc_kernel<NBH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem));
-  const int rows = (g.Ly + 127) / 128, ncs = std::max(1, p.colSplits);
-  const int tiles = rows * p.batch * ncs;
   const int grid = std::min(tiles, ctx->sm_count);  // persistent: one CTA per SM
   StageScope sc(ctx, LITHO_STAGE_WIN_DFT);
-  win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(mM, mB, g.Lx, g.Ly, g.Fx, g.Fy, g.Nx, g.Ny, rows,
-                                                                  p.batch, ncs, S,
-                                                                  reinterpret_cast<const float2*>(yt), win_part,
-                                                                  p.part_stride, err, ctx->test_stall_chunk);
+  win_dft_tc_kernel<NBH><<<grid, WP_THREADS, smem, ctx->stream>>>(G, g0.Fx, g0.Fy, g0.Nx, g0.Ny, S, win_part,
+                                                                  parts[0].plan.part_stride, err,
+                                                                  ctx->test_stall_chunk);
   LITHO_CUDA_TRY(ctx, cudaGetLastError());
   return LITHO_OK;
 }
 
-// Build the cached tables and the timeout flag a mixed window DFT of this geometry reads,
-// on the context's stream (so that launches on other streams find them ready).
-int prepare_win_dft_tc(litho_ctx* ctx, const ImgPlan& p) {
-  int* err = nullptr;
-  LITHO_RET(tc_err_flag(ctx, &err));
-  float *twh = nullptr, *yt = nullptr;
-  switch (nb_for(p.g.Nx)) {
-    case 8: return win_tc_tables<8>(ctx, p.g, &twh, &yt);
-    case 16: return win_tc_tables<16>(ctx, p.g, &twh, &yt);
-    case 24: return win_tc_tables<24>(ctx, p.g, &twh, &yt);
-    case 32: return win_tc_tables<32>(ctx, p.g, &twh, &yt);
-    case 40: return win_tc_tables<40>(ctx, p.g, &twh, &yt);
-    default: return LITHO_OK;  // the launch reports the unsupported size
+// One persistent launch over the masks of up to WP_MAX_GEO sizes that share the period,
+// the kernel support and the partial array (their plans' Fx, Fy, Nx, Ny and part_stride).
+int run_win_dft_tc_multi(litho_ctx* ctx, const WinPart* parts, int n, float2* win_part) {
+  if (n < 1 || n > WP_MAX_GEO) {
+    set_error(ctx, LITHO_ERR_ARG, "window DFT over %d mask sizes (1..%d)", n, WP_MAX_GEO);
+    return LITHO_ERR_ARG;
   }
-}
-
-int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
+  const ImgGeom& g0 = parts[0].plan.g;
+  for (int i = 1; i < n; ++i) {
+    const ImgPlan& p = parts[i].plan;
+    if (p.g.Fx != g0.Fx || p.g.Fy != g0.Fy || p.g.Nx != g0.Nx || p.g.Ny != g0.Ny ||
+        p.part_stride != parts[0].plan.part_stride) {
+      set_error(ctx, LITHO_ERR_ARG, "window DFT mask sizes of one launch must share the period and the kernels");
+      return LITHO_ERR_ARG;
+    }
+  }
   int* err = nullptr;
   LITHO_RET(tc_err_flag(ctx, &err));
-  switch (nb_for(p.g.Nx)) {
-    case 8: return launch_win_tc<8>(ctx, p, masks, win_part, err);
-    case 16: return launch_win_tc<16>(ctx, p, masks, win_part, err);
-    case 24: return launch_win_tc<24>(ctx, p, masks, win_part, err);
-    case 32: return launch_win_tc<32>(ctx, p, masks, win_part, err);
-    case 40: return launch_win_tc<40>(ctx, p, masks, win_part, err);
+  switch (nb_for(g0.Nx)) {
+    case 8: return launch_win_tc<8>(ctx, parts, n, win_part, err);
+    case 16: return launch_win_tc<16>(ctx, parts, n, win_part, err);
+    case 24: return launch_win_tc<24>(ctx, parts, n, win_part, err);
+    case 32: return launch_win_tc<32>(ctx, parts, n, win_part, err);
+    case 40: return launch_win_tc<40>(ctx, parts, n, win_part, err);
     default:
       set_error(ctx, LITHO_ERR_UNSUPPORTED, "tensor-core window DFT supports Nx <= 16");
       return LITHO_ERR_UNSUPPORTED;
   }
+}
+
+int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part) {
+  const WinPart part{p, masks, 0};
+  return run_win_dft_tc_multi(ctx, &part, 1, win_part);
 }
 
 template <int KBLK, int BN>
