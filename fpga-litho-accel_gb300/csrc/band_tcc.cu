@@ -288,7 +288,11 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
   {
     StageScope sc(ctx, LITHO_STAGE_SOCS, 2);
     const int bx = (KDP + 127) / 128;
-    const int by = std::max(1, std::min(65535, (p.batch + 3) / 4));  // about four images per thread
+    // up to four images per thread (their partial loads in flight together), fewer where
+    // that would leave fewer than ~4 blocks per SM
+    const int sms = std::max(1, p.sms > 0 ? p.sms : ctx->sm_count);
+    const int ipt = std::max(1, std::min(4, (p.batch * bx) / (4 * sms)));
+    const int by = std::max(1, std::min(65535, (p.batch + ipt - 1) / ipt));
     win_sum_kernel<<<dim3(bx, by), 128, 0, ctx->stream>>>(
         w.part, w.nparts, w.mskf_r, w.mskf_i, g.Fx, g.Fy, g.Nx, g.Ny, KDP, p.batch, wsum);
     LITHO_CUDA_TRY(ctx, cudaGetLastError());
@@ -301,7 +305,6 @@ int run_band_tcc(litho_ctx* ctx, const ImgPlan& p, const WindowSrc& w, const lit
     LITHO_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(BT_WARPS)));
     // warps per CTA: the largest that still gives every SM a CTA (small batches take
     // smaller CTAs, so that the tasks spread over the whole GPU)
-    const int sms = std::max(1, p.sms > 0 ? p.sms : ctx->sm_count);
     int nw = 2;
     for (int w = BT_WARPS; w >= 2; w /= 2)
       if ((long long)ntc * ((p.batch + w * IPW - 1) / (w * IPW)) >= sms) {
