@@ -76,6 +76,33 @@ def test_batch_plan_uneven_sizes(ctx, L, classes, prec_name, tol):
         s.close()
 
 
+@pytest.mark.parametrize("prec_name,tol", [("fp32", 1e-5), ("mixed", 1e-4)])
+def test_batch_plan_many_sizes_in_one_class(ctx, L, classes, prec_name, tol):
+    """Six mask sizes in one class: the mixed window DFT takes up to four sizes per launch
+    (a tensor map pair, row twiddles and a tile range each), so this class runs two launches
+    (4 + 2 sizes) into the same partial array; the plain form runs six branches."""
+    import torch
+    from litho_gb300 import synth
+    prec = L.PREC_FP32 if prec_name == "fp32" else L.PREC_MIXED
+    Lp, k = classes[0]
+    ks = ctx.kernel_set(k[0], k[1], k[2], k[2])
+    items = [(0, 512, 512), (0, 64, 64), (0, 384, 384), (0, 128, 96), (0, 256, 256), (0, 192, 320), (0, 64, 64)]
+    plan = L.BatchPlan(ctx, [ks], [Lp], items, precision=prec)
+    masks = [np.ascontiguousarray(synth.density_rect_mask(max(x, y), 0.3 + 0.04 * i, seed=90 + i)[:y, :x])
+             for i, (_, x, y) in enumerate(items)]
+    for i, m in enumerate(masks):
+        plan.mask(i).copy_(torch.from_numpy(m))
+    torch.cuda.synchronize()
+    plan.run()
+    ctx.synchronize()
+    krns, scales, nx = k
+    for i in range(len(items)):
+        ref = R.mask_to_image(R.create_mask(masks[i], Lp, Lp), krns, scales, nx, nx)
+        assert R.rel_l2(plan.image(i).cpu().numpy(), ref) < tol, (prec_name, i)
+    plan.close()
+    ks.close()
+
+
 def test_batch_plan_rejects_bad_items(ctx, L, classes):
     sets = [ctx.kernel_set(k[0], k[1], k[2], k[2]) for _, k in classes]
     with pytest.raises(L.LithoError):
