@@ -952,12 +952,16 @@ static cudaError_t launch_fi_rows_t(cudaStream_t s, const ImgPlan& p, const floa
   auto k = fi_rows_kernel<MAXD, KMAJ, KPC>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  // column blocks over the x' < 0 half; enough image groups for a few CTAs per SM,
-  // each CTA walking its group's images with its twiddles kept in registers
+  // column blocks over the x' < 0 half; as many image groups as keep every CTA resident
+  // at once (a second partial wave would double the time of the CTAs in it), each CTA
+  // walking its group's images with its twiddles kept in registers
   const int nb = g.Fx / 2 - (g.Fx - g.Lx) / 2;
   const int ncb = std::max(1, (nb + FR_COLS - 1) / FR_COLS);
   const int sms = p.sms > 0 ? p.sms : 148;
-  const int groups = std::max(1, std::min(p.batch, (4 * sms + ncb - 1) / ncb));
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, FR_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  const int groups = std::max(1, std::min(p.batch, std::max(1, per_sm) * sms / ncb));
   k<<<dim3(ncb, groups), FR_THREADS, smem, s>>>(band_part, p.ngroups, twF, g.Lx, g.Fx, g.Nx, g.Ny, KP, p.batch,
                                                 pre ? rawn : 0, tm, tmh, tml, t0);
   return cudaGetLastError();
