@@ -400,7 +400,10 @@ class Context:
         return KernelSet(self, krn, scales, Nx, Ny)
 
     def image_batch(self, ks: KernelSet, masks, images=None, precision: int = PREC_FP32):
-        """Image a batch of equal-size masks (B, Ly, Lx).  Device tensors stay on the device."""
+        """Image a batch of equal-size masks (B, Ly, Lx).  Device tensors stay on the device; the
+        work is queued on the context's stream (its own non-blocking stream unless set_stream
+        chose another), so the tensors' producers on other streams must be ordered before the
+        call (torch.cuda.synchronize(), or set_stream(torch.cuda.current_stream().cuda_stream))."""
         B, Ly, Lx = masks.shape
         if _is_dev(masks):
             import torch

@@ -114,6 +114,7 @@ def test_default_is_tcc_band_for_large_batches_at_nx8(ctx):
     assert nx == 8
     m = torch.from_numpy(np.stack([synth.density_rect_mask(1024, 0.3 + 0.001 * i, seed=200 + i)
                                    for i in range(4)]).astype(np.float32)).cuda().repeat(64, 1, 1)
+    torch.cuda.synchronize()  # the context images on its own stream
     outs = {}
     ks = ctx.kernel_set(krn, scales, nx, ny)
     try:

@@ -62,6 +62,7 @@ def test_stalled_producer_times_out_and_context_recovers(case, chunk):
         # same context: host buffers, then device buffers with an explicit synchronise
         _check(ctx.image_batch(ks, case["masks"], precision=Lib.PREC_MIXED), case["ref"])
         dm = torch.from_numpy(case["masks"]).cuda()
+        torch.cuda.synchronize()  # the context images on its own stream
         out = ctx.image_batch(ks, dm, precision=Lib.PREC_MIXED)
         ctx.synchronize()
         _check(out.cpu().numpy(), case["ref"])

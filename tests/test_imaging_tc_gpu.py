@@ -120,7 +120,9 @@ def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec, chunk):
     try:
         ctx.set_host_chunk(chunk)
         host = ctx.image_batch(ks, masks, precision=p)          # numpy in, numpy out
-        dev = ctx.image_batch(ks, torch.from_numpy(masks).cuda(), precision=p)
+        dm = torch.from_numpy(masks).cuda()
+        torch.cuda.synchronize()  # the context images on its own stream
+        dev = ctx.image_batch(ks, dm, precision=p)
         ctx.synchronize()
         dev = dev.cpu().numpy()
     finally:
