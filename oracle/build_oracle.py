@@ -24,7 +24,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "fftw_shim")
-DEFAULT_REF = "/root/reference"
+# the reference checkout: the first argument, else $LITHO_REFERENCE_DIR, else this build's checkout
+DEFAULT_REF = os.environ.get("LITHO_REFERENCE_DIR", "/root/reference")
 
 
 def _openblas():
