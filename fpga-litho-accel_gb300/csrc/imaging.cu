@@ -29,6 +29,7 @@
 #include "litho_internal.cuh"
 #include "fft_warp.cuh"
 #include "fft_lane8.cuh"
+#include "fi_mirror.hpp"
 #include "tc_common.cuh"
 
 #include <algorithm>
@@ -1036,13 +1037,6 @@ __global__ void fo_cm_init_kernel(float* __restrict__ cm, int nbp, int Fy, int N
   if (b < nbp) cm[(size_t)r * nbp + b] = fo_cm(r, b, Fy, Ny);
 }
 
-// base rows of a geometry: b = 0 .. max |y'| over the image rows
-__host__ __device__ inline int fo_nbase(int Ly, int Fy) {
-  const long long oy = (long long)(Fy - Ly) / 2 - Fy / 2;
-  const long long lo = oy < 0 ? -oy : oy, hi = oy + Ly - 1 < 0 ? -(oy + Ly - 1) : oy + Ly - 1;
-  return (int)(lo > hi ? lo : hi) + 1;
-}
-
 // the Cm table of a geometry, cached per (Ly, Fy, Ny) on the context
 static int fo_cm_table(litho_ctx* ctx, const ImgGeom& g, const float** out, int* nbp) {
   *nbp = (fo_nbase(g.Ly, g.Fy) + FO_BM - 1) / FO_BM * FO_BM;
@@ -1124,7 +1118,6 @@ __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restr
   for (int r = 0; r <= 2 * Ny; ++r) step(r, A);
 #pragma unroll 4
   for (int r = 2 * Ny + 1; r < KB; ++r) step(r, Bs);
-  const int oy = (Fy - Ly) / 2 - Fy / 2;
   const int nbase = fo_nbase(Ly, Fy);
   float* O = images + (size_t)img * Lx * Ly;
   const int X = X0 + 4 * lane;
@@ -1134,9 +1127,8 @@ __global__ void __launch_bounds__(FO_THREADS) fi_out_kernel(const float* __restr
     if (b >= nbase) continue;
 #pragma unroll
     for (int sgn = 0; sgn < 2; ++sgn) {
-      if (sgn == 1 && b == 0) continue;  // y' = 0 has no mirror
-      const int Y = (sgn == 0 ? b : -b) - oy;
-      if (Y < 0 || Y >= Ly) continue;
+      const int Y = fo_row(b, sgn, Ly, Fy);  // y' = +b, -b (y' = 0 once)
+      if (Y < 0) continue;
       const float o[4] = {sgn == 0 ? A[i][0].x + Bs[i][0].x : A[i][0].x - Bs[i][0].x,
                           sgn == 0 ? A[i][0].y + Bs[i][0].y : A[i][0].y - Bs[i][0].y,
                           sgn == 0 ? A[i][1].x + Bs[i][1].x : A[i][1].x - Bs[i][1].x,
