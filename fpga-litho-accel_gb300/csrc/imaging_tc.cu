@@ -35,6 +35,7 @@
 //                     image is written exactly once).
 #include "litho_internal.cuh"
 #include "tc_common.cuh"
+#include "win_tiles.hpp"
 
 #include <cstring>
 
@@ -184,8 +185,7 @@ struct WinGeo {
   CUtensorMap mM[WP_MAX_GEO];  // masks [img][Ly][Lx]
   CUtensorMap mB[WP_MAX_GEO];  // twiddles [hi; lo] x Lx
   const float2* ytab[WP_MAX_GEO];
-  int Lx[WP_MAX_GEO], rows[WP_MAX_GEO], ncs[WP_MAX_GEO], img0[WP_MAX_GEO], tile0[WP_MAX_GEO + 1];
-  int n;
+  WinTiles T;                  // widths, row blocks, splits, first images and tiles (win_tiles.hpp)
 };
 
 // mbarriers and flags after the epilogue buffers (S <= WP_MAX_STAGES): 5 per stage, 5 more,
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   volatile int* tq = nzflag + S;                          // [WP_TQ] tile index, -1 = no more tiles
   volatile int* gtile = tq + WP_TQ;                       // [2] consumers' / epilogue's current tile
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int T = G.tile0[G.n];
+  const int T = G.T.tile0[G.T.n];
 
   if (warp == 0) tmem_alloc(tslot, 2 * P::NCOL);
   if (tid == 0) {
@@ -276,16 +276,7 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
   // tile t -> (geometry, image, row block, column split) and its chunk range (chunks of
   // 32 KB columns)
   auto decode = [&](int t, int& g, int& img, int& rb, int& cs, int& c0, int& c1) {
-    g = 0;
-    while (g + 1 < G.n && t >= G.tile0[g + 1]) ++g;
-    const int l = t - G.tile0[g], rows = G.rows[g], ncs = G.ncs[g];
-    const int nch = (G.Lx[g] + 32 * P::KB - 1) / (32 * P::KB);
-    img = l / (rows * ncs);
-    const int r = l - img * rows * ncs;
-    rb = r / ncs;
-    cs = r - rb * ncs;
-    c0 = (int)((long long)nch * cs / ncs);
-    c1 = (int)((long long)nch * (cs + 1) / ncs);
+    win_tile(G.T, t, 32 * P::KB, g, img, rb, cs, c0, c1);
   };
 
   if (warp == 8) {
@@ -496,9 +487,9 @@ __global__ void __launch_bounds__(WP_THREADS, 1) win_dft_tc_kernel(const __grid_
       mbar_arrive(&accempty[buf]);  // the MMA lane may refill this accumulator
       const int y0 = 128 * rb;
       named_bar(2, 128);
-      const int rows = G.rows[g], ncs = G.ncs[g];
+      const int rows = G.T.rows[g], ncs = G.T.ncs[g];
       const int nps = part_stride > 0 ? part_stride : rows * ncs;
-      float2* out = win_part + ((size_t)(G.img0[g] + img) * nps + (rb * ncs + cs)) * KY * NU;
+      float2* out = win_part + ((size_t)(G.T.img0[g] + img) * nps + (rb * ncs + cs)) * KY * NU;
       // one thread per (|v|, u): four row sums give both outputs +v and -v
       //   S1 = sum c tx, S2 = sum s ty, S3 = sum c ty, S4 = sum s tx
       //   (+v): (S1 - S2, S3 + S4)    (-v): (S1 + S2, S4 - S3)
@@ -1022,7 +1013,7 @@ template <int NBH>
 static int launch_win_tc(litho_ctx* ctx, const WinPart* parts, int n, float2* win_part, int* err) {
   WinGeo G;
   std::memset(&G, 0, sizeof(G));
-  G.n = n;
+  G.T.n = n;
   int tiles = 0;
   for (int i = 0; i < n; ++i) {
     const ImgPlan& p = parts[i].plan;
@@ -1032,14 +1023,14 @@ static int launch_win_tc(litho_ctx* ctx, const WinPart* parts, int n, float2* wi
     LITHO_RET(make_map(ctx, &G.mM[i], parts[i].masks, 3, g.Lx, g.Ly, p.batch, 128));
     LITHO_RET(make_map(ctx, &G.mB[i], twh, 2, g.Lx, 2 * NBH, 1, 2 * NBH));  // hi rows, then lo rows
     G.ytab[i] = reinterpret_cast<const float2*>(yt);
-    G.Lx[i] = g.Lx;
-    G.rows[i] = (g.Ly + 127) / 128;
-    G.ncs[i] = std::max(1, p.colSplits);
-    G.img0[i] = parts[i].img0;
-    G.tile0[i] = tiles;
-    tiles += G.rows[i] * p.batch * G.ncs[i];
+    G.T.Lx[i] = g.Lx;
+    G.T.rows[i] = (g.Ly + 127) / 128;
+    G.T.ncs[i] = std::max(1, p.colSplits);
+    G.T.img0[i] = parts[i].img0;
+    G.T.tile0[i] = tiles;
+    tiles += G.T.rows[i] * p.batch * G.T.ncs[i];
   }
-  G.tile0[n] = tiles;
+  G.T.tile0[n] = tiles;
   const ImgGeom& g0 = parts[0].plan.g;
   // as many ring stages as shared memory holds
   using P = WinTC<NBH>;

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/litho_gb300.h"
+#include "win_tiles.hpp"
 
 namespace litho {
 
@@ -250,14 +251,14 @@ bool use_band_tcc(const litho_ctx* ctx, const litho_kernel_set* ks, int batch);
 
 // mixed precision window DFT / interpolation (imaging_tc.cu)
 int run_win_dft_tc(litho_ctx* ctx, const ImgPlan& p, const float* masks, float2* win_part);
-// masks of one size for a multi-size window launch: its plan, its masks and its first image
+// masks of one size for a multi-size window launch (at most WIN_MAX_SIZES, win_tiles.hpp):
+// its plan, its masks and its first image
 // in the shared partial array
 struct WinPart {
   ImgPlan plan;
   const float* masks;
   int img0;
 };
-constexpr int WIN_MAX_SIZES = 4;  // mask sizes one window launch takes
 int run_win_dft_tc_multi(litho_ctx* ctx, const WinPart* parts, int n, float2* win_part);
 int run_fi_tc(litho_ctx* ctx, const ImgPlan& p, const float2* band_part, float* tmT, float* images);
 struct FiTcBufs {
