@@ -571,7 +571,7 @@ struct FiTC {
   static constexpr int NS = KBLK == 1 ? 2 : 3;
   static constexpr int NOUT = KBLK == 1 ? 4 : 2;
   static constexpr uint32_t OUT_B = 32 * 128;     // 32 rows x 32 fp32 staging tile of one warp
-  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * STAGE_B + 8 * NOUT * OUT_B + 2 * BN * 4 + 512;
+  static constexpr size_t SMEM = 1024 + A_BYTES + (size_t)NS * STAGE_B + 8 * NOUT * OUT_B + 3 * BN * 4 + 512;
 };
 constexpr int FI_THREADS = 320;  // warps 0-7 epilogue (two groups), 8 TMA, 9 MMA
 constexpr int FI_TQ = 8;         // tile ring slots
@@ -606,8 +606,8 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
   unsigned char* sAl = sm + KBLK * P::A_KB;
   unsigned char* sB = sm + P::A_BYTES;               // [NS][kb][hi, lo]
   unsigned char* sOut = sB + NS * P::STAGE_B;        // [8 epilogue warps][NOUT][OUT_B]
-  float* sT0 = reinterpret_cast<float*>(sOut + 8 * NOUT * P::OUT_B);  // [2 accumulators][BN]: the tile's DC row
-  uint64_t* fullA = reinterpret_cast<uint64_t*>(sT0 + 2 * BN);
+  float* sT0 = reinterpret_cast<float*>(sOut + 8 * NOUT * P::OUT_B);  // [3][BN]: the DC rows of tiles q % 3
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(sT0 + 3 * BN);
   uint64_t* emptyA = fullA + 1;
   uint64_t* fullB = fullA + 2;           // [NS]
   uint64_t* emptyB = fullB + NS;         // [NS]
@@ -820,11 +820,13 @@ __global__ void __launch_bounds__(FI_THREADS, 1) fi_tc_kernel(const __grid_const
       } else {
         t0_of(i, t0c);
       }
-      // the shared DC row of accumulator buffer b: this warp writes and then reads only its
-      // own slabs' columns (warps of the other quarters write the same values), and no warp
-      // is ever more than one tile ahead of another (the MMA lane refills buffer b only after
-      // every warp has released it)
-      float* t0s = sT0 + b * BN;
+      // the shared DC row of tile q, in row buffer q % 3: this warp writes and then reads only
+      // its own slabs' columns (warps of the other quarters write the same values).  A warp
+      // writes it before waiting for the accumulator, so a fast warp writes tile q's row
+      // while a slow one may still read tile q - 2's (the MMA lane refills an accumulator only
+      // after every warp has released it, so no warp is three tiles ahead of another): three
+      // row buffers keep those apart.
+      float* t0s = sT0 + (q % 3) * BN;
 #pragma unroll
       for (int k = 0; k < NSL; ++k) t0s[(half + 2 * k) * 32 + lane] = t0c[k];
       __syncwarp();
