@@ -134,9 +134,10 @@ def test_host_buffer_pipeline_matches_device_path(ctx, L, quasar, prec, chunk):
     assert R.rel_l2(host[17], ref) < (TOL_MIXED if prec == "mixed" else 1e-5)
 
 
-def test_mixed_images_are_deterministic(L, quasar):
-    """A fresh context images 256 masks of 1024^2 (four masks repeated): every copy of a mask
-    gives the same image bit for bit, within the first call and across calls.  (A DC row of
+@pytest.mark.parametrize("prec_name", ["mixed", "plain"])
+def test_images_are_deterministic(L, quasar, prec_name):
+    """A fresh context images 256 masks of 1024^2 (four masks repeated) in each form: every
+    copy of a mask gives the same image bit for bit, within the first call and across calls.  (A DC row of
     the FI contraction's epilogue once raced with a warp two tiles ahead and corrupted a
     32 x 32 slab of the first call.)"""
     import torch
@@ -148,11 +149,12 @@ def test_mixed_images_are_deterministic(L, quasar):
         m = torch.from_numpy(np.stack([synth.density_rect_mask(1024, 0.3 + 0.001 * i, seed=200 + i)
                                        for i in range(4)]).astype(np.float32)).cuda().repeat(64, 1, 1)
         torch.cuda.synchronize()  # the context images on its own stream
-        first = c.image_batch(ks, m, precision=L.PREC_MIXED)
+        prec = L.PREC_MIXED if prec_name == "mixed" else L.PREC_FP32
+        first = c.image_batch(ks, m, precision=prec)
         c.synchronize()
         for i in range(4, 256):
             assert torch.equal(first[i], first[i % 4]), i
-        again = c.image_batch(ks, m, precision=L.PREC_MIXED)
+        again = c.image_batch(ks, m, precision=prec)
         c.synchronize()
         assert torch.equal(first, again)
         ks.close()
